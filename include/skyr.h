@@ -1,0 +1,173 @@
+/*
+ * skyr.h — C ABI of the GB300-native atmosphere-LUT / volumetric-cloud hot path.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int status (SKYR_OK on success) and never throws.  Device buffers are owned by
+ * the caller; their layouts are documented beside each call.  One skyr_ctx is
+ * bound to one CUDA stream; calls on one context are ordered by that stream.
+ * A context is not thread-safe; separate contexts are independent.
+ *
+ * Units follow the reference: lengths in km, extinction in 1/km, angles in
+ * degrees in parameter structs.  Images are row-major with x fastest:
+ * texel (x, y, z) of a W x H x D image with C channels is at
+ * ((z * H + y) * W + x) * C.
+ *
+ * The comment on each declaration names the reference interface it replaces
+ * (file:line within the c52e/SkyRendering project).
+ */
+#ifndef SKYR_H_
+#define SKYR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SKYR_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define SKYR_OK 0
+#define SKYR_EINVAL 1   /* bad argument (null pointer, size out of range, NaN parameter) */
+#define SKYR_ENOMEM 2   /* device or host allocation failed */
+#define SKYR_ECUDA 3    /* a CUDA runtime call failed */
+#define SKYR_ETIMEOUT 4 /* a bounded device-side wait gave up */
+#define SKYR_ENOTSUP 5  /* combination not supported */
+
+/* ---- storage formats of LUT outputs ----------------------------------- */
+#define SKYR_FORMAT_RGBA32F 0 /* float4 per texel (reference GL_RGBA32F) */
+#define SKYR_FORMAT_RGBA16F 1 /* half4 per texel */
+
+typedef struct skyr_ctx skyr_ctx;
+
+/* Version of this ABI (SKYR_ABI_VERSION of the built library). */
+int skyr_abi_version(void);
+
+/* Human-readable name of a status code; static storage. */
+const char* skyr_status_string(int status);
+
+/* Message of the last failed call on this host thread; static thread-local storage. */
+const char* skyr_last_error(void);
+
+/* sizeof() of the public structs, for binding layout checks:
+ * 0 skyr_atmosphere_parameters, 1 skyr_atmosphere_render_parameters,
+ * 2 skyr_lut_sizes; further ids are listed beside later structs.
+ * Returns 0 for an unknown id.  (No reference counterpart: ABI hygiene.) */
+size_t skyr_struct_size(int which);
+
+/* Create a context bound to `cuda_stream` (a cudaStream_t; NULL = legacy default
+ * stream) on the current CUDA device.
+ * Replaces the GL-context ownership of Atmosphere/AtmosphereRenderer/VolumetricCloud
+ * (src/SkyRendering/Atmosphere.cpp:43-70, src/SkyRendering/VolumetricCloud.cpp:54-113). */
+int skyr_ctx_create(void* cuda_stream, skyr_ctx** out_ctx);
+int skyr_ctx_destroy(skyr_ctx* ctx);
+/* Block the host until all work queued on the context's stream is done. */
+int skyr_ctx_synchronize(skyr_ctx* ctx);
+
+/* ======================================================================== */
+/* Atmosphere                                                                */
+/* ======================================================================== */
+
+/* User-unit atmosphere description; same fields, units and defaults as
+ * AtmosphereParameters (src/SkyRendering/Atmosphere.h:10-38) and the
+ * "earth_.parameters" block of bin/config.json:62-108. */
+typedef struct skyr_atmosphere_parameters {
+    float solar_illuminance[3];
+    float sun_angular_radius; /* degrees */
+    float bottom_radius;      /* km */
+    float thickness;          /* km; top radius = bottom_radius + thickness */
+    float ground_albedo[3];
+    float rayleigh_exponential_distribution; /* km */
+    float rayleigh_scattering_scale;         /* 1/km */
+    float rayleigh_scattering[3];
+    float mie_exponential_distribution; /* km */
+    float mie_phase_g;
+    float mie_scattering_scale; /* 1/km */
+    float mie_scattering[3];
+    float mie_absorption_scale; /* 1/km */
+    float mie_absorption[3];
+    float ozone_center_altitude; /* km */
+    float ozone_width;           /* km */
+    float ozone_absorption_scale; /* 1/km */
+    float ozone_absorption[3];
+    float transmittance_steps;
+    float multiscattering_steps;
+    float multiscattering_mask; /* 0..1 */
+} skyr_atmosphere_parameters;
+
+/* Fill `p` with the reference defaults (src/SkyRendering/Atmosphere.h:13-38). */
+int skyr_atmosphere_parameters_default(skyr_atmosphere_parameters* p);
+
+/* View-dependent part of AtmosphereRenderParameters
+ * (src/SkyRendering/AtmosphereRenderer.h:12-35) plus the camera inputs that
+ * AtmosphereRenderer::Render derives its frame from
+ * (src/SkyRendering/AtmosphereRenderer.cpp:52-83). */
+typedef struct skyr_atmosphere_render_parameters {
+    float sun_direction_theta; /* zenith angle, degrees */
+    float sun_direction_phi;   /* azimuth, degrees */
+    float sky_view_lut_steps;
+    float aerial_perspective_lut_steps;
+    float aerial_perspective_lut_max_distance; /* km */
+    float camera_position[3];  /* world space, y up, km; Earth centre at (0, -bottom_radius, 0) */
+    float view_projection[16]; /* column-major (glm::mat4 memory order) */
+} skyr_atmosphere_render_parameters;
+
+/* Sizes of every LUT.  Reference sizes: transmittance 256x64
+ * (src/SkyRendering/Atmosphere.cpp:9-15), multi-scattering 32x32 (:17-19),
+ * sky-view 128x128 (src/SkyRendering/AtmosphereRenderer.cpp:15-17),
+ * aerial perspective 32x32xdepth (:19-21, depth from
+ * AtmosphereRenderInitParameters::aerial_perspective_lut_depth). */
+typedef struct skyr_lut_sizes {
+    int transmittance_width, transmittance_height;
+    int multiscattering_width, multiscattering_height;
+    int sky_view_width, sky_view_height;
+    int aerial_perspective_width, aerial_perspective_height, aerial_perspective_depth;
+    int format; /* SKYR_FORMAT_* of the multi-scattering, sky-view and AP outputs;
+                   the transmittance LUT is always RGBA32F (grazing-ray
+                   transmittance falls below the FP16 normal range). */
+} skyr_lut_sizes;
+
+/* Bytes of one LUT of `kind` (SKYR_LUT_*) for one parameter set. */
+#define SKYR_LUT_TRANSMITTANCE 0
+#define SKYR_LUT_MULTISCATTERING 1
+#define SKYR_LUT_SKY_VIEW 2
+#define SKYR_LUT_AERIAL_PERSPECTIVE 3
+size_t skyr_lut_bytes(const skyr_lut_sizes* sizes, int kind);
+
+/* Atmosphere::UpdateLuts (src/SkyRendering/Atmosphere.cpp:101-124):
+ * regenerate the transmittance and multi-scattering LUTs of `n_sets`
+ * parameter sets.  Outputs are device buffers holding n_sets consecutive LUTs:
+ *   transmittance   : RGBA32F, rgb = T to the top boundary, a = 1
+ *   multiscattering : `sizes->format`, rgb = Psi_ms, a = 1              */
+int skyr_update_luts(skyr_ctx* ctx, const skyr_atmosphere_parameters* params, int n_sets,
+                     const skyr_lut_sizes* sizes, void* transmittance, void* multiscattering);
+
+/* The SKY_VIEW and AERIAL_PERSPECTIVE passes of AtmosphereRenderer::Render
+ * (src/SkyRendering/AtmosphereRenderer.cpp:221-233,
+ *  shaders/SkyRendering/AtmosphereRenderer.glsl:147-245) for `n_sets` views;
+ * view i uses params[i], render[i] and the i-th transmittance /
+ * multi-scattering LUT.  Outputs (device, n_sets consecutive images):
+ *   sky_view_luminance, sky_view_transmittance        : W x H, a = 0
+ *   aerial_perspective_luminance, ..._transmittance   : W x H x D, a = 0  */
+int skyr_render_view_luts(skyr_ctx* ctx, const skyr_atmosphere_parameters* params,
+                          const skyr_atmosphere_render_parameters* render, int n_sets,
+                          const skyr_lut_sizes* sizes, const void* transmittance,
+                          const void* multiscattering, void* sky_view_luminance,
+                          void* sky_view_transmittance, void* aerial_perspective_luminance,
+                          void* aerial_perspective_transmittance);
+
+/* The whole LUT set of Earth::Update + the LUT passes of AtmosphereRenderer::Render
+ * for `n_sets` (parameter set, view) pairs in one stream-ordered launch sequence:
+ * transmittance -> multi-scattering -> {sky-view, aerial perspective}.
+ * Same buffers and layouts as the two calls above. */
+int skyr_update_lut_set(skyr_ctx* ctx, const skyr_atmosphere_parameters* params,
+                        const skyr_atmosphere_render_parameters* render, int n_sets,
+                        const skyr_lut_sizes* sizes, void* transmittance, void* multiscattering,
+                        void* sky_view_luminance, void* sky_view_transmittance,
+                        void* aerial_perspective_luminance, void* aerial_perspective_transmittance);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SKYR_H_ */

@@ -1,0 +1,164 @@
+"""ctypes mirror of include/skyr.h and loader of the in-tree libskyr.so.
+
+There is no fallback: if libskyr.so is missing or cannot be loaded, every call
+raises.  The structs below must match include/skyr.h field for field; the
+layout is checked against ``skyr_struct_size`` at load time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libskyr.so"
+
+SKYR_OK, SKYR_EINVAL, SKYR_ENOMEM, SKYR_ECUDA, SKYR_ETIMEOUT, SKYR_ENOTSUP = range(6)
+SKYR_FORMAT_RGBA32F, SKYR_FORMAT_RGBA16F = 0, 1
+SKYR_LUT_TRANSMITTANCE, SKYR_LUT_MULTISCATTERING, SKYR_LUT_SKY_VIEW, SKYR_LUT_AERIAL_PERSPECTIVE = range(4)
+
+f3 = C.c_float * 3
+f16 = C.c_float * 16
+
+
+class AtmosphereParameters(C.Structure):
+    """skyr_atmosphere_parameters (AtmosphereParameters, src/SkyRendering/Atmosphere.h:10-38)."""
+
+    _fields_ = [
+        ("solar_illuminance", f3),
+        ("sun_angular_radius", C.c_float),
+        ("bottom_radius", C.c_float),
+        ("thickness", C.c_float),
+        ("ground_albedo", f3),
+        ("rayleigh_exponential_distribution", C.c_float),
+        ("rayleigh_scattering_scale", C.c_float),
+        ("rayleigh_scattering", f3),
+        ("mie_exponential_distribution", C.c_float),
+        ("mie_phase_g", C.c_float),
+        ("mie_scattering_scale", C.c_float),
+        ("mie_scattering", f3),
+        ("mie_absorption_scale", C.c_float),
+        ("mie_absorption", f3),
+        ("ozone_center_altitude", C.c_float),
+        ("ozone_width", C.c_float),
+        ("ozone_absorption_scale", C.c_float),
+        ("ozone_absorption", f3),
+        ("transmittance_steps", C.c_float),
+        ("multiscattering_steps", C.c_float),
+        ("multiscattering_mask", C.c_float),
+    ]
+
+
+class AtmosphereRenderParameters(C.Structure):
+    """skyr_atmosphere_render_parameters (src/SkyRendering/AtmosphereRenderer.h:12-35)."""
+
+    _fields_ = [
+        ("sun_direction_theta", C.c_float),
+        ("sun_direction_phi", C.c_float),
+        ("sky_view_lut_steps", C.c_float),
+        ("aerial_perspective_lut_steps", C.c_float),
+        ("aerial_perspective_lut_max_distance", C.c_float),
+        ("camera_position", f3),
+        ("view_projection", f16),
+    ]
+
+
+class LutSizes(C.Structure):
+    """skyr_lut_sizes."""
+
+    _fields_ = [
+        ("transmittance_width", C.c_int),
+        ("transmittance_height", C.c_int),
+        ("multiscattering_width", C.c_int),
+        ("multiscattering_height", C.c_int),
+        ("sky_view_width", C.c_int),
+        ("sky_view_height", C.c_int),
+        ("aerial_perspective_width", C.c_int),
+        ("aerial_perspective_height", C.c_int),
+        ("aerial_perspective_depth", C.c_int),
+        ("format", C.c_int),
+    ]
+
+
+# struct id (skyr_struct_size) -> ctypes type; extended by later modules
+STRUCT_IDS: dict[int, type] = {0: AtmosphereParameters, 1: AtmosphereRenderParameters, 2: LutSizes}
+
+P = C.c_void_p
+_SIGNATURES = {
+    "skyr_abi_version": (C.c_int, []),
+    "skyr_status_string": (C.c_char_p, [C.c_int]),
+    "skyr_last_error": (C.c_char_p, []),
+    "skyr_struct_size": (C.c_size_t, [C.c_int]),
+    "skyr_ctx_create": (C.c_int, [P, C.POINTER(P)]),
+    "skyr_ctx_destroy": (C.c_int, [P]),
+    "skyr_ctx_synchronize": (C.c_int, [P]),
+    "skyr_atmosphere_parameters_default": (C.c_int, [C.POINTER(AtmosphereParameters)]),
+    "skyr_lut_bytes": (C.c_size_t, [C.POINTER(LutSizes), C.c_int]),
+    "skyr_update_luts": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.c_int, C.POINTER(LutSizes), P, P]),
+    "skyr_render_view_luts": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(AtmosphereRenderParameters),
+                                        C.c_int, C.POINTER(LutSizes), P, P, P, P, P, P]),
+    "skyr_update_lut_set": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(AtmosphereRenderParameters),
+                                      C.c_int, C.POINTER(LutSizes), P, P, P, P, P, P]),
+}
+
+_lib = None
+
+
+class SkyrError(RuntimeError):
+    def __init__(self, status: int, where: str, message: str):
+        self.status = status
+        super().__init__(f"{where}: {status_name(status)}: {message}")
+
+
+def register(signatures: dict) -> None:
+    """Add signatures of entry points declared by later modules of skyr.h."""
+    _SIGNATURES.update(signatures)
+    if _lib is not None:
+        _bind(_lib, signatures)
+
+
+def _bind(lib, sigs):
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)  # AttributeError: symbol missing from the build
+        fn.restype = res
+        fn.argtypes = args
+
+
+def lib():
+    """The loaded libskyr.so; raises if it is missing (no fallback path)."""
+    global _lib
+    if _lib is None:
+        path = Path(os.environ.get("SKYR_LIB", LIB_PATH))
+        if not path.exists():
+            raise RuntimeError(
+                f"{path} not found: build the CUDA extension first "
+                "(python -c 'import __graft_entry__ as g; g.build()')")
+        lb = C.CDLL(str(path))
+        _bind(lb, _SIGNATURES)
+        for sid, st in STRUCT_IDS.items():
+            n = lb.skyr_struct_size(sid)
+            if n != C.sizeof(st):
+                raise RuntimeError(f"ABI mismatch: {st.__name__} is {C.sizeof(st)} bytes in Python, {n} in C")
+        _lib = lb
+    return _lib
+
+
+def status_name(status: int) -> str:
+    try:
+        return lib().skyr_status_string(status).decode()
+    except Exception:  # pragma: no cover - only when the library itself is missing
+        return str(status)
+
+
+def check(status: int, where: str) -> None:
+    if status != SKYR_OK:
+        msg = lib().skyr_last_error().decode(errors="replace")
+        raise SkyrError(status, where, msg)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib(), name)(*args), name)
+
+
+def exported_symbols() -> list[str]:
+    return sorted(_SIGNATURES)

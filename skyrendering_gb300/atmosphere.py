@@ -1,0 +1,146 @@
+"""Host-side mirror of the reference's atmosphere classes over the C ABI.
+
+* ``Atmosphere.update_luts`` ~ Atmosphere::UpdateLuts
+  (src/SkyRendering/Atmosphere.cpp:101-124): transmittance + multi-scattering.
+* ``AtmosphereRenderer.render_luts`` ~ the SKY_VIEW / AERIAL_PERSPECTIVE passes
+  of AtmosphereRenderer::Render (src/SkyRendering/AtmosphereRenderer.cpp:164-233).
+* ``update_lut_set`` runs both for one or many (parameter set, view) pairs.
+
+Device memory comes from torch (plumbing only); every kernel is a libskyr.so
+kernel.  Errors raise ``SkyrError`` carrying the C status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import torch
+
+from . import _abi
+
+
+class Context:
+    """A skyr_ctx bound to a CUDA stream (default: torch's current stream)."""
+
+    def __init__(self, stream: torch.cuda.Stream | None = None, device: int | None = None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("skyrendering_gb300 requires a CUDA device")
+        if device is not None:
+            torch.cuda.set_device(device)
+        self.stream = stream if stream is not None else torch.cuda.current_stream()
+        self._ctx = C.c_void_p()
+        _abi.call("skyr_ctx_create", C.c_void_p(self.stream.cuda_stream), C.byref(self._ctx))
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._ctx
+
+    def synchronize(self) -> None:
+        _abi.call("skyr_ctx_synchronize", self._ctx)
+
+    def close(self) -> None:
+        if self._ctx:
+            _abi.call("skyr_ctx_destroy", self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):  # best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ptr(t: torch.Tensor | None) -> C.c_void_p:
+    return C.c_void_p(0 if t is None else t.data_ptr())
+
+
+def texel_channels(fmt: int):
+    return (torch.float16, 4) if fmt == _abi.SKYR_FORMAT_RGBA16F else (torch.float32, 4)
+
+
+@dataclass
+class LutSet:
+    """Device LUTs of n parameter sets, shaped (n, [D,] H, W, 4)."""
+
+    transmittance: torch.Tensor
+    multiscattering: torch.Tensor
+    sky_view_luminance: torch.Tensor | None = None
+    sky_view_transmittance: torch.Tensor | None = None
+    aerial_perspective_luminance: torch.Tensor | None = None
+    aerial_perspective_transmittance: torch.Tensor | None = None
+
+    @staticmethod
+    def allocate(sizes: _abi.LutSizes, n: int = 1, views: bool = True, device="cuda") -> "LutSet":
+        dt, c = texel_channels(sizes.format)
+        t = torch.empty((n, sizes.transmittance_height, sizes.transmittance_width, 4), dtype=torch.float32,
+                        device=device)
+        ms = torch.empty((n, sizes.multiscattering_height, sizes.multiscattering_width, c), dtype=dt, device=device)
+        out = LutSet(t, ms)
+        if views:
+            out.sky_view_luminance = torch.empty((n, sizes.sky_view_height, sizes.sky_view_width, c), dtype=dt,
+                                                 device=device)
+            out.sky_view_transmittance = torch.empty_like(out.sky_view_luminance)
+            shape = (n, sizes.aerial_perspective_depth, sizes.aerial_perspective_height,
+                     sizes.aerial_perspective_width, c)
+            out.aerial_perspective_luminance = torch.empty(shape, dtype=dt, device=device)
+            out.aerial_perspective_transmittance = torch.empty_like(out.aerial_perspective_luminance)
+        return out
+
+
+def _as_array(items, ctype):
+    if isinstance(items, ctype):
+        arr = (ctype * 1)()
+        arr[0] = items
+        return arr, 1
+    if isinstance(items, C.Array):
+        return items, len(items)
+    arr = (ctype * len(items))(*items)
+    return arr, len(items)
+
+
+class Atmosphere:
+    """Atmosphere (src/SkyRendering/Atmosphere.h:70-92)."""
+
+    def __init__(self, ctx: Context, sizes: _abi.LutSizes):
+        self.ctx, self.sizes = ctx, sizes
+
+    def update_luts(self, params, out: LutSet | None = None) -> LutSet:
+        arr, n = _as_array(params, _abi.AtmosphereParameters)
+        out = out or LutSet.allocate(self.sizes, n, views=False)
+        _abi.call("skyr_update_luts", self.ctx.handle, arr, n, C.byref(self.sizes), _ptr(out.transmittance),
+                  _ptr(out.multiscattering))
+        return out
+
+
+class AtmosphereRenderer:
+    """LUT passes of AtmosphereRenderer (src/SkyRendering/AtmosphereRenderer.h:86-132)."""
+
+    def __init__(self, ctx: Context, sizes: _abi.LutSizes):
+        self.ctx, self.sizes = ctx, sizes
+
+    def render_luts(self, params, render, luts: LutSet) -> LutSet:
+        pa, n = _as_array(params, _abi.AtmosphereParameters)
+        ra, m = _as_array(render, _abi.AtmosphereRenderParameters)
+        if n != m:
+            raise ValueError("one render parameter block per atmosphere parameter set")
+        if luts.sky_view_luminance is None:
+            full = LutSet.allocate(self.sizes, n, views=True)
+            full.transmittance, full.multiscattering = luts.transmittance, luts.multiscattering
+            luts = full
+        _abi.call("skyr_render_view_luts", self.ctx.handle, pa, ra, n, C.byref(self.sizes),
+                  _ptr(luts.transmittance), _ptr(luts.multiscattering), _ptr(luts.sky_view_luminance),
+                  _ptr(luts.sky_view_transmittance), _ptr(luts.aerial_perspective_luminance),
+                  _ptr(luts.aerial_perspective_transmittance))
+        return luts
+
+
+def update_lut_set(ctx: Context, params, render, sizes: _abi.LutSizes, out: LutSet | None = None) -> LutSet:
+    pa, n = _as_array(params, _abi.AtmosphereParameters)
+    ra, m = _as_array(render, _abi.AtmosphereRenderParameters)
+    if n != m:
+        raise ValueError("one render parameter block per atmosphere parameter set")
+    out = out or LutSet.allocate(sizes, n, views=True)
+    _abi.call("skyr_update_lut_set", ctx.handle, pa, ra, n, C.byref(sizes), _ptr(out.transmittance),
+              _ptr(out.multiscattering), _ptr(out.sky_view_luminance), _ptr(out.sky_view_transmittance),
+              _ptr(out.aerial_perspective_luminance), _ptr(out.aerial_perspective_transmittance))
+    return out

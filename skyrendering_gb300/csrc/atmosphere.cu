@@ -1,0 +1,524 @@
+// atmosphere.cu — transmittance, multi-scattering, sky-view and
+// aerial-perspective LUT kernels for sm_103a.
+//
+// Semantics follow shaders/SkyRendering/Atmosphere.glsl and
+// shaders/SkyRendering/AtmosphereRenderer.glsl of c52e/SkyRendering; the
+// arithmetic is reorganised for the GPU:
+//  * every radius difference (r^2 - R^2, top - r) is carried from an exact
+//    source instead of being formed by cancellation in FP32;
+//  * the samples of one ray are split over a group of LANES lanes, each lane
+//    integrating a contiguous chunk, and the chunks are composed with the
+//    associative rule (L_a, T_a) o (L_b, T_b) = (L_a + T_a L_b, T_a T_b)
+//    through warp shuffles;
+//  * the multi-scattering texel is one warp (64 sphere directions, two per
+//    lane) reduced with shuffles instead of a shared-memory tree.
+#include "skyr_internal.cuh"
+#include "atmosphere_kernels.cuh"
+
+namespace skyr {
+
+// ---------------------------------------------------------------------------
+// LUT storage access
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float3 load_rgb(const float4* p, int i) {
+    float4 v = __ldg(p + i);
+    return f3(v.x, v.y, v.z);
+}
+__device__ __forceinline__ float3 load_rgb(const __half2* p, int i) {  // half4 = 2 x half2
+    uint2 raw = __ldg(reinterpret_cast<const uint2*>(p) + i);
+    __half2 a = *reinterpret_cast<__half2*>(&raw.x);
+    __half2 b = *reinterpret_cast<__half2*>(&raw.y);
+    float2 fa = __half22float2(a), fb = __half22float2(b);
+    return f3(fa.x, fa.y, fb.x);
+}
+__device__ __forceinline__ void store_rgba(float4* p, size_t i, float3 v, float a) {
+    p[i] = make_float4(v.x, v.y, v.z, a);
+}
+__device__ __forceinline__ void store_rgba(__half2* p, size_t i, float3 v, float a) {
+    __half2 lo = __floats2half2_rn(v.x, v.y), hi = __floats2half2_rn(v.z, a);
+    uint2 raw;
+    raw.x = *reinterpret_cast<uint32_t*>(&lo);
+    raw.y = *reinterpret_cast<uint32_t*>(&hi);
+    reinterpret_cast<uint2*>(p)[i] = raw;
+}
+
+// GL LINEAR + CLAMP_TO_EDGE fetch at continuous texel coordinate (x, y) =
+// (u*W - 0.5, v*H - 0.5).
+template <class S>
+__device__ __forceinline__ float3 bilinear_clamp(const S* lut, int w, int h, float x, float y) {
+    float fx = floorf(x), fy = floorf(y);
+    float a = x - fx, b = y - fy;
+    int x0 = (int)fx, y0 = (int)fy;
+    int x1 = min(max(x0 + 1, 0), w - 1), y1 = min(max(y0 + 1, 0), h - 1);
+    x0 = min(max(x0, 0), w - 1);
+    y0 = min(max(y0, 0), h - 1);
+    float3 t00 = load_rgb(lut, y0 * w + x0), t10 = load_rgb(lut, y0 * w + x1);
+    float3 t01 = load_rgb(lut, y1 * w + x0), t11 = load_rgb(lut, y1 * w + x1);
+    float3 top = t00 + (t10 - t00) * a;
+    float3 bot = t01 + (t11 - t01) * a;
+    return top + (bot - top) * b;
+}
+
+struct LutView {
+    const float4* t;
+    int tw, th;
+};
+
+// GetTransmittanceToTopAtmosphereBoundary x horizon smoothstep = GetSunVisibility
+// (Atmosphere.glsl:90-117) at a point of radius r with rho2 = r^2 - R^2 and
+// altitude h = r - R.
+__device__ __forceinline__ float3 sun_visibility(const AtmoConsts& A, const LutView& L, float r, float inv_r,
+                                                 float rho2, float h, float mu_s) {
+    float rho = sqrtf(fmaxf(rho2, 0.f));
+    float d_min = A.thickness - h;
+    float d = dist_to_top(r, d_min, A.top, mu_s);
+    float d_max = rho + A.Hh;
+    float x_mu = __fdividef(d - d_min, d_max - d_min);
+    float x_r = rho * A.inv_Hh;
+    float3 t = bilinear_clamp(L.t, L.tw, L.th, x_mu * (float)(L.tw - 1), x_r * (float)(L.th - 1));
+    // smoothstep(-e, e, mu_s - cos_h) with e = (R / r) alpha and cos_h = -rho / r:
+    // the normalised argument is 1/2 + (mu_s r + rho) / (2 R alpha)
+    float u = clamp01(fmaf(fmaf(mu_s, r, rho), A.inv_2R_alpha, 0.5f));
+    (void)inv_r;
+    return t * (u * u * (3.f - 2.f * u));
+}
+
+// GetMultiscatteringContribution (Atmosphere.glsl:169-178)
+template <class S>
+__device__ __forceinline__ float3 ms_contribution(const AtmoConsts& A, const S* ms, int mw, int mh, float h,
+                                                  float mu_s) {
+    float x_mu_s = mu_s * 0.5f + 0.5f;
+    float x_r = h * A.inv_thickness;
+    return bilinear_clamp(ms, mw, mh, x_mu_s * (float)(mw - 1), x_r * (float)(mh - 1));
+}
+
+// GetExtinction / GetScattering (Atmosphere.glsl:119-132,156-159)
+__device__ __forceinline__ void medium(const AtmoConsts& A, float h, float3& ray_s, float3& mie_s, float3& ext) {
+    float er = clamp01(__expf(-h * A.inv_rayleigh_h));
+    float em = clamp01(__expf(-h * A.inv_mie_h));
+    float dz = h - A.ozone_center;
+    float oz = fmaxf(0.f, h < A.ozone_center ? 1.f + dz * A.inv_ozone_width : 1.f - dz * A.inv_ozone_width);
+    ray_s = A.rayleigh_scattering * er;
+    mie_s = A.mie_scattering * em;
+    ext = ray_s + A.mie_extinction * em + A.ozone_absorption * oz;
+}
+
+// Number of samples of `for (float i = start; i < steps; ++i)`.
+__device__ __forceinline__ int sample_count(float start, float steps) {
+    float c = ceilf(steps - start);
+    return c > 0.f ? (int)c : 0;
+}
+
+// State at the start of a ray segment.
+struct RayStart {
+    float r, h, rho2;  // radius, altitude, r^2 - R^2
+    float mu;          // cos(view, up)
+    float mu_s;        // cos(sun, up)
+    float nu;          // cos(view, sun)
+};
+
+// Compose (L, T) pairs of LANES consecutive lanes, earliest chunk first; the
+// group leader ends with the whole-ray result.
+template <int LANES>
+__device__ __forceinline__ void compose_lanes(float3& L, float3& T, float3* Lf) {
+#pragma unroll
+    for (int o = 1; o < LANES; o <<= 1) {
+        float3 Lp, Tp, Fp;
+        Lp.x = __shfl_down_sync(0xffffffffu, L.x, o);
+        Lp.y = __shfl_down_sync(0xffffffffu, L.y, o);
+        Lp.z = __shfl_down_sync(0xffffffffu, L.z, o);
+        Tp.x = __shfl_down_sync(0xffffffffu, T.x, o);
+        Tp.y = __shfl_down_sync(0xffffffffu, T.y, o);
+        Tp.z = __shfl_down_sync(0xffffffffu, T.z, o);
+        if (Lf) {
+            Fp.x = __shfl_down_sync(0xffffffffu, Lf->x, o);
+            Fp.y = __shfl_down_sync(0xffffffffu, Lf->y, o);
+            Fp.z = __shfl_down_sync(0xffffffffu, Lf->z, o);
+        }
+        L = L + T * Lp;
+        if (Lf) *Lf = *Lf + T * Fp;
+        T = T * Tp;
+    }
+}
+
+// ComputeScatteredLuminance (Atmosphere.glsl:220-295) over samples
+// [k0, k1) of a ray with `n` samples starting at index `start_i`.
+// MS = the MULTISCATTERING_COMPUTE_PROGRAM variant.
+template <bool MS, class S>
+__device__ __forceinline__ void integrate(const AtmoConsts& A, const LutView& L, const S* ms, int mw, int mh,
+                                          const RayStart& s0, float dx, float start_i, int k0, int k1, float ph_r,
+                                          float ph_m, float3& lum, float3& trans, float3& lf) {
+    lum = f3(0.f);
+    trans = f3(1.f);
+    lf = f3(0.f);
+    float b = 2.f * s0.r * s0.mu;
+    float rms = s0.r * s0.mu_s;
+    for (int k = k0; k < k1; ++k) {
+        float d = ((float)k + start_i) * dx;
+        float s = fmaf(d, b + d, s0.rho2);  // r_i^2 - R^2
+        float r2 = A.R2 + s;
+        float inv_r = rsqrtf(r2);
+        float r_i = r2 * inv_r;
+        float h_i = __fdividef(s, r_i + A.R);
+        float mu_s_i = fmaf(d, s0.nu, rms) * inv_r;
+        float3 ray_s, mie_s, ext;
+        medium(A, h_i, ray_s, mie_s, ext);
+        float3 tr_i, phi;
+        phi.x = seg_phi(ext.x * dx, tr_i.x);
+        phi.y = seg_phi(ext.y * dx, tr_i.y);
+        phi.z = seg_phi(ext.z * dx, tr_i.z);
+        float3 sv = sun_visibility(A, L, r_i, inv_r, s, h_i, mu_s_i);
+        float3 li = (ray_s * ph_r + mie_s * ph_m) * sv;
+        float3 sc = ray_s + mie_s;
+        if constexpr (!MS) {
+            float3 m = ms_contribution(A, ms, mw, mh, h_i, mu_s_i);
+            li = (li + m * sc * A.ms_mask) * A.solar_illuminance;
+        }
+        // (L - L T_i) / ext = L dx phi(ext dx)
+        float3 w = trans * phi * dx;
+        lum += li * w;
+        if constexpr (MS) lf += sc * w;
+        trans = trans * tr_i;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// TRANSMITTANCE (Atmosphere.glsl:309-337): LANES lanes per texel.
+// ---------------------------------------------------------------------------
+template <int LANES, bool TABLE>
+__global__ void __launch_bounds__(128) transmittance_kernel(JobSrc<TABLE> jobs, int n_sets, int w, int h,
+                                                            float4* __restrict__ out) {
+    int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    int lane = gid % LANES;
+    int texel = gid / LANES;
+    int per_set = w * h;
+    int set = texel / per_set;
+    bool valid = set < n_sets;
+    if (!valid) set = n_sets - 1;  // keep the warp converged for the shuffles
+    int t = texel % per_set;
+    const AtmoConsts& A = jobs.get(set).a;
+    int ix = t % w, iy = t / w;
+    // GetRMuFromTransmittanceTextureIndex (Atmosphere.glsl:71-88), with
+    // rho^2 = r^2 - R^2 and 2 r mu = (H^2 - rho^2 - d^2) / d kept exact.
+    float x_mu = (float)ix / (float)(w - 1);
+    float x_r = (float)iy / (float)(h - 1);
+    float rho = A.Hh * x_r;
+    float rho2 = rho * rho;
+    float r = sqrtf(rho2 + A.R2);
+    float alt = rho2 / (r + A.R);
+    float d_min = A.thickness - alt;
+    float d_max = rho + A.Hh;
+    float d = d_min + x_mu * (d_max - d_min);
+    float b = d == 0.f ? 2.f * r : (A.top2_minus_R2 - rho2 - d * d) / d;  // 2 r mu
+    b = fminf(fmaxf(b, -2.f * r), 2.f * r);                               // ClampCosine
+    float mu = b / (2.f * r);
+    float dist = dist_to_top(r, d_min, A.top, mu);
+    float steps = A.transmittance_steps;
+    float dx = dist / steps;
+    int n = sample_count(0.5f, steps);
+    int k0 = (n * lane) / LANES, k1 = (n * (lane + 1)) / LANES;
+    // optical length, Kahan-compensated per channel
+    float3 sum = f3(0.f), comp = f3(0.f);
+    for (int k = k0; k < k1; ++k) {
+        float di = ((float)k + 0.5f) * dx;
+        float s = fmaf(di, b + di, rho2);
+        float r_i = sqrtf(A.R2 + s);
+        float h_i = s / (r_i + A.R);
+        float3 ray_s, mie_s, ext;
+        medium(A, h_i, ray_s, mie_s, ext);
+        float3 y = ext * dx - comp;
+        float3 tt = sum + y;
+        comp = (tt - sum) - y;
+        sum = tt;
+    }
+#pragma unroll
+    for (int o = 1; o < LANES; o <<= 1) {
+        sum.x += __shfl_down_sync(0xffffffffu, sum.x, o);
+        sum.y += __shfl_down_sync(0xffffffffu, sum.y, o);
+        sum.z += __shfl_down_sync(0xffffffffu, sum.z, o);
+    }
+    if (valid && lane == 0) {
+        float3 T = f3(expf(-sum.x), expf(-sum.y), expf(-sum.z));
+        store_rgba(out, (size_t)set * per_set + t, T, 1.f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// MULTISCATTERING (Atmosphere.glsl:342-438): one 256-thread block per texel.
+// Thread t integrates chunk (t % MS_CHUNKS) of sphere direction t / MS_CHUNKS
+// (GetDirectionFromLocalIndex, :344-355); the chunks of a direction are
+// composed through shuffles, the 64 directions summed through shuffles and a
+// shared-memory pass over the block's warps.
+// ---------------------------------------------------------------------------
+constexpr int kMsChunks = 4;
+constexpr int kMsThreads = 64 * kMsChunks;
+
+template <class S, bool TABLE>
+__global__ void __launch_bounds__(kMsThreads) multiscattering_kernel(JobSrc<TABLE> jobs, int n_sets, LutView L,
+                                                                     int tstride, int w, int h,
+                                                                     S* __restrict__ out) {
+    __shared__ float red[kMsThreads / 32][6];
+    int texel = blockIdx.x;
+    int per_set = w * h;
+    int set = texel / per_set;
+    int t = texel % per_set;
+    const AtmoConsts& A = jobs.get(set).a;
+    LutView Ls = L;
+    Ls.t = L.t + (size_t)set * tstride;
+    int ix = t % w, iy = t / w;
+    float x_mu_s = (float)ix / (float)(w - 1);
+    float x_alt = (float)iy / (float)(h - 1);
+    float alt = x_alt * A.thickness;
+    float mu_s = x_mu_s * 2.f - 1.f;
+    float sun_z = sqrtf(1.f - mu_s * mu_s);
+    float r = alt + A.R;
+    float rho2 = alt * (2.f * A.R + alt);
+    float steps = A.multiscattering_steps;
+    int n = sample_count(0.5f, steps);
+    const float iso = 1.f / (4.f * SKYR_PI);
+
+    int index = threadIdx.x / kMsChunks;
+    int chunk = threadIdx.x % kMsChunks;
+    float unit_theta = (0.5f + (float)(index / 8)) / 8.f;
+    float unit_phi = (0.5f + (float)(index % 8)) / 8.f;
+    float cos_theta = 1.f - 2.f * unit_theta;
+    float sin_theta = sqrtf(clamp01(1.f - cos_theta * cos_theta));
+    float sphi, cphi;
+    sincospif(2.f * unit_phi, &sphi, &cphi);
+    float3 view = f3(cphi * sin_theta, cos_theta, sphi * sin_theta);
+    float mu = view.y;
+    bool ground = ray_hits_ground(r, rho2, mu);
+    float dist = ground ? dist_to_bottom(r, rho2, mu) : dist_to_top(r, A.thickness - alt, A.top, mu);
+    RayStart s0{r, alt, rho2, mu, mu_s, view.z * sun_z + view.y * mu_s};
+    int k0 = (n * chunk) / kMsChunks, k1 = (n * (chunk + 1)) / kMsChunks;
+    float3 lum, tr, lf;
+    integrate<true, float4>(A, Ls, nullptr, 0, 0, s0, dist / steps, 0.5f, k0, k1, iso, iso, lum, tr, lf);
+    compose_lanes<kMsChunks>(lum, tr, &lf);
+    if (chunk == 0 && ground) {
+        // ComputeGroundLuminance (Atmosphere.glsl:297-306) at r = R
+        float mu_s_g = (r * mu_s + dist * s0.nu) / A.R;
+        float3 sv = sun_visibility(A, Ls, A.R, 1.f / A.R, 0.f, 0.f, mu_s_g);
+        lum += tr * (A.ground_albedo * sv * (clamp01(mu_s_g) / SKYR_PI));
+    }
+    if (chunk != 0) lum = lf = f3(0.f);
+#pragma unroll
+    for (int o = 16; o >= kMsChunks; o >>= 1) {
+        lum.x += __shfl_xor_sync(0xffffffffu, lum.x, o);
+        lum.y += __shfl_xor_sync(0xffffffffu, lum.y, o);
+        lum.z += __shfl_xor_sync(0xffffffffu, lum.z, o);
+        lf.x += __shfl_xor_sync(0xffffffffu, lf.x, o);
+        lf.y += __shfl_xor_sync(0xffffffffu, lf.y, o);
+        lf.z += __shfl_xor_sync(0xffffffffu, lf.z, o);
+    }
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        red[warp][0] = lum.x; red[warp][1] = lum.y; red[warp][2] = lum.z;
+        red[warp][3] = lf.x; red[warp][4] = lf.y; red[warp][5] = lf.z;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float3 L2 = f3(0.f), F = f3(0.f);
+#pragma unroll
+        for (int i = 0; i < kMsThreads / 32; ++i) {
+            L2 += f3(red[i][0], red[i][1], red[i][2]);
+            F += f3(red[i][3], red[i][4], red[i][5]);
+        }
+        float3 l2 = L2 * (1.f / 64.f), fms = F * (1.f / 64.f);
+        float3 c = l2 / (f3(1.f) - fms);
+        store_rgba(out, (size_t)set * per_set + t, c, 1.f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// SKY_VIEW (AtmosphereRenderer.glsl:147-188) and AERIAL_PERSPECTIVE
+// (:191-245) in one launch: rays [0, n_sv) are sky-view texels, the rest are
+// aerial-perspective froxels.  LANES lanes per ray.
+// ---------------------------------------------------------------------------
+
+// ComputeRaymarchingStartPositionAndChangeDistance (AtmosphereRenderer.glsl:56-72)
+// + FromSpaceIntersectTopAtmosphereBoundary (AtmosphereInterface.glsl:6-13).
+__device__ __forceinline__ RayStart ray_start(const AtmoConsts& A, const ViewConsts& V, float mu, float nu,
+                                              float& marching) {
+    float mu_s = dot3(V.sun, V.up);
+    RayStart s{V.cam_r, V.cam_h, V.cam_rho2, mu, mu_s, nu};
+    if (V.in_space != 0.f) {
+        float r = V.cam_r, rm = r * mu;
+        float c = (V.cam_h - A.thickness) * (r + A.top);  // r^2 - top^2 > 0
+        float disc = rm * rm - c;
+        if (mu < 0.f && disc >= 0.f) {
+            float sq = sqrtf(fmaxf(disc, 0.f));
+            float nd = fmaxf(c / (-rm + sq), 0.f);
+            marching -= nd;
+            // move the start to the top boundary: r = top exactly
+            float r_s = A.top;
+            s.r = r_s;
+            s.h = A.thickness;
+            s.rho2 = A.top2_minus_R2;
+            s.mu = (rm + nd) / r_s;
+            s.mu_s = (r * mu_s + nd * nu) / r_s;
+        } else {
+            marching = 0.f;
+        }
+    }
+    return s;
+}
+
+template <int LANES, class S, bool TABLE>
+__global__ void __launch_bounds__(128) view_luts_kernel(JobSrc<TABLE> jobs, int n_sets, LutView L, int tstride,
+                                                        const S* __restrict__ ms, int mw, int mh, int msstride,
+                                                        int sv_w, int sv_h, int ap_w, int ap_h, int ap_d,
+                                                        S* __restrict__ sv_lum, S* __restrict__ sv_trans,
+                                                        S* __restrict__ ap_lum, S* __restrict__ ap_trans) {
+    int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    int lane = gid % LANES;
+    int ray = gid / LANES;
+    int n_sv = sv_w * sv_h, n_ap = ap_w * ap_h * ap_d;
+    int per_set = n_sv + n_ap;
+    int set = ray / per_set;
+    bool valid = set < n_sets;
+    if (!valid) set = n_sets - 1;
+    int t = ray % per_set;
+    const LutSetJob& J = jobs.get(set);
+    const AtmoConsts& A = J.a;
+    const ViewConsts& V = J.v;
+    LutView Ls = L;
+    Ls.t = L.t + (size_t)set * tstride;
+    const S* mss = ms + (size_t)set * msstride;
+
+    float3 view;
+    float mu, marching, steps;
+    RayStart s0;
+    bool is_sv = t < n_sv;
+    if (is_sv) {
+        // GetCosLatLonFromSkyViewTextureIndex / GetViewDirectionFromCosLatLon (:74-111)
+        int ix = t % sv_w, iy = t / sv_w;
+        float x_cos_lon = (float)ix / (float)(sv_w - 1);
+        float x_cos_lat = (float)iy / (float)(sv_h - 1);
+        float horizon_down = acosf(sqrtf(fmaxf(V.cam_rho2, 0.f)) / V.cam_r);
+        float horizon_up = SKYR_PI - horizon_down;
+        float lat;
+        if (x_cos_lat < 0.5f) {
+            float c = 1.f - 2.f * x_cos_lat;
+            lat = horizon_up * (1.f - c * c);
+        } else {
+            float c = x_cos_lat * 2.f - 1.f;
+            lat = horizon_up + horizon_down * (c * c);
+        }
+        float cos_lat = cosf(lat);
+        float cos_lon = -(x_cos_lon * x_cos_lon * 2.f - 1.f);
+        float sin_lat = clamp01(sqrtf(1.f - cos_lat * cos_lat));
+        float sin_lon = clamp01(sqrtf(1.f - cos_lon * cos_lon));
+        view = V.up * cos_lat + V.front * (sin_lat * cos_lon) + V.right * (sin_lat * sin_lon);
+        mu = cos_lat;
+        bool ground = ray_hits_ground(V.cam_r, V.cam_rho2, mu);
+        marching = ground ? dist_to_bottom(V.cam_r, V.cam_rho2, mu)
+                          : dist_to_top(V.cam_r, A.thickness - V.cam_h, A.top, mu);
+        s0 = ray_start(A, V, mu, dot3(view, V.sun), marching);
+        steps = V.sky_view_steps;
+    } else {
+        // GetMarchingDistanceFromAerialPerspectiveTextureIndex (:191-197) + main (:205-243)
+        int q = t - n_sv;
+        int ix = q % ap_w, iy = (q / ap_w) % ap_h, iz = q / (ap_w * ap_h);
+        float x = 2.f * ((float)ix / (float)(ap_w - 1)) - 1.f;
+        float y = 2.f * ((float)iy / (float)(ap_h - 1)) - 1.f;
+        float wz = (float)iz / (float)(ap_d - 1);
+        float3 dir = V.ap_a0 * x + V.ap_a1 * y + V.ap_a3;
+        float wsign = fmaf(V.ap_w0, x, fmaf(V.ap_w1, y, V.ap_w3)) < 0.f ? -1.f : 1.f;
+        view = dir * (wsign * rsqrtf(dot3(dir, dir)));
+        marching = wz * wz * V.ap_max_distance;
+        mu = dot3(view, V.up);
+        bool ground = ray_hits_ground(V.cam_r, V.cam_rho2, mu);
+        float max_marching = ground ? marching : dist_to_top(V.cam_r, A.thickness - V.cam_h, A.top, mu);
+        s0 = ray_start(A, V, mu, dot3(view, V.sun), max_marching);
+        marching = fminf(marching, max_marching);
+        steps = V.ap_steps;
+    }
+    float nu = s0.nu;
+    float3 lum = f3(0.f), tr = f3(1.f), lf;
+    bool active = marching > 0.f;
+    if (active) {
+        // RayleighPhaseFunction / MiePhaseFunction (Atmosphere.glsl:138-154)
+        float ph_r = 3.f / (16.f * SKYR_PI) * (1.f + nu * nu);
+        float g = A.mie_g;
+        float den = 1.f + g * g - 2.f * g * nu;
+        float ph_m = A.mie_phase_k * (1.f + nu * nu) / (den * sqrtf(den));
+        int n = sample_count(0.5f, steps);
+        int k0 = (n * lane) / LANES, k1 = (n * (lane + 1)) / LANES;
+        integrate<false, S>(A, Ls, mss, mw, mh, s0, marching / steps, 0.5f, k0, k1, ph_r, ph_m, lum, tr, lf);
+    }
+    // every lane of a group shares `active`, so the shuffles stay converged
+    compose_lanes<LANES>(lum, tr, nullptr);
+    if (valid && lane == 0) {
+        if (is_sv) {
+            size_t o = (size_t)set * n_sv + t;
+            store_rgba(sv_lum, o, lum, 0.f);
+            store_rgba(sv_trans, o, tr, 0.f);
+        } else {
+            size_t o = (size_t)set * n_ap + (t - n_sv);
+            store_rgba(ap_lum, o, lum, 0.f);
+            store_rgba(ap_trans, o, tr, 0.f);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+constexpr int kTLanes = 8;
+constexpr int kViewLanes = 8;
+
+template <bool TABLE>
+cudaError_t launch_transmittance(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, float4* out,
+                                 cudaStream_t st) {
+    long long threads = (long long)n_sets * s.transmittance_width * s.transmittance_height * kTLanes;
+    int blocks = (int)((threads + 127) / 128);
+    transmittance_kernel<kTLanes, TABLE>
+        <<<blocks, 128, 0, st>>>(jobs, n_sets, s.transmittance_width, s.transmittance_height, out);
+    return cudaGetLastError();
+}
+
+template <class S, bool TABLE>
+cudaError_t launch_multiscattering(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, const float4* tlut,
+                                   S* out, cudaStream_t st) {
+    int blocks = n_sets * s.multiscattering_width * s.multiscattering_height;
+    LutView L{tlut, s.transmittance_width, s.transmittance_height};
+    multiscattering_kernel<S, TABLE><<<blocks, kMsThreads, 0, st>>>(jobs, n_sets, L,
+                                                             s.transmittance_width * s.transmittance_height,
+                                                             s.multiscattering_width, s.multiscattering_height, out);
+    return cudaGetLastError();
+}
+
+template <class S, bool TABLE>
+cudaError_t launch_view_luts(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, const float4* tlut,
+                             const S* ms, S* svl, S* svt, S* apl, S* apt, cudaStream_t st) {
+    long long rays = (long long)n_sets * (s.sky_view_width * s.sky_view_height +
+                                          s.aerial_perspective_width * s.aerial_perspective_height *
+                                              s.aerial_perspective_depth);
+    int blocks = (int)((rays * kViewLanes + 127) / 128);
+    LutView L{tlut, s.transmittance_width, s.transmittance_height};
+    view_luts_kernel<kViewLanes, S, TABLE><<<blocks, 128, 0, st>>>(
+        jobs, n_sets, L, s.transmittance_width * s.transmittance_height, ms, s.multiscattering_width,
+        s.multiscattering_height, s.multiscattering_width * s.multiscattering_height, s.sky_view_width,
+        s.sky_view_height, s.aerial_perspective_width, s.aerial_perspective_height, s.aerial_perspective_depth, svl,
+        svt, apl, apt);
+    return cudaGetLastError();
+}
+
+#define SKYR_INST(TABLE)                                                                                        \
+    template cudaError_t launch_transmittance<TABLE>(JobSrc<TABLE>, int, const skyr_lut_sizes&, float4*,        \
+                                                     cudaStream_t);                                             \
+    template cudaError_t launch_multiscattering<float4, TABLE>(JobSrc<TABLE>, int, const skyr_lut_sizes&,       \
+                                                               const float4*, float4*, cudaStream_t);           \
+    template cudaError_t launch_multiscattering<__half2, TABLE>(JobSrc<TABLE>, int, const skyr_lut_sizes&,      \
+                                                                const float4*, __half2*, cudaStream_t);         \
+    template cudaError_t launch_view_luts<float4, TABLE>(JobSrc<TABLE>, int, const skyr_lut_sizes&,             \
+                                                         const float4*, const float4*, float4*, float4*,        \
+                                                         float4*, float4*, cudaStream_t);                       \
+    template cudaError_t launch_view_luts<__half2, TABLE>(JobSrc<TABLE>, int, const skyr_lut_sizes&,            \
+                                                          const float4*, const __half2*, __half2*, __half2*,    \
+                                                          __half2*, __half2*, cudaStream_t);
+SKYR_INST(false)
+SKYR_INST(true)
+#undef SKYR_INST
+
+}  // namespace skyr
