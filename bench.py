@@ -1,16 +1,20 @@
 """Benchmark of the atmosphere-LUT / volumetric-cloud hot path on one GB300.
 
-A step is one full plain frame of the 1920x1080 workload: the whole LUT set
-(transmittance 256x64 / 40 samples, multi-scattering 32x32 / 64 directions x
-20 samples, sky-view 192x108 / 30 samples, aerial perspective 32^3 / 40
-samples over 32 km) followed by the per-pixel cloud raymarch.  Inputs are
-seeded synthetic (no dataset); see skyrendering_gb300/workloads.py.
+A step is one plain 1920x1080 frame:
+  * the whole LUT set (transmittance 256x64 / 40 samples, multi-scattering
+    32x32 / 64 directions x 20 samples, sky-view 192x108 / 30 samples, aerial
+    perspective 32^3 / 40 samples over 32 km), then
+  * the per-pixel cloud raymarch (layer 1.5-4.0 km, Material1, 50/km,
+    64 primary steps, 6 light-march steps, seeded blue-noise jitter).
+Noise textures (512^2 RG8 weather map, 128^3 RGBA8 base noise) are generated
+once before timing, as the reference regenerates them only when their
+parameters change.  Inputs are seeded synthetic (skyrendering_gb300/workloads.py).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 Prints one JSON line.  --impl reference times the CPU restatement of the
 reference's shader math (the reference itself is GLSL for an OpenGL driver,
-which this machine cannot run) on the host cores.
+which these machines cannot run) on the host cores.
 """
 from __future__ import annotations
 
@@ -28,24 +32,24 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "LUT-set regen µs; 1080p cloud frame ms; surrogate vs path-trace GPU time @2% err"
+UNIT = "ms per 1920x1080 frame (LUT set + cloud raymarch)"
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
+SUN_ZENITH = 45.0
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="skyr", choices=["skyr", "reference"])
-    ap.add_argument("--cpu-sample-s", type=float, default=15.0)
+    ap.add_argument("--cpu-sample-s", type=float, default=12.0)
     return ap.parse_args()
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 class ClockSampler:
@@ -67,7 +71,7 @@ class ClockSampler:
                                          stdout=self.file, stderr=subprocess.DEVNULL)
         except FileNotFoundError:
             self.proc = None
-        time.sleep(0.3)
+        time.sleep(0.4)
         return self
 
     def __exit__(self, *a):
@@ -96,7 +100,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def measured_peaks():
+def peaks():
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
         d = json.loads(f.read_text())
@@ -104,15 +108,62 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / "ncu_dram_bytes.json"
+    if f.exists():
+        return json.loads(f.read_text()).get(kernel)
+    return None
+
+
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+class FrameState:
+    def __init__(self, ctx):
+        import torch
+
+        from skyrendering_gb300 import workloads as W
+        from skyrendering_gb300.atmosphere import LutSet
+        from skyrendering_gb300.cloud import (NoiseTexture, VolumetricCloud, blue_noise_tile, prepare_textures,
+                                              textures_struct)
+
+        self.W = W
+        self.ctx = ctx
+        self.atmo = W.earth_like_atmosphere()
+        self.sizes = W.plain_lut_sizes()
+        self.cam = W.frame_camera()
+        self.render = W.render_parameters(self.cam, SUN_ZENITH)
+        self.luts = LutSet.allocate(self.sizes, 1)
+        self.tex = {"cloud_map": NoiseTexture(W.cloud_map_desc()).generate(ctx),
+                    "detail": NoiseTexture(W.base_noise_desc()).generate(ctx)}
+        self.material = W.frame_material()
+        prepare_textures(ctx, self.material.type, self.tex)
+        self.bn_host = blue_noise_tile().pin_memory()
+        self.bn = self.bn_host.cuda()
+        self.view = W.frame_view(self.cam, SUN_ZENITH)
+        self.vc = VolumetricCloud(ctx, W.frame_cloud_parameters(), self.material, textures_struct(**self.tex))
+        h, w = self.view.height, self.view.width
+        self.rgba = torch.empty((h, w, 4), dtype=torch.float16, device="cuda")
+        self.dist = torch.empty((h, w), dtype=torch.float32, device="cuda")
+
+    def luts_step(self):
+        from skyrendering_gb300.atmosphere import update_lut_set
+
+        update_lut_set(self.ctx, self.atmo, self.render, self.sizes, self.luts)
+
+    def cloud_step(self):
+        self.vc.render(self.atmo, self.view, self.sizes, self.luts, self.bn, out_rgba=self.rgba,
+                       out_distance=self.dist)
+
+
 def run_skyr(args):
+    import ctypes as C
+
     import torch
 
     from skyrendering_gb300 import _abi
-    from skyrendering_gb300 import workloads as W
-    from skyrendering_gb300.atmosphere import Context, LutSet, update_lut_set
+    from skyrendering_gb300.atmosphere import Context, _ptr
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -123,76 +174,92 @@ def run_skyr(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ctx = Context(stream)
-
-    p = W.earth_like_atmosphere()
-    sizes = W.plain_lut_sizes()
-    cam = W.frame_camera()
-    render = W.render_parameters(cam, 45.0)
-    luts = LutSet.allocate(sizes, 1)
+    fs = FrameState(ctx)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-
-    def step():
-        update_lut_set(ctx, p, render, sizes, luts)
-
-    kernels_per_step = 3
-    for _ in range(max(args.warmup, 3)):
-        step()
-    torch.cuda.synchronize()
+    kernels_per_step = 4  # transmittance, multi-scattering, sky-view + AP, cloud raymarch
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for _ in range(max(args.warmup, 3)):
+        fs.luts_step()
+        fs.cloud_step()
+    barrier()
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     with ClockSampler(local) as clk:
         barrier()
         wall0 = time.perf_counter()
         for i in range(args.steps):
-            flush.fill_(float(i))  # evict L2 between steps (not timed)
-            starts[i].record(stream)
-            step()
-            ends[i].record(stream)
+            flush.fill_(float(i))  # evict L2 between steps (outside the timed interval)
+            ev[i][0].record(stream)
+            fs.luts_step()
+            ev[i][1].record(stream)
+            fs.cloud_step()
+            ev[i][2].record(stream)
         barrier()
         wall = time.perf_counter() - wall0
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = statistics.mean(step_ms)
+        # e2e through the public API with host buffers: the blue-noise tile
+        # H2D from pinned memory (parameter blocks travel by value in the
+        # launches) and both frame outputs D2H into pinned memory
+        host_rgba = torch.empty(fs.rgba.shape, dtype=fs.rgba.dtype, pin_memory=True)
+        host_dist = torch.empty(fs.dist.shape, dtype=fs.dist.dtype, pin_memory=True)
+
+        def e2e_step():
+            fs.bn.copy_(fs.bn_host, non_blocking=True)
+            fs.luts_step()
+            fs.cloud_step()
+            host_rgba.copy_(fs.rgba, non_blocking=True)
+            host_dist.copy_(fs.dist, non_blocking=True)
+
+        for _ in range(3):
+            e2e_step()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    lut_ms = [a.elapsed_time(b) for a, b, _ in ev]
+    cloud_ms = [b.elapsed_time(c) for _, b, c in ev]
+    frame_ms = [a.elapsed_time(c) for a, _, c in ev]
+    ms = statistics.mean(frame_ms)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
 
-    # e2e: public API with host buffers: parameter blocks H2D (pinned) and the
-    # LUT outputs D2H (pinned) inside the timed region
-    host_out = {n: torch.empty(getattr(luts, n).shape, dtype=getattr(luts, n).dtype, pin_memory=True)
-                for n in ("transmittance", "multiscattering", "sky_view_luminance", "sky_view_transmittance",
-                          "aerial_perspective_luminance", "aerial_perspective_transmittance")}
-    d2h = sum(t.numel() * t.element_size() for t in host_out.values())
-    import ctypes as C
-    h2d = C.sizeof(p) + C.sizeof(render)
-
-    def e2e_step():
-        update_lut_set(ctx, p, render, sizes, luts)
-        for n, t in host_out.items():
-            t.copy_(getattr(luts, n), non_blocking=True)
-
-    for _ in range(3):
-        e2e_step()
+    # work counters of one frame (instrumented launch, outside the timing)
+    counters = torch.zeros(2, dtype=torch.int64, device="cuda")
+    L = fs.luts
+    _abi.call("skyr_cloud_render_counted", ctx.handle, C.byref(fs.atmo), C.byref(fs.vc.params),
+              C.byref(fs.vc.material), C.byref(fs.vc.textures), C.byref(fs.view), C.byref(fs.sizes),
+              _ptr(L.transmittance), _ptr(L.aerial_perspective_luminance), _ptr(L.aerial_perspective_transmittance),
+              _ptr(fs.bn), None, _ptr(fs.rgba), _ptr(fs.dist), _ptr(counters))
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
+    samples, evals = (int(x) for x in counters.cpu())
 
     clocks = clk.summary()
+    hbm_peak, peak_kind = peaks()
+    npx = fs.view.width * fs.view.height
+    # algorithmic bytes of one raymarch launch: the outputs (8 B RGBA16F + 4 B
+    # R32F per pixel) plus one read of every input it samples (weather map
+    # level 0 RG, base noise level 0 R, the transmittance LUT, both AP volumes)
+    tex_bytes = 512 * 512 * 2 + 128 ** 3 * 1
+    lut_bytes = 256 * 64 * 16 + 2 * 32 ** 3 * 16
+    alg_bytes = npx * 12 + tex_bytes + lut_bytes
+    cloud_mean = statistics.mean(cloud_ms)
+    achieved = alg_bytes / (cloud_mean * 1e-3) / 1e9
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     result = {
         "metric": METRIC,
-        "value": ms * 1000.0,
-        "unit": "us per LUT set",
+        "value": ms,
+        "unit": UNIT,
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
@@ -201,12 +268,26 @@ def run_skyr(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded Earth-like atmosphere, 1 km camera, sun zenith 45 deg)",
-        "config": {"workload": "plain LUT set: T 256x64x40, MS 32x32x64x20, SV 192x108x30, AP 32^3x40 over 32 km",
-                   "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}"},
-        "e2e": {"value": e2e_ms * 1000.0, "unit": "us per LUT set", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+        "data": "synthetic (seeded Earth-like atmosphere and Perlin-Worley cloud textures, 1 km camera, "
+                "60 deg FOV, sun zenith 45 deg, seeded 64x64 blue noise)",
+        "config": {"workload": "plain 1920x1080 frame: LUT set (T 256x64x40, MS 32x32x64x20, SV 192x108x30, "
+                               "AP 32^3x40 over 32 km) + per-pixel cloud raymarch (layer 1.5-4.0 km, "
+                               "Material1 50/km, 64 steps, 6 light steps)",
+                   "l2": "flushed between timed steps (512 MB write outside the timed interval)",
+                   "parallelism": f"replicas x{world}"},
+        "components": {"lut_set_us": statistics.mean(lut_ms) * 1000.0, "cloud_frame_ms": cloud_mean,
+                       "raymarch_samples": samples, "density_evaluations": evals,
+                       "density_evaluations_per_s": evals / (cloud_mean * 1e-3)},
+        "e2e": {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": fs.bn_host.numel() * 4,
+                "d2h_bytes_per_step": host_rgba.numel() * 2 + host_dist.numel() * 4},
         "gpu_launches": kernels_per_step * args.steps,
+        "roofline": {"kernel": "cloud_render_kernel", "bound": "hbm", "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                     "traffic": ncu_traffic("cloud_render_kernel"),
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "note": "compulsory bytes; the raymarch is issue/FP32-bound on L1-resident textures"},
+        "roofline_fp32": {"kernel": "cloud_render_kernel", "peak_tflops_nominal": fp32_peak,
+                          "note": "152 SMs x 128 FP32 lanes x 2 x median SM clock; pipe use in profiles/"},
         "clocks": clocks,
         "wall_s": wall,
     }
@@ -220,32 +301,56 @@ def run_skyr(args):
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline / reference arm: the FP32 restatement of the shader math on the
-# host cores (oracle/, test infrastructure; timed, never shipped)
+# CPU baseline / reference arm: the FP32 restatement of the shader math
+# (oracle/, test infrastructure; timed, never shipped) on the host cores, on a
+# bounded sample scaled to a full frame.
 # ---------------------------------------------------------------------------
-def cpu_lut_set_us(sample_s: float, threads: int):
+_HOST_TEXTURES = {}
+
+
+def cpu_frame_ms(sample_s: float, threads: int):
+    import numpy as np
+
     from oracle import oracle as orc
     from skyrendering_gb300 import workloads as W
 
-    p = W.earth_like_atmosphere()
-    s = W.plain_lut_sizes()
-    r = W.render_parameters(W.frame_camera(), 45.0)
-    orc.lut_set(p, r, s, 32, nthreads=threads)  # warm-up / build
-    n, t0 = 0, time.perf_counter()
-    while True:
-        orc.lut_set(p, r, s, 32, nthreads=threads)
-        n += 1
+    atmo, sizes, cam = W.earth_like_atmosphere(), W.plain_lut_sizes(), W.frame_camera()
+    render = W.render_parameters(cam, SUN_ZENITH)
+    t0 = time.perf_counter()
+    luts = orc.lut_set(atmo, render, sizes, 32, nthreads=threads)
+    lut_s = time.perf_counter() - t0
+    if not _HOST_TEXTURES:  # generated once, like the GPU arm's textures
+        _HOST_TEXTURES["cloud_map"] = (W.cloud_map_desc(), orc.noise_generate(W.cloud_map_desc(), 32, threads))
+        _HOST_TEXTURES["detail"] = (W.base_noise_desc(), orc.noise_generate(W.base_noise_desc(), 32, threads))
+    host = dict(_HOST_TEXTURES)
+    view = W.frame_view(cam, SUN_ZENITH)
+    from skyrendering_gb300.cloud import blue_noise_tile
+
+    bn = blue_noise_tile().numpy()
+    npx = view.width * view.height
+    args = (W.frame_cloud_parameters(), W.frame_material(), host, view, sizes, luts["transmittance"],
+            luts["aerial_perspective_luminance"], luts["aerial_perspective_transmittance"], bn)
+    stride = 4096
+    done, spent = 0, 0.0
+    while spent < max(sample_s - lut_s, 0.5) and stride >= 1:
+        px = np.arange(done % stride, npx, stride, dtype=np.int32)
+        t0 = time.perf_counter()
+        orc.cloud_render(atmo, *args, pixels=px, precision=32, nthreads=threads)
         el = time.perf_counter() - t0
-        if el >= sample_s or n >= 1000:
-            break
-    return el / n * 1e6, n
+        spent += el
+        done += len(px)
+        stride = max(stride // 2, 1)
+    cloud_s = spent / done * npx
+    return (lut_s + cloud_s) * 1000.0, done, lut_s * 1e3
 
 
 def cpu_baseline(sample_s: float):
     threads = os.cpu_count() or 1
-    us, n = cpu_lut_set_us(sample_s, threads)
-    return {"value": us, "unit": "us per LUT set", "cores": threads, "kind": "port",
-            "sample": f"{n} full plain LUT sets in FP32 on {threads} threads (~{sample_s:.0f} s)"}
+    ms, n, lut_ms = cpu_frame_ms(sample_s, threads)
+    return {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
+            "lut_set_ms": lut_ms,
+            "sample": f"one full LUT set + {n} of 2073600 raymarched pixels (spread over the frame) in FP32 "
+                      f"on {threads} threads, scaled to the full frame"}
 
 
 def run_reference(args):
@@ -253,20 +358,24 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    vals = []
-    for _ in range(max(args.warmup, 0)):
-        cpu_lut_set_us(0.5, threads)
+    per = max(2.0, min(args.cpu_sample_s, 150.0 / max(args.steps + args.warmup, 1)))
+    for _ in range(args.warmup):
+        cpu_frame_ms(1.0, threads)
+    vals, ns = [], []
     for _ in range(args.steps):
-        us, _n = cpu_lut_set_us(min(args.cpu_sample_s, 120.0 / max(args.steps, 1)), threads)
-        vals.append(us)
+        ms, n, _l = cpu_frame_ms(per, threads)
+        vals.append(ms)
+        ns.append(n)
     v = statistics.mean(vals)
+    sample = (f"per step: one full LUT set + ~{int(statistics.mean(ns))} raymarched pixels in FP32 on "
+              f"{threads} threads (oracle/ restatement of the reference shaders), scaled to 1920x1080")
     print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "us per LUT set", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v / 1000.0, "higher_is_better": False,
-        "dtype": "f32", "data": "synthetic", "config": {"workload": "plain LUT set (as the skyr arm)"},
-        "cpu_baseline": {"value": v, "unit": "us per LUT set", "cores": threads, "kind": "port",
-                         "sample": "FP32 restatement of the reference shaders (oracle/), all host threads"},
-        "e2e": {"value": v, "unit": "us per LUT set", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (same seeded inputs as the skyr arm)",
+        "config": {"workload": "plain 1920x1080 frame: LUT set + per-pixel cloud raymarch (as the skyr arm)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
 

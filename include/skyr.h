@@ -52,7 +52,9 @@ const char* skyr_last_error(void);
 
 /* sizeof() of the public structs, for binding layout checks:
  * 0 skyr_atmosphere_parameters, 1 skyr_atmosphere_render_parameters,
- * 2 skyr_lut_sizes; further ids are listed beside later structs.
+ * 2 skyr_lut_sizes, 3 skyr_noise_texture_desc, 4 skyr_cloud_material,
+ * 5 skyr_cloud_textures, 6 skyr_cloud_parameters, 7 skyr_cloud_view;
+ * further ids are listed beside later structs.
  * Returns 0 for an unknown id.  (No reference counterpart: ABI hygiene.) */
 size_t skyr_struct_size(int which);
 

@@ -122,3 +122,101 @@ def transmittance_at(params, r: float, mu: float) -> np.ndarray:
     out = np.zeros(3)
     assert lib().oracle_transmittance_at(_ref(params), r, mu, _dp(out)) == 0
     return out
+
+
+# ---------------------------------------------------------------------------
+# noise and cloud raymarch
+# ---------------------------------------------------------------------------
+U8 = C.POINTER(C.c_uint8)
+I32 = C.POINTER(C.c_int)
+F32 = C.POINTER(C.c_float)
+
+
+def _declare_cloud(lb):
+    lb.oracle_noise_generate.restype = C.c_int
+    lb.oracle_noise_generate.argtypes = [P, C.c_int, C.c_int, U8]
+    lb.oracle_noise_mips.restype = C.c_int
+    lb.oracle_noise_mips.argtypes = [P, U8]
+    lb.oracle_noise_values.restype = C.c_int
+    lb.oracle_noise_values.argtypes = [P, C.c_int, I32, C.c_int, D]
+    lb.oracle_wang_hash.restype = C.c_uint32
+    lb.oracle_wang_hash.argtypes = [C.c_uint32]
+    lb.oracle_pcg_hash.restype = C.c_uint32
+    lb.oracle_pcg_hash.argtypes = [C.c_uint32]
+    lb.oracle_cloud_render.restype = C.c_int
+    lb.oracle_cloud_render.argtypes = [P, P, P, P, P, P, D, D, D, F32, F32, I32, C.c_int, C.c_int, C.c_int, D, D]
+
+
+_EXT.append(_declare_cloud)
+
+
+def noise_bytes(desc) -> int:
+    total, m = 0, max(desc.width, desc.height, desc.depth)
+    levels = m.bit_length()
+    for l in range(levels):
+        total += max(desc.width >> l, 1) * max(desc.height >> l, 1) * max(desc.depth >> l, 1) * desc.channels
+    return total
+
+
+def noise_generate(desc, precision: int = 64, nthreads: int | None = None) -> np.ndarray:
+    out = np.zeros(noise_bytes(desc), dtype=np.uint8)
+    assert lib().oracle_noise_generate(_ref(desc), precision, nthreads or threads(),
+                                       out.ctypes.data_as(U8)) == 0
+    return out
+
+
+def noise_mips(desc, tex: np.ndarray) -> np.ndarray:
+    """Rebuild levels 1.. from level 0 of `tex` (copy)."""
+    out = np.ascontiguousarray(tex, dtype=np.uint8).copy()
+    assert lib().oracle_noise_mips(_ref(desc), out.ctypes.data_as(U8)) == 0
+    return out
+
+
+def noise_values(desc, channel: int, idx: np.ndarray) -> np.ndarray:
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    out = np.zeros(len(idx))
+    assert lib().oracle_noise_values(_ref(desc), channel, idx.ctypes.data_as(I32), len(idx), _dp(out)) == 0
+    return out
+
+
+def wang_hash(x: int) -> int:
+    return lib().oracle_wang_hash(x)
+
+
+def pcg_hash(x: int) -> int:
+    return lib().oracle_pcg_hash(x)
+
+
+def cloud_render(atmo, cloud, material, textures_host: dict, view, sizes, transmittance, ap_lum, ap_trans,
+                 blue_noise, depth=None, pixels=None, precision: int = 64, nthreads: int | None = None):
+    """Raymarch pixels (flat indices, or all) of `view` with host textures.
+
+    textures_host maps 'cloud_map' / 'detail' / 'displacement' / 'voxel' to
+    (desc, uint8 array)."""
+    import skyrendering_gb300._abi as A  # struct layout only
+
+    t = A.CloudTextures()
+    keep = []
+    for name in ("cloud_map", "detail", "displacement", "voxel"):
+        if name in textures_host:
+            desc, arr = textures_host[name]
+            arr = np.ascontiguousarray(arr, dtype=np.uint8)
+            keep.append(arr)
+            setattr(t, name, arr.ctypes.data)
+            setattr(t, name + "_desc", desc)
+    n = view.width * view.height if pixels is None else len(pixels)
+    px = None if pixels is None else np.ascontiguousarray(pixels, dtype=np.int32)
+    rgba = np.zeros((n, 4))
+    dist = np.zeros(n)
+    bn = np.ascontiguousarray(blue_noise, dtype=np.float32)
+    dp = None if depth is None else np.ascontiguousarray(depth, dtype=np.float32)
+    tl = np.ascontiguousarray(transmittance, dtype=np.float64)
+    al = np.ascontiguousarray(ap_lum, dtype=np.float64)
+    at = np.ascontiguousarray(ap_trans, dtype=np.float64)
+    rc = lib().oracle_cloud_render(_ref(atmo), _ref(cloud), _ref(material), _ref(t), _ref(view), _ref(sizes),
+                                   _dp(tl), _dp(al), _dp(at), bn.ctypes.data_as(F32),
+                                   None if dp is None else dp.ctypes.data_as(F32),
+                                   None if px is None else px.ctypes.data_as(I32), n, precision,
+                                   nthreads or threads(), _dp(rgba), _dp(dist))
+    assert rc == 0
+    return rgba, dist

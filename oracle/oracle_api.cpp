@@ -7,6 +7,8 @@
 #include <thread>
 
 #include "oracle_atmosphere.hpp"
+#include "oracle_cloud.hpp"
+#include "oracle_noise.hpp"
 
 namespace {
 
@@ -144,6 +146,128 @@ int oracle_transmittance_at(const skyr_atmosphere_parameters* p, double r, doubl
     orc::V3<double> t = O.ComputeTransmittance(r, mu);
     out3[0] = t.x; out3[1] = t.y; out3[2] = t.z;
     return 0;
+}
+
+}  // extern "C"
+
+// ---- noise ---------------------------------------------------------------
+namespace {
+
+int noise_levels(const skyr_noise_texture_desc* d) {
+    int m = std::max(d->width, std::max(d->height, d->depth)), l = 1;
+    while ((m >> l) > 0) ++l;
+    return l;
+}
+
+size_t level_bytes(const skyr_noise_texture_desc* d, int l) {
+    return (size_t)std::max(d->width >> l, 1) * std::max(d->height >> l, 1) * std::max(d->depth >> l, 1) *
+           d->channels;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Mip chain of levels 1.. from level 0 already in `tex` (bit-exact integer work).
+int oracle_noise_mips(const skyr_noise_texture_desc* d, uint8_t* tex) {
+    size_t off = 0;
+    int L = noise_levels(d);
+    for (int l = 0; l + 1 < L; ++l) {
+        size_t nb = level_bytes(d, l);
+        orc::box_reduce(tex + off, std::max(d->width >> l, 1), std::max(d->height >> l, 1),
+                        std::max(d->depth >> l, 1), tex + off + nb, d->channels);
+        off += nb;
+    }
+    return 0;
+}
+
+// Level 0 and the mip chain.  precision 64 or 32.
+int oracle_noise_generate(const skyr_noise_texture_desc* d, int precision, int threads, uint8_t* tex) {
+    int w = d->width, h = d->height, dd = d->depth;
+    size_t plane = (size_t)w * h * dd;
+    parallel_for(h * dd, threads, [&](int row) {
+        int y = row % h, z = row / h;
+        for (int c = 0; c < d->channels; ++c)
+            for (int x = 0; x < w; ++x) {
+                uint8_t b = precision == 32
+                                ? orc::unorm8(orc::channel_value<float>(d->channel[c], x, y, z, w, h, dd, d->octaves))
+                                : orc::unorm8(orc::channel_value<double>(d->channel[c], x, y, z, w, h, dd, d->octaves));
+                tex[c * plane + ((size_t)z * h + y) * w + x] = b;
+            }
+    });
+    return oracle_noise_mips(d, tex);
+}
+
+// Noise values (unquantised) at level-0 texels, for error analysis.
+int oracle_noise_values(const skyr_noise_texture_desc* d, int channel, const int* idx, int n, double* out) {
+    int w = d->width, h = d->height, dd = d->depth;
+    for (int i = 0; i < n; ++i) {
+        int x = idx[i] % w, y = (idx[i] / w) % h, z = idx[i] / (w * h);
+        out[i] = orc::channel_value<double>(d->channel[channel], x, y, z, w, h, dd, d->octaves);
+    }
+    return 0;
+}
+
+uint32_t oracle_wang_hash(uint32_t x) { return orc::WangHash(x); }
+uint32_t oracle_pcg_hash(uint32_t x) { return orc::PCGHash(x); }
+
+}  // extern "C"
+
+// ---- cloud raymarch --------------------------------------------------------
+namespace {
+
+template <class T>
+int cloud_render_t(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                          const skyr_cloud_material* m, const skyr_cloud_textures* tx, const skyr_cloud_view* v,
+                          const skyr_lut_sizes* s, const double* tlut_in, const double* apl_in,
+                          const double* apt_in, const float* blue_noise, const float* depth, const int* pixels,
+                          int n_pixels, int threads, double* out_rgba, double* out_dist) {
+    orc::AtmosphereOracle<T> O{orc::derive_atmosphere<T>(*atmo)};
+    orc::Image<T> tl = image_from<T>(tlut_in, s->transmittance_width, s->transmittance_height);
+    int W = s->aerial_perspective_width, H = s->aerial_perspective_height, D = s->aerial_perspective_depth;
+    orc::Image<T> al = image_from<T>(apl_in, W, H, D), at = image_from<T>(apt_in, W, H, D);
+    orc::CloudOracle<T> C{O, orc::derive_cloud_frame<T>(*atmo, *cp, *m, *tx, *v), {}, {}, {}, {}, nullptr,
+                          nullptr, nullptr, nullptr};
+    auto set = [](orc::Tex8& t, const void* p, const skyr_noise_texture_desc& d, bool border) {
+        t.data = (const uint8_t*)p;
+        t.w = d.width; t.h = d.height; t.d = d.depth; t.channels = d.channels;
+        t.border = border;
+        t.init();
+    };
+    set(C.cloud_map, tx->cloud_map, tx->cloud_map_desc, false);
+    set(C.detail, tx->detail, tx->detail_desc, false);
+    set(C.displacement, tx->displacement, tx->displacement_desc, false);
+    set(C.voxel, tx->voxel, tx->voxel_desc, true);
+    C.tlut = &tl;
+    C.ap_lum = &al;
+    C.ap_trans = &at;
+    C.blue_noise = blue_noise;
+    parallel_for(n_pixels, threads, [&](int i) {
+        int p = pixels ? pixels[i] : i;
+        int px = p % v->width, py = p / v->width;
+        T rgba[4], dist;
+        C.Pixel(px, py, v->width, v->height, depth ? depth[p] : 1.0f, rgba, dist);
+        for (int k = 0; k < 4; ++k) out_rgba[(size_t)i * 4 + k] = double(rgba[k]);
+        if (out_dist) out_dist[i] = double(dist);
+    });
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Raymarch the listed pixels (or all when pixels == NULL) of the view.
+int oracle_cloud_render(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                        const skyr_cloud_material* m, const skyr_cloud_textures* tx, const skyr_cloud_view* v,
+                        const skyr_lut_sizes* s, const double* tlut, const double* apl, const double* apt,
+                        const float* blue_noise, const float* depth, const int* pixels, int n_pixels, int precision,
+                        int threads, double* out_rgba, double* out_dist) {
+    if (precision == 32)
+        return cloud_render_t<float>(atmo, cp, m, tx, v, s, tlut, apl, apt, blue_noise, depth, pixels, n_pixels,
+                                     threads, out_rgba, out_dist);
+    return cloud_render_t<double>(atmo, cp, m, tx, v, s, tlut, apl, apt, blue_noise, depth, pixels, n_pixels,
+                                  threads, out_rgba, out_dist);
 }
 
 }  // extern "C"

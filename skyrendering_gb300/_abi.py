@@ -162,3 +162,97 @@ def call(name: str, *args) -> None:
 
 def exported_symbols() -> list[str]:
     return sorted(_SIGNATURES)
+
+
+# ---------------------------------------------------------------------------
+# skyr_cloud.h
+# ---------------------------------------------------------------------------
+SKYR_NOISE_PERLIN, SKYR_NOISE_WORLEY, SKYR_NOISE_PERLIN_WORLEY, SKYR_NOISE_ZERO = range(4)
+SKYR_MATERIAL_DEFAULT0, SKYR_MATERIAL_DEFAULT1, SKYR_MATERIAL_MINIMAL, SKYR_MATERIAL_VOXEL = range(4)
+(SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST, SKYR_MIPMAP_LINEAR_MIPMAP_NEAREST, SKYR_MIPMAP_NEAREST_MIPMAP_LINEAR,
+ SKYR_MIPMAP_LINEAR_MIPMAP_LINEAR) = range(4)
+f2 = C.c_float * 2
+
+
+class NoiseCreateInfo(C.Structure):
+    """skyr_noise_create_info (NoiseCreateInfo, src/SkyRendering/VolumetricCloudDefaultMaterial.h:57-64)."""
+
+    _fields_ = [("seed", C.c_int), ("base_frequency", C.c_int), ("remap_min", C.c_float), ("remap_max", C.c_float)]
+
+
+class NoiseChannel(C.Structure):
+    _fields_ = [("kind", C.c_int), ("a", NoiseCreateInfo), ("b", NoiseCreateInfo)]
+
+
+class NoiseTextureDesc(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("depth", C.c_int), ("channels", C.c_int),
+                ("octaves", C.c_int), ("channel", NoiseChannel * 4)]
+
+
+class CloudMaterial(C.Structure):
+    """skyr_cloud_material (the IVolumetricCloudMaterial implementations)."""
+
+    _fields_ = [
+        ("type", C.c_int),
+        ("density", C.c_float), ("lod_bias", C.c_float),
+        ("cloud_map_repeat_size", C.c_float), ("detail_repeat_size", C.c_float),
+        ("displacement_repeat_size", C.c_float),
+        ("offset_from_first", f2), ("detail_offset_from_first", f2),
+        ("minfilter2d", C.c_int), ("minfilter3d", C.c_int), ("minfilter_displacement", C.c_int),
+        ("base_density_threshold", C.c_float), ("base_height_hardness", C.c_float),
+        ("base_edge_hardness", C.c_float), ("detail_base", C.c_float), ("detail_scale", C.c_float),
+        ("height_cut", C.c_float), ("edge_cut", C.c_float),
+        ("detail_param", f2), ("displacement_scale", C.c_float),
+        ("voxel_base", f2), ("voxel_width", f2),
+    ]
+
+
+class CloudTextures(C.Structure):
+    _fields_ = [("cloud_map", C.c_void_p), ("cloud_map_desc", NoiseTextureDesc),
+                ("detail", C.c_void_p), ("detail_desc", NoiseTextureDesc),
+                ("displacement", C.c_void_p), ("displacement_desc", NoiseTextureDesc),
+                ("voxel", C.c_void_p), ("voxel_desc", NoiseTextureDesc),
+                ("cloud_map_expanded", C.c_void_p), ("detail_expanded", C.c_void_p),
+                ("displacement_expanded", C.c_void_p), ("voxel_expanded", C.c_void_p),
+                ("cloud_map_expanded_channels", C.c_int), ("detail_expanded_channels", C.c_int),
+                ("displacement_expanded_channels", C.c_int), ("voxel_expanded_channels", C.c_int)]
+
+
+class CloudParameters(C.Structure):
+    """skyr_cloud_parameters (VolumetricCloud fields, src/SkyRendering/VolumetricCloud.h:20-55)."""
+
+    _fields_ = [
+        ("bottom_altitude", C.c_float), ("thickness", C.c_float), ("max_raymarch_distance", C.c_float),
+        ("max_raymarch_steps", C.c_float), ("max_visible_distance", C.c_float), ("env_color", f3),
+        ("env_color_scale", C.c_float), ("sun_illuminance_scale", C.c_float), ("shadow_steps", C.c_float),
+        ("shadow_distance", C.c_float), ("shadow_froxel_max_distance", C.c_float),
+        ("sun_multiscattering_sigma_scale", C.c_float), ("env_multiscattering_sigma_scale", C.c_float),
+        ("env_bottom_visibility", C.c_float), ("env_sun_height_curve_exp", C.c_float),
+        ("phase_g_forward", C.c_float), ("phase_g_back", C.c_float), ("phase_back_scale", C.c_float),
+    ]
+
+
+class CloudView(C.Structure):
+    _fields_ = [("camera_position", f3), ("view_projection", f16), ("fovy", C.c_float),
+                ("viewport_width", C.c_int), ("viewport_height", C.c_int), ("width", C.c_int),
+                ("height", C.c_int), ("sun_direction_theta", C.c_float), ("sun_direction_phi", C.c_float),
+                ("frame_id", C.c_float), ("aerial_perspective_lut_max_distance", C.c_float)]
+
+
+STRUCT_IDS.update({3: NoiseTextureDesc, 4: CloudMaterial, 5: CloudTextures, 6: CloudParameters, 7: CloudView})
+_SIGNATURES.update({
+    "skyr_noise_texture_levels": (C.c_int, [C.POINTER(NoiseTextureDesc)]),
+    "skyr_noise_level_offset": (C.c_size_t, [C.POINTER(NoiseTextureDesc), C.c_int]),
+    "skyr_noise_generate": (C.c_int, [P, C.POINTER(NoiseTextureDesc), P]),
+    "skyr_cloud_material_default": (C.c_int, [C.c_int, C.POINTER(CloudMaterial)]),
+    "skyr_cloud_parameters_default": (C.c_int, [C.POINTER(CloudParameters)]),
+    "skyr_cloud_render": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                    C.POINTER(CloudMaterial), C.POINTER(CloudTextures), C.POINTER(CloudView),
+                                    C.POINTER(LutSizes), P, P, P, P, P, P, P]),
+    "skyr_blue_noise_generate": (C.c_int, [C.c_uint32, C.POINTER(C.c_float)]),
+    "skyr_noise_expanded_bytes": (C.c_size_t, [C.POINTER(NoiseTextureDesc), C.c_int]),
+    "skyr_noise_expand": (C.c_int, [P, C.POINTER(NoiseTextureDesc), P, C.c_int, P]),
+})
+_SIGNATURES["skyr_cloud_render_counted"] = (
+    C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters), C.POINTER(CloudMaterial),
+              C.POINTER(CloudTextures), C.POINTER(CloudView), C.POINTER(LutSizes), P, P, P, P, P, P, P, P])

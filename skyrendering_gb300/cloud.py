@@ -1,0 +1,126 @@
+"""Host-side mirror of the reference's volumetric-cloud classes over the C ABI.
+
+* ``NoiseTexture`` ~ DynamicTexture (src/SkyRendering/VolumetricCloudDefaultMaterial.h:20-55):
+  a generated UNORM8 texture with its mip chain, regenerated when its
+  parameters change (GenerateIfParameterChanged).
+* ``VolumetricCloud.render`` ~ the raymarch pass of VolumetricCloud::Render
+  (src/SkyRendering/VolumetricCloud.cpp:361-385) at full resolution.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _abi
+from .atmosphere import Context, LutSet, _ptr
+
+
+class NoiseTexture:
+    def __init__(self, desc: _abi.NoiseTextureDesc, device="cuda"):
+        self.desc = desc
+        lib = _abi.lib()
+        self.levels = lib.skyr_noise_texture_levels(C.byref(desc))
+        if self.levels == 0:
+            _abi.check(_abi.SKYR_EINVAL, "skyr_noise_texture_levels")
+        self.nbytes = lib.skyr_noise_level_offset(C.byref(desc), self.levels)
+        self.data = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
+        self.expanded = None
+        self.expanded_channels = 0
+        self._generated = None
+
+    def level_offset(self, level: int) -> int:
+        return _abi.lib().skyr_noise_level_offset(C.byref(self.desc), level)
+
+    def level(self, level: int) -> torch.Tensor:
+        """Level `level` as a (channels, d, h, w) view."""
+        d = self.desc
+        w, h, dd = max(d.width >> level, 1), max(d.height >> level, 1), max(d.depth >> level, 1)
+        o = self.level_offset(level)
+        return self.data[o:o + w * h * dd * d.channels].view(d.channels, dd, h, w)
+
+    def generate(self, ctx: Context) -> "NoiseTexture":
+        _abi.call("skyr_noise_generate", ctx.handle, C.byref(self.desc), _ptr(self.data))
+        self._generated = bytes(self.desc)
+        if self.expanded is not None:
+            self.expand(ctx, self.expanded_channels)
+        return self
+
+    def expand(self, ctx: Context, channels: int) -> "NoiseTexture":
+        """Build the filtering layout of level 0 for the first `channels` channels."""
+        n = _abi.lib().skyr_noise_expanded_bytes(C.byref(self.desc), channels)
+        if n == 0:
+            _abi.check(_abi.SKYR_EINVAL, "skyr_noise_expanded_bytes")
+        if self.expanded is None or self.expanded.numel() != n:
+            self.expanded = torch.empty(n, dtype=torch.uint8, device=self.data.device)
+        _abi.call("skyr_noise_expand", ctx.handle, C.byref(self.desc), _ptr(self.data), channels,
+                  _ptr(self.expanded))
+        self.expanded_channels = channels
+        return self
+
+    def generate_if_parameter_changed(self, ctx: Context) -> bool:
+        if self._generated != bytes(self.desc):
+            self.generate(ctx)
+            return True
+        return False
+
+
+def textures_struct(cloud_map: NoiseTexture | None = None, detail: NoiseTexture | None = None,
+                    displacement: NoiseTexture | None = None, voxel: NoiseTexture | None = None):
+    t = _abi.CloudTextures()
+    for name, tex in (("cloud_map", cloud_map), ("detail", detail), ("displacement", displacement),
+                      ("voxel", voxel)):
+        if tex is not None:
+            setattr(t, name, tex.data.data_ptr())
+            setattr(t, name + "_desc", tex.desc)
+            if tex.expanded is not None:
+                setattr(t, name + "_expanded", tex.expanded.data_ptr())
+                setattr(t, name + "_expanded_channels", tex.expanded_channels)
+    return t
+
+
+# channels of each texture that a material's SampleSigmaT filters at level 0
+MATERIAL_CHANNELS = {
+    _abi.SKYR_MATERIAL_DEFAULT1: {"cloud_map": 1, "detail": 1},
+    _abi.SKYR_MATERIAL_DEFAULT0: {"cloud_map": 2, "detail": 1, "displacement": 4},
+    _abi.SKYR_MATERIAL_MINIMAL: {},
+    _abi.SKYR_MATERIAL_VOXEL: {},
+}
+
+
+def prepare_textures(ctx: Context, material_type: int, textures: dict) -> dict:
+    """Expand the level-0 channels that `material_type` filters (exact re-layout)."""
+    for name, ch in MATERIAL_CHANNELS[material_type].items():
+        if name in textures and textures[name].expanded_channels < ch:
+            textures[name].expand(ctx, ch)
+    return textures
+
+
+class VolumetricCloud:
+    """VolumetricCloud (src/SkyRendering/VolumetricCloud.h:16-193): parameters,
+    material and the textures its material samples."""
+
+    def __init__(self, ctx: Context, params: _abi.CloudParameters, material: _abi.CloudMaterial,
+                 textures: _abi.CloudTextures):
+        self.ctx, self.params, self.material, self.textures = ctx, params, material, textures
+
+    def render(self, atmosphere: _abi.AtmosphereParameters, view: _abi.CloudView, sizes: _abi.LutSizes,
+               luts: LutSet, blue_noise: torch.Tensor, depth: torch.Tensor | None = None,
+               out_rgba: torch.Tensor | None = None, out_distance: torch.Tensor | None = None):
+        if out_rgba is None:
+            out_rgba = torch.empty((view.height, view.width, 4), dtype=torch.float16, device="cuda")
+        if out_distance is None:
+            out_distance = torch.empty((view.height, view.width), dtype=torch.float32, device="cuda")
+        _abi.call("skyr_cloud_render", self.ctx.handle, C.byref(atmosphere), C.byref(self.params),
+                  C.byref(self.material), C.byref(self.textures), C.byref(view), C.byref(sizes),
+                  _ptr(luts.transmittance), _ptr(luts.aerial_perspective_luminance),
+                  _ptr(luts.aerial_perspective_transmittance), _ptr(blue_noise), _ptr(depth), _ptr(out_rgba),
+                  _ptr(out_distance))
+        return out_rgba, out_distance
+
+
+def blue_noise_tile(seed: int = 0x5EED) -> torch.Tensor:
+    """Seeded 64x64 blue-noise tile (host float32)."""
+    out = (C.c_float * 4096)()
+    _abi.call("skyr_blue_noise_generate", C.c_uint32(seed), out)
+    return torch.frombuffer(bytearray(out), dtype=torch.float32).view(64, 64).clone()

@@ -14,74 +14,14 @@
 //    lane) reduced with shuffles instead of a shared-memory tree.
 #include "skyr_internal.cuh"
 #include "atmosphere_kernels.cuh"
+#include "lut_access.cuh"
 
 namespace skyr {
-
-// ---------------------------------------------------------------------------
-// LUT storage access
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float3 load_rgb(const float4* p, int i) {
-    float4 v = __ldg(p + i);
-    return f3(v.x, v.y, v.z);
-}
-__device__ __forceinline__ float3 load_rgb(const __half2* p, int i) {  // half4 = 2 x half2
-    uint2 raw = __ldg(reinterpret_cast<const uint2*>(p) + i);
-    __half2 a = *reinterpret_cast<__half2*>(&raw.x);
-    __half2 b = *reinterpret_cast<__half2*>(&raw.y);
-    float2 fa = __half22float2(a), fb = __half22float2(b);
-    return f3(fa.x, fa.y, fb.x);
-}
-__device__ __forceinline__ void store_rgba(float4* p, size_t i, float3 v, float a) {
-    p[i] = make_float4(v.x, v.y, v.z, a);
-}
-__device__ __forceinline__ void store_rgba(__half2* p, size_t i, float3 v, float a) {
-    __half2 lo = __floats2half2_rn(v.x, v.y), hi = __floats2half2_rn(v.z, a);
-    uint2 raw;
-    raw.x = *reinterpret_cast<uint32_t*>(&lo);
-    raw.y = *reinterpret_cast<uint32_t*>(&hi);
-    reinterpret_cast<uint2*>(p)[i] = raw;
-}
-
-// GL LINEAR + CLAMP_TO_EDGE fetch at continuous texel coordinate (x, y) =
-// (u*W - 0.5, v*H - 0.5).
-template <class S>
-__device__ __forceinline__ float3 bilinear_clamp(const S* lut, int w, int h, float x, float y) {
-    float fx = floorf(x), fy = floorf(y);
-    float a = x - fx, b = y - fy;
-    int x0 = (int)fx, y0 = (int)fy;
-    int x1 = min(max(x0 + 1, 0), w - 1), y1 = min(max(y0 + 1, 0), h - 1);
-    x0 = min(max(x0, 0), w - 1);
-    y0 = min(max(y0, 0), h - 1);
-    float3 t00 = load_rgb(lut, y0 * w + x0), t10 = load_rgb(lut, y0 * w + x1);
-    float3 t01 = load_rgb(lut, y1 * w + x0), t11 = load_rgb(lut, y1 * w + x1);
-    float3 top = t00 + (t10 - t00) * a;
-    float3 bot = t01 + (t11 - t01) * a;
-    return top + (bot - top) * b;
-}
 
 struct LutView {
     const float4* t;
     int tw, th;
 };
-
-// GetTransmittanceToTopAtmosphereBoundary x horizon smoothstep = GetSunVisibility
-// (Atmosphere.glsl:90-117) at a point of radius r with rho2 = r^2 - R^2 and
-// altitude h = r - R.
-__device__ __forceinline__ float3 sun_visibility(const AtmoConsts& A, const LutView& L, float r, float inv_r,
-                                                 float rho2, float h, float mu_s) {
-    float rho = sqrtf(fmaxf(rho2, 0.f));
-    float d_min = A.thickness - h;
-    float d = dist_to_top(r, d_min, A.top, mu_s);
-    float d_max = rho + A.Hh;
-    float x_mu = __fdividef(d - d_min, d_max - d_min);
-    float x_r = rho * A.inv_Hh;
-    float3 t = bilinear_clamp(L.t, L.tw, L.th, x_mu * (float)(L.tw - 1), x_r * (float)(L.th - 1));
-    // smoothstep(-e, e, mu_s - cos_h) with e = (R / r) alpha and cos_h = -rho / r:
-    // the normalised argument is 1/2 + (mu_s r + rho) / (2 R alpha)
-    float u = clamp01(fmaf(fmaf(mu_s, r, rho), A.inv_2R_alpha, 0.5f));
-    (void)inv_r;
-    return t * (u * u * (3.f - 2.f * u));
-}
 
 // GetMultiscatteringContribution (Atmosphere.glsl:169-178)
 template <class S>
@@ -167,7 +107,7 @@ __device__ __forceinline__ void integrate(const AtmoConsts& A, const LutView& L,
         phi.x = seg_phi(ext.x * dx, tr_i.x);
         phi.y = seg_phi(ext.y * dx, tr_i.y);
         phi.z = seg_phi(ext.z * dx, tr_i.z);
-        float3 sv = sun_visibility(A, L, r_i, inv_r, s, h_i, mu_s_i);
+        float3 sv = sun_visibility_lut(A, L.t, L.tw, L.th, r_i, s, h_i, mu_s_i);
         float3 li = (ray_s * ph_r + mie_s * ph_m) * sv;
         float3 sc = ray_s + mie_s;
         if constexpr (!MS) {
@@ -297,7 +237,7 @@ __global__ void __launch_bounds__(kMsThreads) multiscattering_kernel(JobSrc<TABL
     if (chunk == 0 && ground) {
         // ComputeGroundLuminance (Atmosphere.glsl:297-306) at r = R
         float mu_s_g = (r * mu_s + dist * s0.nu) / A.R;
-        float3 sv = sun_visibility(A, Ls, A.R, 1.f / A.R, 0.f, 0.f, mu_s_g);
+        float3 sv = sun_visibility_lut(A, Ls.t, Ls.tw, Ls.th, A.R, 0.f, 0.f, mu_s_g);
         lum += tr * (A.ground_albedo * sv * (clamp01(mu_s_g) / SKYR_PI));
     }
     if (chunk != 0) lum = lf = f3(0.f);

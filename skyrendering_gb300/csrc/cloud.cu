@@ -1,0 +1,722 @@
+// cloud.cu — the volumetric-cloud raymarch (VolumetricCloudRender.comp) with
+// the material plug-ins (SampleSigmaT) for sm_103a.
+//
+// One thread per pixel, each warp an 8x4 pixel tile so that the rays of a warp
+// stay coherent through the cloud layer (their texture reads share cache lines).
+// Texture filtering is done in software in FP32 with GL's exact rules (hardware
+// texture units interpolate with 8-bit weights).  The shell intersections use
+// cancellation-free FP32 forms; all frame derivations are done on the host in
+// double.
+#include <cmath>
+#include <cstring>
+
+#include "atmosphere_kernels.cuh"
+#include "cloud_internal.cuh"
+#include "lut_access.cuh"
+#include "skyr_ctx.cuh"
+
+namespace skyr {
+
+// ---------------------------------------------------------------------------
+// Host derivation
+// ---------------------------------------------------------------------------
+namespace {
+struct D3 {
+    double x, y, z;
+};
+D3 sub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+D3 add(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+D3 mul(D3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+double dotd(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+D3 crossd(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+D3 normd(D3 a) { return mul(a, 1.0 / std::sqrt(dotd(a, a))); }
+float3 tof(D3 a) { return make_float3((float)a.x, (float)a.y, (float)a.z); }
+
+bool inv4(const double* m, double* out) {
+    double w[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            w[r][c] = m[c * 4 + r];
+            w[r][c + 4] = r == c ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 4; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 4; ++r)
+            if (std::fabs(w[r][c]) > std::fabs(w[p][c])) p = r;
+        if (w[p][c] == 0.0) return false;
+        if (p != c)
+            for (int k = 0; k < 8; ++k) std::swap(w[c][k], w[p][k]);
+        double iv = 1.0 / w[c][c];
+        for (int k = 0; k < 8; ++k) w[c][k] *= iv;
+        for (int r = 0; r < 4; ++r) {
+            if (r == c) continue;
+            double f = w[r][c];
+            for (int k = 0; k < 8; ++k) w[r][k] -= f * w[c][k];
+        }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) out[c * 4 + r] = w[r][c + 4];
+    return true;
+}
+
+void matmul4(const double* a, const double* b, double* c) {  // column-major c = a b
+    for (int r = 0; r < 4; ++r)
+        for (int col = 0; col < 4; ++col) {
+            double s = 0;
+            for (int k = 0; k < 4; ++k) s += a[k * 4 + r] * b[col * 4 + k];
+            c[col * 4 + r] = s;
+        }
+}
+
+int fill_tex(DTex& t, const void* p, const skyr_noise_texture_desc& d, bool border, bool required,
+             const char* what, const void* ex, int ex_channels) {
+    std::memset(&t, 0, sizeof(t));
+    if (!p) {
+        if (required) return set_error(SKYR_EINVAL, "material needs the %s texture", what);
+        t.w = t.h = t.d = t.levels = 1;
+        return SKYR_OK;
+    }
+    if (int st = validate_noise_desc(&d, false)) return st;
+    t.base = reinterpret_cast<const uint8_t*>(p);
+    t.w = d.width;
+    t.h = d.height;
+    t.d = d.depth;
+    t.levels = noise_levels(&d);
+    if (t.levels > kMaxLevels) return set_error(SKYR_EINVAL, "%s texture has too many mip levels", what);
+    t.border = border ? 1 : 0;
+    t.channels = d.channels;
+    if (ex) {
+        if (ex_channels < 1 || ex_channels > d.channels)
+            return set_error(SKYR_EINVAL, "%s expanded texture: bad channel count %d", what, ex_channels);
+        if (d.depth > 1 && (d.width < 2 || d.height < 2))
+            return set_error(SKYR_EINVAL, "%s expanded texture: 3D needs width, height >= 2", what);
+        t.ex = ex;
+        t.ex_channels = ex_channels;
+    }
+    return SKYR_OK;
+}
+}  // namespace
+
+// VolumetricCloud::Update (VolumetricCloud.cpp:168-280), the material Update
+// (VolumetricCloudDefaultMaterial.cpp:84-101,451-463; VolumetricCloudVoxelMaterial.cpp:93-105)
+// and CalKLod (VolumetricCloudDefaultMaterial.cpp:24-28).
+int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud_parameters& cp,
+                        const skyr_cloud_material& m, const skyr_cloud_textures& tex, const skyr_cloud_view& v,
+                        const skyr_lut_sizes& sizes, CloudConsts& c, MaterialConsts& mc) {
+    std::memset(&c, 0, sizeof(c));
+    std::memset(&mc, 0, sizeof(mc));
+    const double deg = M_PI / 180.0;
+    double R = atmo.bottom_radius;
+    D3 center{0.0, -R, 0.0};
+    D3 cam{v.camera_position[0], v.camera_position[1], v.camera_position[2]};
+    D3 up = normd(sub(cam, center));
+    D3 origin = add(center, mul(up, R));
+    D3 front = normd(crossd(up, D3{1.0, 0.0, 0.0}));
+    D3 right = normd(crossd(up, front));
+    double model[16] = {front.x, front.y, front.z, 0, right.x, right.y, right.z, 0,
+                        up.x,    up.y,    up.z,    0, origin.x, origin.y, origin.z, 1};
+    double vp[16], mvp[16], imvp[16];
+    for (int i = 0; i < 16; ++i) vp[i] = v.view_projection[i];
+    matmul4(vp, model, mvp);
+    if (!inv4(mvp, imvp)) return set_error(SKYR_EINVAL, "view_projection is singular");
+    // local camera: the model is a rotation + translation, inverse = transpose
+    D3 rel = sub(cam, origin);
+    D3 cam_l{dotd(front, rel), dotd(right, rel), dotd(up, rel)};
+    D3 sun_w{std::cos(v.sun_direction_phi * deg) * std::sin(v.sun_direction_theta * deg),
+             std::cos(v.sun_direction_theta * deg),
+             std::sin(v.sun_direction_phi * deg) * std::sin(v.sun_direction_theta * deg)};
+    D3 sun_l = normd(D3{dotd(front, sun_w), dotd(right, sun_w), dotd(up, sun_w)});
+    auto col = [&](int k) { return D3{imvp[k * 4 + 0], imvp[k * 4 + 1], imvp[k * 4 + 2]}; };
+    auto colw = [&](int k) { return imvp[k * 4 + 3]; };
+    c.a0 = tof(sub(col(0), mul(cam_l, colw(0))));
+    c.a1 = tof(sub(col(1), mul(cam_l, colw(1))));
+    c.a2 = tof(sub(col(2), mul(cam_l, colw(2))));
+    c.af = tof(add(sub(col(2), mul(cam_l, colw(2))), sub(col(3), mul(cam_l, colw(3)))));
+    c.w0 = (float)colw(0);
+    c.w1 = (float)colw(1);
+    c.w2 = (float)colw(2);
+    c.wf = (float)(colw(2) + colw(3));
+    c.cam = tof(cam_l);
+    c.sun = tof(sun_l);
+    c.R = (float)R;
+    c.bottom = cp.bottom_altitude;
+    c.top = (float)((double)cp.bottom_altitude + cp.thickness);
+    c.rb = (float)(R + cp.bottom_altitude);
+    c.rt = (float)(R + (double)cp.bottom_altitude + cp.thickness);
+    c.inv_layer = (float)(1.0 / cp.thickness);
+    {
+        double b = cp.bottom_altitude, tp = (double)cp.bottom_altitude + cp.thickness, h = cam_l.z;
+        c.rho2_bottom = (float)(b * (2.0 * R + b));
+        c.rho2_top = (float)(tp * (2.0 * R + tp));
+        c.cam_rho2 = (float)(h * (2.0 * R + h));
+    }
+    c.jitter_offset = (float)v.frame_id * 0.61803398875f;
+    c.sun_illuminance_scale = cp.sun_illuminance_scale;
+    c.max_raymarch_distance = cp.max_raymarch_distance;
+    c.max_raymarch_steps = cp.max_raymarch_steps;
+    c.max_visible_distance = cp.max_visible_distance;
+    c.env_color_scale = make_float3(cp.env_color[0] * cp.env_color_scale, cp.env_color[1] * cp.env_color_scale,
+                                    cp.env_color[2] * cp.env_color_scale);
+    c.shadow_steps = cp.shadow_steps;
+    c.sun_ms_sigma_scale = cp.sun_multiscattering_sigma_scale;
+    c.env_ms_sigma_scale = cp.env_multiscattering_sigma_scale;
+    c.shadow_distance = cp.shadow_distance;
+    c.env_bottom_visibility = cp.env_bottom_visibility;
+    c.env_sun_height_curve_exp = cp.env_sun_height_curve_exp;
+    c.g_fwd = cp.phase_g_forward;
+    c.g_back = cp.phase_g_back;
+    c.back_scale = cp.phase_back_scale;
+    c.ap_max_distance = v.aerial_perspective_lut_max_distance;
+    c.inv_ap_max_distance = (float)(1.0 / v.aerial_perspective_lut_max_distance);
+    double cam_r = R + cam_l.z;
+    c.atmo_in_space = cam_r > R + (double)atmo.thickness ? 1.f : 0.f;
+    c.width = v.width;
+    c.height = v.height;
+    c.ap_w = sizes.aerial_perspective_width;
+    c.ap_h = sizes.aerial_perspective_height;
+    c.ap_d = sizes.aerial_perspective_depth;
+
+    mc.type = m.type;
+    mc.min2d = m.minfilter2d;
+    mc.min3d = m.minfilter3d;
+    mc.mindisp = m.minfilter_displacement;
+    double tan_half = std::tan(v.fovy * deg * 0.5);
+    double vmin = std::min(v.viewport_width, v.viewport_height);
+    auto info = [&](const skyr_noise_texture_desc& d, double repeat, double ox, double oy) {
+        SampleInfoD s;
+        s.frequency = (float)(1.0 / repeat);
+        s.bias_x = (float)(ox / repeat - std::floor(ox / repeat));
+        s.bias_y = (float)(oy / repeat - std::floor(oy / repeat));
+        double maxw = std::max(d.width, std::max(d.height, d.depth));
+        s.k_lod = (float)(maxw * tan_half / (repeat * vmin));
+        return s;
+    };
+    double ox = m.offset_from_first[0], oy = m.offset_from_first[1];
+    mc.cloud_map = info(tex.cloud_map_desc, m.cloud_map_repeat_size, ox, oy);
+    mc.detail = info(tex.detail_desc, m.detail_repeat_size, ox + m.detail_offset_from_first[0],
+                     oy + m.detail_offset_from_first[1]);
+    mc.displacement = info(tex.displacement_desc, m.displacement_repeat_size, ox, oy);
+    mc.lod_bias = m.lod_bias;
+    mc.density = m.density;
+    mc.m1_threshold = m.base_density_threshold;
+    mc.m1_height_hardness = m.base_height_hardness;
+    mc.m1_edge_hardness = m.base_edge_hardness;
+    mc.m1_detail_base = m.detail_base;
+    mc.m1_detail_scale = m.detail_scale;
+    mc.m1_height_cut = 1.f - m.height_cut;
+    mc.m1_edge_cut = m.edge_cut;
+    mc.m0_detail_x = m.detail_param[0];
+    mc.m0_detail_y = m.detail_param[1];
+    mc.m0_disp_scale = m.displacement_scale;
+    mc.vx_freq_x = (float)(1.0 / m.voxel_width[0]);
+    mc.vx_freq_y = (float)(1.0 / m.voxel_width[1]);
+    mc.vx_bias_x = (float)((ox + m.voxel_base[0]) / m.voxel_width[0]);
+    mc.vx_bias_y = (float)((oy + m.voxel_base[1]) / m.voxel_width[1]);
+    {
+        const skyr_noise_texture_desc& d = tex.voxel_desc;
+        double maxw = std::max(d.width, std::max(d.height, d.depth));
+        mc.vx_k_lod = (float)(maxw * tan_half / (std::min(m.voxel_width[0], m.voxel_width[1]) * vmin));
+    }
+    bool d0 = m.type == SKYR_MATERIAL_DEFAULT0, d1 = m.type == SKYR_MATERIAL_DEFAULT1;
+    if (int st = fill_tex(mc.cloud_map_tex, tex.cloud_map, tex.cloud_map_desc, false, d0 || d1, "cloud map",
+                          tex.cloud_map_expanded, tex.cloud_map_expanded_channels))
+        return st;
+    if (int st = fill_tex(mc.detail_tex, tex.detail, tex.detail_desc, false, d0 || d1, "detail", tex.detail_expanded,
+                          tex.detail_expanded_channels))
+        return st;
+    if (int st = fill_tex(mc.displacement_tex, tex.displacement, tex.displacement_desc, false, d0, "displacement",
+                          tex.displacement_expanded, tex.displacement_expanded_channels))
+        return st;
+    if (int st = fill_tex(mc.voxel_tex, tex.voxel, tex.voxel_desc, true, m.type == SKYR_MATERIAL_VOXEL, "voxel",
+                          nullptr, 0))
+        return st;
+    if (d0 && tex.displacement_desc.channels < 4) return set_error(SKYR_EINVAL, "displacement texture needs 4 channels");
+    if ((d0 || d1) && tex.cloud_map_desc.channels < 2) return set_error(SKYR_EINVAL, "cloud map needs 2 channels");
+    return SKYR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Device: material SampleSigmaT
+// ---------------------------------------------------------------------------
+// CalHeight01 (VolumetricCloudCommon.glsl:36-39) with the altitude formed as
+// (x^2 + y^2 + z (z + 2R)) / (|p + R z^| + R) (no cancellation).
+__device__ __forceinline__ float height01(const CloudConsts& C, float3 p) {
+    float rho2 = fmaf(p.x, p.x, fmaf(p.y, p.y, p.z * (p.z + 2.f * C.R)));
+    float r = sqrtf(fmaf(C.R, C.R, rho2));
+    float alt = __fdividef(rho2, r + C.R);
+    return clamp01((alt - C.bottom) * C.inv_layer);
+}
+
+// height01 of a point with rho2 = |p + R z^|^2 - R^2 already known
+__device__ __forceinline__ float height01_rho2(const CloudConsts& C, float rho2) {
+    float r = sqrtf(fmaf(C.R, C.R, rho2));
+    float alt = __fdividef(rho2, r + C.R);
+    return clamp01((alt - C.bottom) * C.inv_layer);
+}
+
+__device__ __forceinline__ float sample_sigma_t(const MaterialConsts& M, float3 p, float h01, float dist_to_cam) {
+    switch (M.type) {
+        case SKYR_MATERIAL_DEFAULT1: {
+            // VolumetricCloudDefaultMaterial1.glsl:14-29
+            float u = fmaf(p.x, M.cloud_map.frequency, M.cloud_map.bias_x);
+            float v = fmaf(p.y, M.cloud_map.frequency, M.cloud_map.bias_y);
+            float lg = __log2f(dist_to_cam);
+            float cr = dtex_sample(M.cloud_map_tex, 0, u, v, 0.f, __log2f(M.cloud_map.k_lod) + lg + M.lod_bias,
+                                   M.min2d);
+            float density = clamp01((cr - M.m1_threshold) * M.m1_edge_hardness);
+            density *= clamp01((1.f - h01) * M.m1_height_hardness);
+            if (density == 0.f) return 0.f;
+            float du = fmaf(p.x, M.detail.frequency, M.detail.bias_x);
+            float dv = fmaf(p.y, M.detail.frequency, M.detail.bias_y);
+            float dw = p.z * M.detail.frequency;
+            float dt = dtex_sample(M.detail_tex, 0, du, dv, dw, __log2f(M.detail.k_lod) + lg + M.lod_bias, M.min3d);
+            dt = (dt + M.m1_detail_base) * M.m1_detail_scale;
+            dt *= fmaxf(clamp01(h01 - M.m1_height_cut), clamp01(M.m1_edge_cut - cr));
+            return clamp01(density - dt) * M.density * h01;
+        }
+        case SKYR_MATERIAL_MINIMAL: return M.density;
+        default: return 0.f;
+    }
+}
+
+// Material0 and Voxel need the camera position for the LOD of a displaced /
+// arbitrary point; they are evaluated here.
+__device__ __forceinline__ float sigma_t(const CloudConsts& C, const MaterialConsts& M, float3 p, float h01,
+                                         float dist_to_cam) {
+    if (M.type == SKYR_MATERIAL_DEFAULT1 || M.type == SKYR_MATERIAL_MINIMAL)
+        return sample_sigma_t(M, p, h01, dist_to_cam);
+    if (M.type == SKYR_MATERIAL_DEFAULT0) {
+        float lg = __log2f(dist_to_cam);
+        float u = fmaf(p.x, M.cloud_map.frequency, M.cloud_map.bias_x);
+        float v = fmaf(p.y, M.cloud_map.frequency, M.cloud_map.bias_y);
+        float lod = __log2f(M.cloud_map.k_lod) + lg + M.lod_bias;
+        float cr = dtex_sample(M.cloud_map_tex, 0, u, v, 0.f, lod, M.min2d);
+        float cg = dtex_sample(M.cloud_map_tex, 1, u, v, 0.f, lod, M.min2d);
+        float xu = fmaf(p.x, M.displacement.frequency, M.displacement.bias_x);
+        float xv = fmaf(p.y, M.displacement.frequency, M.displacement.bias_y);
+        float xw = p.z * M.displacement.frequency;
+        float xl = __log2f(M.displacement.k_lod) + lg + M.lod_bias;
+        float3 disp;
+        disp.x = dtex_sample(M.displacement_tex, 0, xu, xv, 0.f, xl, M.mindisp) +
+                 dtex_sample(M.displacement_tex, 2, xu, xw, 0.f, xl, M.mindisp);
+        disp.y = dtex_sample(M.displacement_tex, 1, xu, xv, 0.f, xl, M.mindisp);
+        disp.z = dtex_sample(M.displacement_tex, 3, xu, xw, 0.f, xl, M.mindisp);
+        float3 q = p + disp * M.m0_disp_scale;
+        float3 dq = q - C.cam;
+        float dl = __log2f(sqrtf(dot3(dq, dq)));
+        float du = fmaf(q.x, M.detail.frequency, M.detail.bias_x);
+        float dv = fmaf(q.y, M.detail.frequency, M.detail.bias_y);
+        float dw = q.z * M.detail.frequency;
+        float dt = dtex_sample(M.detail_tex, 0, du, dv, dw, __log2f(M.detail.k_lod) + dl + M.lod_bias, M.min3d);
+        dt = fmaf(dt, M.m0_detail_x, M.m0_detail_y);
+        // CalHeightMask (VolumetricCloudDefaultMaterial0.glsl:9-12)
+        float hit = clamp01(h01 / cg);
+        float mask = clamp01(hit * (hit - 1.f) * -4.f);
+        return clamp01((cr * mask - dt) / (1.f - dt)) * h01 * M.density;
+    }
+    if (M.type == SKYR_MATERIAL_VOXEL) {
+        // VolumetricCloudMaterialVoxel.glsl:12-16
+        float u = fmaf(p.x, M.vx_freq_x, M.vx_bias_x);
+        float v = fmaf(p.y, M.vx_freq_y, M.vx_bias_y);
+        float lod = __log2f(M.vx_k_lod * dist_to_cam) + M.lod_bias;
+        return dtex_sample(M.voxel_tex, 0, u, v, h01, lod, SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST) * M.density;
+    }
+    return 0.f;
+}
+
+// ---------------------------------------------------------------------------
+// Device: the raymarch
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float hg(float c, float g) {  // VolumetricCloudCommon.glsl:58-63
+    float a = 1.f - g * g;
+    float b = fmaf(-2.f * g, c, 1.f + g * g);
+    return (0.25f / SKYR_PI) * __fdividef(a, b * sqrtf(b));
+}
+
+// 1 - exp(-x) without cancellation (x >= 0); also returns exp(-x)
+__device__ __forceinline__ float one_minus_exp(float x, float& e) {
+    float phi = seg_phi(x, e);
+    return x * phi;
+}
+
+// SampleShadow (VolumetricCloudRender.comp:98-114).  The loop variable
+// accumulates in FP32 exactly as the reference's `t += inv_shadow_steps`.
+// Sample heights come from rho2(d) = rho2_p + d (2 q + d) with
+// q = sun . (p + R z^), exact relative to the primary sample.
+__device__ __forceinline__ float sample_shadow(const CloudConsts& C, const MaterialConsts& M, float3 pos,
+                                               float rho2_p) {
+    float od = 0.f;
+    float inv = 1.f / C.shadow_steps;
+    float3 sv = C.sun * C.shadow_distance;
+    float q2 = 2.f * fmaf(C.sun.x, pos.x, fmaf(C.sun.y, pos.y, C.sun.z * (pos.z + C.R)));
+    float prev = 0.f;
+    for (float t = inv; t <= 1.f; t += inv) {
+        float cur = t * t;
+        float dt = cur - prev;
+        float f = fmaf(0.5f, dt, prev);
+        float3 sp = pos + sv * f;
+        float d = C.shadow_distance * f;
+        float h = height01_rho2(C, fmaf(d, q2 + d, rho2_p));
+        float3 dc = sp - C.cam;
+        od += sigma_t(C, M, sp, h, sqrtf(dot3(dc, dc))) * C.shadow_distance * dt;
+        prev = cur;
+    }
+    return __expf(-od);
+}
+
+// number of light-march samples of `for (float t = inv; t <= 1; t += inv)`
+__device__ __forceinline__ unsigned shadow_sample_count(float steps) {
+    unsigned n = 0;
+    float inv = 1.f / steps;
+    for (float t = inv; t <= 1.f; t += inv) ++n;
+    return n;
+}
+
+struct March {
+    float trans, trans_sum, wsum, sun, env;
+    unsigned samples, evals;  // work counters (instrumented launches only)
+};
+
+// One shell segment [t0, t1] of the raymarch loop (VolumetricCloudRender.comp:160-187).
+// Sample heights are taken relative to the segment entry, whose
+// rho2_e = R_e^2 - R^2 is exact: rho2(t0 + e) = rho2_e + e (k_e + e) with
+// k_e = 2 (r mu + t0) = 2 R_e mu_e.
+__device__ __forceinline__ void march_segment(const CloudConsts& C, const MaterialConsts& M, float3 view,
+                                              float t0, float t1, float rho2_e, float k_e, float jitter,
+                                              float ph_back, float ph_fwd, March& S) {
+    float dist = fminf(t1 - t0, C.max_raymarch_distance);
+    unsigned n = (unsigned)fmaxf(C.max_raymarch_steps * (dist / C.max_raymarch_distance), 1.f);
+    float step = dist / (float)n;
+    float e = step * jitter;
+    float t = t0 + e;
+    for (unsigned k = n; k != 0; --k, t += step, e += step) {
+        float3 pos = C.cam + view * t;
+        float rho2 = fmaf(e, k_e + e, rho2_e);
+        float h = height01_rho2(C, rho2);
+        // RayMarchStep (VolumetricCloudRender.comp:116-137)
+        float sigma = sigma_t(C, M, pos, h, t);
+        S.samples++;
+        S.evals++;
+        if (sigma >= 1e-5f) {
+            S.evals += shadow_sample_count(C.shadow_steps);
+            float tr;
+            float one_m_tr = one_minus_exp(step * sigma, tr);
+            float tsun = sample_shadow(C, M, pos, rho2);
+            float w = __expf(-C.sun_ms_sigma_scale * sigma);
+            float phase = ph_back * (1.f - w) + ph_fwd * w;
+            float e_dummy;
+            float env = fmaf(h, 1.f - C.env_bottom_visibility, C.env_bottom_visibility) *
+                        one_minus_exp(C.env_ms_sigma_scale * sigma, e_dummy);
+            S.sun += S.trans * (tsun * phase) * one_m_tr;
+            S.env += S.trans * env * one_m_tr;
+            S.trans_sum += S.trans;
+            S.wsum += t * S.trans;
+            S.trans *= tr;
+        }
+        if (S.trans < 0.01f) break;
+    }
+}
+
+// Shell intersections (RayShellIntersect, VolumetricCloudRender.comp:39-71) in
+// cancellation-free form: with c = (R_x - r)(R_x + r), -r mu + sqrt(d) equals
+// c / (r mu + sqrt(d)) for mu > 0, and -r mu - sqrt(d) equals
+// -c / (-r mu + sqrt(d)) for mu < 0.
+__device__ __forceinline__ void shell_intersect(const CloudConsts& C, float mu, float t[4], float e[2]) {
+    float r = C.R + C.cam.z;
+    float rm = r * mu;
+    float cb = (C.bottom - C.cam.z) * (C.rb + r);
+    float ct = (C.top - C.cam.z) * (C.rt + r);
+    float db = fmaf(rm, rm, cb), dt = fmaf(rm, rm, ct);
+    float sb = sqrtf(fmaxf(db, 0.f)), st = sqrtf(fmaxf(dt, 0.f));
+    auto plus = [&](float c, float s) { return rm > 0.f ? c / (rm + s) : s - rm; };
+    auto minus = [&](float c, float s) { return -c / (s - rm); };
+    t[0] = t[1] = t[2] = t[3] = 0.f;
+    // entry rho2 of each segment: the bottom / top sphere or the camera
+    e[0] = C.cam_rho2;
+    e[1] = C.rho2_bottom;
+    if (C.cam.z < C.bottom) {
+        t[0] = plus(cb, sb);
+        t[1] = plus(ct, st);
+        e[0] = C.rho2_bottom;
+    } else if (C.cam.z < C.top) {
+        if (db >= 0.f && mu < 0.f) {
+            t[1] = minus(cb, sb);
+            t[2] = sb - rm;
+            t[3] = st - rm;
+        } else {
+            t[1] = plus(ct, st);
+        }
+    } else {
+        if (db >= 0.f && mu < 0.f) {
+            t[0] = minus(ct, st);
+            t[1] = minus(cb, sb);
+            t[2] = sb - rm;
+            t[3] = st - rm;
+            e[0] = C.rho2_top;
+        } else if (dt >= 0.f && mu < 0.f) {
+            t[0] = minus(ct, st);
+            t[1] = st - rm;
+            e[0] = C.rho2_top;
+        }
+    }
+}
+
+template <class S>
+__device__ __forceinline__ float3 trilinear_clamp(const S* lut, int w, int h, int d, float x, float y, float z) {
+    x = fminf(fmaxf(x, 0.f), (float)(w - 1));
+    y = fminf(fmaxf(y, 0.f), (float)(h - 1));
+    z = fminf(fmaxf(z, 0.f), (float)(d - 1));
+    int x0 = min((int)x, w - 2), y0 = min((int)y, h - 2), z0 = min((int)z, d - 2);
+    float a = x - (float)x0, b = y - (float)y0, g = z - (float)z0;
+    float3 r[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        int base = ((z0 + k) * h + y0) * w + x0;
+        float3 t00 = load_lut_rgb(lut, base), t10 = load_lut_rgb(lut, base + 1);
+        float3 t01 = load_lut_rgb(lut, base + w), t11 = load_lut_rgb(lut, base + w + 1);
+        float3 top = t00 + (t10 - t00) * a, bot = t01 + (t11 - t01) * a;
+        r[k] = top + (bot - top) * b;
+    }
+    return r[0] + (r[1] - r[0]) * g;
+}
+
+template <class S, bool COUNT>
+__global__ void __launch_bounds__(128, 4) cloud_render_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
+                                                           const float4* __restrict__ tlut, int tw, int th,
+                                                           const S* __restrict__ ap_lum,
+                                                           const S* __restrict__ ap_trans,
+                                                           const float* __restrict__ blue_noise,
+                                                           const float* __restrict__ depth,
+                                                           __half2* __restrict__ out_rgba,
+                                                           float* __restrict__ out_dist,
+                                                           unsigned long long* __restrict__ counters) {
+    // 16x8 pixels per block, 8x4 per warp
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    int py = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+    if (px >= C.width || py >= C.height) return;
+    size_t pix = (size_t)py * C.width + px;
+    float u = ((float)px + 0.5f) / (float)C.width, v = ((float)py + 0.5f) / (float)C.height;
+    float x = 2.f * u - 1.f, y = 2.f * v - 1.f;
+    float e = depth ? 2.f * (__ldg(depth + pix) - 1.f) : 0.f;
+    float3 dir = C.a0 * x + C.a1 * y + C.a2 * e + C.af;
+    float wv = fmaf(C.w0, x, fmaf(C.w1, y, fmaf(C.w2, e, C.wf)));
+    float len = sqrtf(dot3(dir, dir));
+    float3 view = dir * (copysignf(1.f, wv) / len);
+    float frag_dist = len / fabsf(wv);
+    float mu = view.z;
+    float it[4], ent[2];
+    shell_intersect(C, mu, it, ent);
+    float vis = fminf(frag_dist, C.max_visible_distance);
+    it[1] = fminf(fmaxf(vis, it[0]), it[1]);
+    it[3] = fminf(fmaxf(vis, it[2]), it[3]);
+    float cos_sv = dot3(C.sun, view);
+    float ph_back = hg(cos_sv, C.g_back) * C.back_scale, ph_fwd = hg(cos_sv, C.g_fwd);
+    float noise = __ldg(blue_noise + (py & 63) * 64 + (px & 63));
+    float j = noise + C.jitter_offset;
+    float jitter = j - floorf(j);
+    March mk{1.f, 0.f, 0.f, 0.f, 0.f, 0u, 0u};
+    float rmu = (C.R + C.cam.z) * mu;
+    march_segment(C, M, view, it[0], it[1], ent[0], 2.f * (rmu + it[0]), jitter, ph_back, ph_fwd, mk);
+    if (it[3] - it[2] > 0.f)
+        march_segment(C, M, view, it[2], it[3], ent[1], 2.f * (rmu + it[2]), jitter, ph_back, ph_fwd, mk);
+
+    float avg_t = mk.wsum == 0.f ? frag_dist : mk.wsum / mk.trans_sum;
+    float3 ap = C.cam + view * avg_t;
+    // GetSunVisibility(transmittance_texture, pos) at the mean depth
+    float rho2 = fmaf(ap.x, ap.x, fmaf(ap.y, ap.y, ap.z * (ap.z + 2.f * C.R)));
+    float r2 = fmaf(C.R, C.R, rho2);
+    float inv_r = rsqrtf(r2);
+    float rr = r2 * inv_r;
+    float hh = __fdividef(rho2, rr + C.R);
+    float mu_s = fmaf(C.sun.x, ap.x, fmaf(C.sun.y, ap.y, C.sun.z * (ap.z + C.R))) * inv_r;
+    float3 sunvis = sun_visibility_lut(A, tlut, tw, th, rr, rho2, hh, mu_s);
+    float sun_cos = clamp01(mu_s);
+    float3 lum = sunvis * (mk.sun * C.sun_illuminance_scale) * A.solar_illuminance +
+                 C.env_color_scale * (mk.env * __powf(sun_cos, C.env_sun_height_curve_exp));
+    // GetAerialPerspective (VolumetricCloudCommon.glsl:81-98)
+    float ta = avg_t;
+    if (C.atmo_in_space != 0.f) {
+        float r = C.R + C.cam.z, rm = r * mu;
+        float c = (C.cam.z - A.thickness) * (r + A.top);
+        float disc = rm * rm - c;
+        if (mu < 0.f && disc >= 0.f) ta -= fmaxf(c / (-rm + sqrtf(disc)), 0.f);
+        else ta = 0.f;
+    }
+    float wz = sqrtf(fmaxf(ta, 0.f) * C.inv_ap_max_distance);
+    float3 at = trilinear_clamp(ap_trans, C.ap_w, C.ap_h, C.ap_d, u * (float)(C.ap_w - 1), v * (float)(C.ap_h - 1),
+                                wz * (float)(C.ap_d - 1));
+    float3 al = trilinear_clamp(ap_lum, C.ap_w, C.ap_h, C.ap_d, u * (float)(C.ap_w - 1), v * (float)(C.ap_h - 1),
+                                wz * (float)(C.ap_d - 1));
+    lum = lum * at + al * (1.f - mk.trans);
+    lum = lum * (1.f / fmaxf(1e-5f, 1.f - mk.trans));
+    float fade = smoothstepf(C.max_visible_distance * 0.75f, C.max_visible_distance, it[0]);
+    float trans = mk.trans + (1.f - mk.trans) * fade;
+    lum = lum * (1.f - trans);
+    if (out_rgba) {
+        __half2 lo = __floats2half2_rn(lum.x, lum.y), hi = __floats2half2_rn(lum.z, trans);
+        uint2 raw;
+        raw.x = *reinterpret_cast<uint32_t*>(&lo);
+        raw.y = *reinterpret_cast<uint32_t*>(&hi);
+        reinterpret_cast<uint2*>(out_rgba)[pix] = raw;
+    }
+    if (out_dist) out_dist[pix] = avg_t;
+    if constexpr (COUNT) {
+        unsigned long long a = mk.samples, b = mk.evals;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(__activemask(), a, o);
+            b += __shfl_xor_sync(__activemask(), b, o);
+        }
+        if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) {
+            atomicAdd(counters, a);
+            atomicAdd(counters + 1, b);
+        }
+    }
+}
+
+}  // namespace skyr
+
+using namespace skyr;
+
+extern "C" {
+
+}  // extern "C"
+
+namespace {
+template <bool COUNT>
+int cloud_render_impl(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                      const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                      const skyr_cloud_textures* textures, const skyr_cloud_view* view,
+                      const skyr_lut_sizes* sizes, const void* transmittance,
+                      const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
+                      const float* blue_noise, const float* depth, void* out_rgba, float* out_distance,
+                      unsigned long long* counters) {
+    if (!ctx) return set_error(SKYR_EINVAL, "null context");
+    if (!atmosphere || !cloud || !material || !textures || !view || !sizes)
+        return set_error(SKYR_EINVAL, "null parameter block");
+    if (!transmittance || !aerial_perspective_luminance || !aerial_perspective_transmittance || !blue_noise)
+        return set_error(SKYR_EINVAL, "null LUT or blue-noise input");
+    if (view->width < 1 || view->height < 1 || view->width > 16384 || view->height > 16384)
+        return set_error(SKYR_EINVAL, "render size must be in [1, 16384]");
+    if (view->viewport_width < 1 || view->viewport_height < 1) return set_error(SKYR_EINVAL, "bad viewport size");
+    if (material->type < SKYR_MATERIAL_DEFAULT0 || material->type > SKYR_MATERIAL_VOXEL)
+        return set_error(SKYR_EINVAL, "unknown material type %d", material->type);
+    if (!(cloud->thickness > 0.f) || !(cloud->max_raymarch_distance > 0.f) || !(cloud->max_raymarch_steps >= 1.f) ||
+        cloud->max_raymarch_steps > 4096.f || !(cloud->shadow_steps > 0.f) || cloud->shadow_steps > 256.f)
+        return set_error(SKYR_EINVAL, "cloud parameters out of range");
+    if (sizes->aerial_perspective_width < 2 || sizes->aerial_perspective_height < 2 ||
+        sizes->aerial_perspective_depth < 2 || sizes->transmittance_width < 2 || sizes->transmittance_height < 2)
+        return set_error(SKYR_EINVAL, "LUT sizes must be >= 2");
+    if (!(view->aerial_perspective_lut_max_distance > 0.f)) return set_error(SKYR_EINVAL, "bad AP max distance");
+    CloudConsts C;
+    MaterialConsts M;
+    if (int st = derive_cloud_consts(*atmosphere, *cloud, *material, *textures, *view, *sizes, C, M)) return st;
+    AtmoConsts A;
+    derive_atmo_consts(*atmosphere, A);
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    dim3 grid((view->width + 15) / 16, (view->height + 7) / 8);
+    const float4* T = reinterpret_cast<const float4*>(transmittance);
+    if (sizes->format == SKYR_FORMAT_RGBA16F) {
+        cloud_render_kernel<__half2, COUNT><<<grid, 128, 0, ctx->stream>>>(
+            C, M, A, T, sizes->transmittance_width, sizes->transmittance_height,
+            reinterpret_cast<const __half2*>(aerial_perspective_luminance),
+            reinterpret_cast<const __half2*>(aerial_perspective_transmittance), blue_noise, depth,
+            reinterpret_cast<__half2*>(out_rgba), out_distance, counters);
+    } else {
+        cloud_render_kernel<float4, COUNT><<<grid, 128, 0, ctx->stream>>>(
+            C, M, A, T, sizes->transmittance_width, sizes->transmittance_height,
+            reinterpret_cast<const float4*>(aerial_perspective_luminance),
+            reinterpret_cast<const float4*>(aerial_perspective_transmittance), blue_noise, depth,
+            reinterpret_cast<__half2*>(out_rgba), out_distance, counters);
+    }
+    return check_cuda(cudaGetLastError(), "cloud raymarch kernel");
+}
+}  // namespace
+
+extern "C" {
+
+int skyr_cloud_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                      const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                      const skyr_cloud_textures* textures, const skyr_cloud_view* view,
+                      const skyr_lut_sizes* sizes, const void* transmittance,
+                      const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
+                      const float* blue_noise, const float* depth, void* out_rgba, float* out_distance) {
+    return cloud_render_impl<false>(ctx, atmosphere, cloud, material, textures, view, sizes, transmittance,
+                                    aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise,
+                                    depth, out_rgba, out_distance, nullptr);
+}
+
+int skyr_cloud_render_counted(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                              const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                              const skyr_cloud_textures* textures, const skyr_cloud_view* view,
+                              const skyr_lut_sizes* sizes, const void* transmittance,
+                              const void* aerial_perspective_luminance,
+                              const void* aerial_perspective_transmittance, const float* blue_noise,
+                              const float* depth, void* out_rgba, float* out_distance,
+                              unsigned long long* counters) {
+    if (!counters) return set_error(SKYR_EINVAL, "null counters");
+    return cloud_render_impl<true>(ctx, atmosphere, cloud, material, textures, view, sizes, transmittance,
+                                   aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise,
+                                   depth, out_rgba, out_distance, counters);
+}
+
+
+
+int skyr_cloud_parameters_default(skyr_cloud_parameters* c) {
+    if (!c) return set_error(SKYR_EINVAL, "null parameters");
+    // VolumetricCloud defaults (src/SkyRendering/VolumetricCloud.h:20-35)
+    *c = skyr_cloud_parameters{};
+    c->bottom_altitude = 2.f;
+    c->thickness = 2.f;
+    c->max_raymarch_distance = 30.f;
+    c->max_raymarch_steps = 128.f;
+    c->max_visible_distance = 120.f;
+    c->env_color[0] = c->env_color[1] = c->env_color[2] = 1.f;
+    c->env_color_scale = 0.1f;
+    c->sun_illuminance_scale = 1.f;
+    c->shadow_steps = 5.f;
+    c->shadow_distance = 2.f;
+    c->shadow_froxel_max_distance = 20.f;
+    c->sun_multiscattering_sigma_scale = 0.3f;
+    c->env_multiscattering_sigma_scale = 0.5f;
+    c->env_bottom_visibility = 0.4f;
+    c->env_sun_height_curve_exp = 1.f;
+    c->phase_g_forward = 0.85f;
+    c->phase_g_back = -0.15f;
+    c->phase_back_scale = 2.16f;
+    return SKYR_OK;
+}
+
+int skyr_cloud_material_default(int type, skyr_cloud_material* m) {
+    if (!m) return set_error(SKYR_EINVAL, "null material");
+    if (type < SKYR_MATERIAL_DEFAULT0 || type > SKYR_MATERIAL_VOXEL)
+        return set_error(SKYR_EINVAL, "unknown material type %d", type);
+    *m = skyr_cloud_material{};
+    m->type = type;
+    // VolumetricCloudDefaultMaterialCommon (VolumetricCloudDefaultMaterial.h:126-133, .cpp:37-64)
+    m->lod_bias = 2.75f;
+    m->density = 15.f;
+    m->cloud_map_repeat_size = 18.99f;
+    m->detail_repeat_size = 5.33f;
+    m->displacement_repeat_size = 3.51f;
+    m->minfilter2d = m->minfilter3d = m->minfilter_displacement = SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST;
+    // VolumetricCloudDefaultMaterial1 (VolumetricCloudDefaultMaterial.h:199-205)
+    m->detail_base = 0.67f;
+    m->detail_scale = 1.86f;
+    m->base_density_threshold = 0.4f;
+    m->base_height_hardness = 6.f;
+    m->base_edge_hardness = 6.f;
+    m->height_cut = 0.9f;
+    m->edge_cut = 0.8f;
+    // VolumetricCloudDefaultMaterial0 (VolumetricCloudDefaultMaterial.h:165-166)
+    m->detail_param[0] = 0.4f;
+    m->detail_param[1] = 0.f;
+    m->displacement_scale = 1.f;
+    // VolumetricCloudVoxelMaterial (VolumetricCloudVoxelMaterial.h:32-35)
+    m->voxel_width[0] = m->voxel_width[1] = 2.f;
+    if (type == SKYR_MATERIAL_VOXEL) m->density = 20.f;
+    if (type == SKYR_MATERIAL_MINIMAL) m->density = 0.5f;  // VolumetricCloudMinimalMaterial.h:26
+    return SKYR_OK;
+}
+
+}  // extern "C"

@@ -1,4 +1,5 @@
 // skyr_modules.cu — lifetime of the per-context scratch buffers.
+#include "../../include/skyr_cloud.h"
 #include "skyr_ctx.cuh"
 
 namespace skyr {
@@ -15,6 +16,12 @@ void ctx_release_resources(skyr_ctx* ctx) {
 }  // namespace skyr
 
 size_t skyr_struct_size_ext(int which) {
-    (void)which;
-    return 0;
+    switch (which) {
+        case 3: return sizeof(skyr_noise_texture_desc);
+        case 4: return sizeof(skyr_cloud_material);
+        case 5: return sizeof(skyr_cloud_textures);
+        case 6: return sizeof(skyr_cloud_parameters);
+        case 7: return sizeof(skyr_cloud_view);
+        default: return 0;
+    }
 }

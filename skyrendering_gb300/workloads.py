@@ -168,3 +168,95 @@ def batched_lut_sets(n: int = 256, seed: int = SEED):
                      pitch=float(rng.uniform(-5.0, 30.0)))
         renders[i] = render_parameters(cam, float(rng.uniform(0.0, 95.0)), float(rng.uniform(0.0, 360.0)))
     return params, renders
+
+
+# ---------------------------------------------------------------------------
+# Cloud frame workload (1920x1080, layer 1.5-4.0 km)
+# ---------------------------------------------------------------------------
+def noise_info(seed, freq, rmin, rmax):
+    ci = _abi.NoiseCreateInfo()
+    ci.seed, ci.base_frequency, ci.remap_min, ci.remap_max = seed, freq, rmin, rmax
+    return ci
+
+
+def noise_desc(w, h, d, channels, octaves=3):
+    desc = _abi.NoiseTextureDesc()
+    desc.width, desc.height, desc.depth, desc.octaves = w, h, d, octaves
+    desc.channels = len(channels)
+    for i, (kind, a, b) in enumerate(channels):
+        desc.channel[i].kind = kind
+        desc.channel[i].a = a
+        if b is not None:
+            desc.channel[i].b = b
+    return desc
+
+
+def cloud_map_desc(size=512, octaves=3):
+    """Weather / cloud map (CLOUD_MAP_GEN, NoiseGen.comp:77-92): R = Perlin fBm
+    coverage-density, G = Worley fBm cloud type; CloudMapBuffer defaults
+    (VolumetricCloudDefaultMaterial.h:66-71)."""
+    return noise_desc(size, size, 1, [(_abi.SKYR_NOISE_PERLIN, noise_info(0, 3, 0.35, 0.75), None),
+                                      (_abi.SKYR_NOISE_WORLEY, noise_info(0, 5, 0.8, 0.4), None)], octaves)
+
+
+def base_noise_desc(size=128, octaves=3):
+    """128^3 RGBA8 base noise: R = Perlin-Worley (DETAIL_MAP_GEN, NoiseGen.comp:95-104,
+    DetailBuffer defaults VolumetricCloudDefaultMaterial.h:73-78), G/B/A = Worley
+    fBm at base frequencies 8, 16, 32.  The reference materials read channel R."""
+    return noise_desc(size, size, size, [
+        (_abi.SKYR_NOISE_PERLIN_WORLEY, noise_info(0, 7, 0.23, 1.0), noise_info(0, 11, 1.0, 0.0)),
+        (_abi.SKYR_NOISE_WORLEY, noise_info(1, 8, 1.0, 0.0), None),
+        (_abi.SKYR_NOISE_WORLEY, noise_info(2, 16, 1.0, 0.0), None),
+        (_abi.SKYR_NOISE_WORLEY, noise_info(3, 32, 1.0, 0.0), None)], octaves)
+
+
+def detail_noise_desc(size=32, octaves=3):
+    """32^3 RGBA8 Worley detail noise (base frequencies 2, 4, 8, 16).  Generated
+    for the frame's texture set; the reference's material formulas do not
+    sample a second 3D texture."""
+    return noise_desc(size, size, size, [(_abi.SKYR_NOISE_WORLEY, noise_info(4 + i, 2 << i, 1.0, 0.0), None)
+                                         for i in range(4)], octaves)
+
+
+def displacement_desc(size=128, octaves=3):
+    """DISPLACEMENT_GEN (NoiseGen.comp:57-74): 4 Perlin fBm channels, seeds s..s+3
+    (DisplacementBuffer defaults, VolumetricCloudDefaultMaterial.h:80-84)."""
+    return noise_desc(size, size, 1, [(_abi.SKYR_NOISE_PERLIN, noise_info(i, 6, 0.25, 0.75), None)
+                                      for i in range(4)], octaves)
+
+
+def frame_cloud_parameters() -> _abi.CloudParameters:
+    """Cloud layer 1.5-4.0 km, 64 primary steps, 6 light-march steps,
+    dual-lobe HG g = 0.8 / -0.3; the other fields are the reference defaults
+    (src/SkyRendering/VolumetricCloud.h:20-35)."""
+    c = _abi.CloudParameters()
+    _abi.call("skyr_cloud_parameters_default", C_ref(c))
+    c.bottom_altitude, c.thickness = 1.5, 2.5
+    c.max_raymarch_steps = 64.0
+    c.shadow_steps = 6.0
+    c.phase_g_forward, c.phase_g_back = 0.8, -0.3
+    return c
+
+
+def frame_material(kind: int = None) -> _abi.CloudMaterial:
+    """VolumetricCloudDefaultMaterial1 defaults with density 50/km (0.05/m)."""
+    kind = _abi.SKYR_MATERIAL_DEFAULT1 if kind is None else kind
+    m = _abi.CloudMaterial()
+    _abi.call("skyr_cloud_material_default", kind, C_ref(m))
+    if kind in (_abi.SKYR_MATERIAL_DEFAULT0, _abi.SKYR_MATERIAL_DEFAULT1):
+        m.density = 50.0
+    return m
+
+
+def frame_view(cam: Camera, sun_zenith_deg: float, sun_azimuth_deg: float = 60.0,
+               ap_max_distance: float = 32.0, width=None, height=None) -> _abi.CloudView:
+    v = _abi.CloudView()
+    v.camera_position[:] = list(cam.position)
+    v.view_projection[:] = column_major(cam.view_projection())
+    v.fovy = cam.fovy
+    v.viewport_width, v.viewport_height = cam.width, cam.height
+    v.width, v.height = width or cam.width, height or cam.height
+    v.sun_direction_theta, v.sun_direction_phi = sun_zenith_deg, sun_azimuth_deg
+    v.frame_id = 0.0
+    v.aerial_perspective_lut_max_distance = ap_max_distance
+    return v

@@ -1,0 +1,184 @@
+"""GPU parity of the noise generators and the cloud raymarch against the FP64
+CPU oracle, through the C ABI.
+
+Tolerances:
+* noise bytes: GPU (FP32 noise) vs oracle (FP64 noise) differ by at most one
+  UNORM8 step, on at most 1e-3 of the texels (values that sit on a rounding
+  boundary); the mip chain built from identical level-0 bytes is bit-exact.
+* raymarched frame: <= 1e-3 mean relative error, sum|gpu - oracle| / sum|oracle|
+  over the frame, per output (luminance rgb, transmittance a, mean distance),
+  with the same textures, LUTs and blue-noise offsets fed to both.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as orc
+from skyrendering_gb300 import _abi
+from skyrendering_gb300 import workloads as W
+from skyrendering_gb300.atmosphere import update_lut_set
+from skyrendering_gb300.cloud import (NoiseTexture, VolumetricCloud, blue_noise_tile, prepare_textures,
+                                      textures_struct)
+
+pytestmark = pytest.mark.gpu
+MEAN_TOL = 1e-3
+
+
+def mean_rel(got, want):
+    return float(np.abs(got - want).sum() / max(np.abs(want).sum(), 1e-300))
+
+
+@pytest.mark.parametrize("desc_fn,size", [(W.cloud_map_desc, 512), (W.base_noise_desc, 64),
+                                          (W.displacement_desc, 128), (W.detail_noise_desc, 32)])
+def test_noise_matches_oracle(ctx, desc_fn, size):
+    desc = desc_fn(size)
+    tex = NoiseTexture(desc).generate(ctx)
+    ctx.synchronize()
+    got = tex.data.cpu().numpy()
+    want = orc.noise_generate(desc)
+    n0 = tex.level_offset(1)
+    diff = np.abs(got[:n0].astype(int) - want[:n0].astype(int))
+    frac = float((diff > 0).mean())
+    print(f"{desc_fn.__name__}: max |d| = {diff.max()}, mismatch fraction = {frac:.2e}")
+    assert diff.max() <= 1 and frac <= 1e-3
+    # mips from the GPU's own level 0 are bit-exact
+    np.testing.assert_array_equal(got, orc.noise_mips(desc, got))
+
+
+class Frame:
+    """One frame's inputs on the device and on the host."""
+
+    def __init__(self, ctx, cam, zenith, material_kind=_abi.SKYR_MATERIAL_DEFAULT1, cloud=None, fmt=0,
+                 size=None, expand=True):
+        self.atmo = W.earth_like_atmosphere()
+        self.sizes = W.plain_lut_sizes(fmt)
+        self.render = W.render_parameters(cam, zenith)
+        self.luts = update_lut_set(ctx, self.atmo, self.render, self.sizes)
+        self.cloud = cloud or W.frame_cloud_parameters()
+        self.material = W.frame_material(material_kind)
+        self.tex = {}
+        self.tex["cloud_map"] = NoiseTexture(W.cloud_map_desc()).generate(ctx)
+        self.tex["detail"] = NoiseTexture(W.base_noise_desc()).generate(ctx)
+        self.tex["displacement"] = NoiseTexture(W.displacement_desc()).generate(ctx)
+        if expand:
+            prepare_textures(ctx, material_kind, self.tex)
+        self.bn = blue_noise_tile().cuda()
+        self.view = W.frame_view(cam, zenith, width=size[0] if size else None, height=size[1] if size else None)
+        self.vc = VolumetricCloud(ctx, self.cloud, self.material, textures_struct(**self.tex))
+        self.rgba, self.dist = self.vc.render(self.atmo, self.view, self.sizes, self.luts, self.bn)
+        ctx.synchronize()
+
+    def oracle(self, pixels=None):
+        host = {k: (t.desc, t.data.cpu().numpy()) for k, t in self.tex.items()}
+        L = self.luts
+        return orc.cloud_render(self.atmo, self.cloud, self.material, host, self.view, self.sizes,
+                                L.transmittance[0].cpu().double().numpy(),
+                                L.aerial_perspective_luminance[0].float().cpu().double().numpy(),
+                                L.aerial_perspective_transmittance[0].float().cpu().double().numpy(),
+                                self.bn.cpu().numpy(), pixels=pixels)
+
+    def compare(self, pixels=None):
+        rgba, dist = self.oracle(pixels)
+        g = self.rgba.float().cpu().numpy().reshape(-1, 4).astype(np.float64)
+        gd = self.dist.cpu().numpy().reshape(-1).astype(np.float64)
+        if pixels is not None:
+            g, gd = g[pixels], gd[pixels]
+        return {"luminance": mean_rel(g[:, :3], rgba[:, :3]), "transmittance": mean_rel(g[:, 3], rgba[:, 3]),
+                "distance": mean_rel(gd, dist)}
+
+
+@pytest.mark.parametrize("zenith", [45.0, 85.0, 95.0])
+def test_frame_1080p_matches_oracle(ctx, zenith):
+    f = Frame(ctx, W.frame_camera(), zenith)
+    err = f.compare()
+    print(f"zenith {zenith}: " + ", ".join(f"{k}={v:.2e}" for k, v in err.items()))
+    assert all(v <= MEAN_TOL for v in err.values()), err
+    rgba = f.rgba.float().cpu().numpy()
+    assert np.isfinite(rgba).all() and (rgba[..., 3] >= 0).all() and (rgba[..., 3] <= 1).all()
+    assert (rgba[..., 3] < 0.999).mean() > 0.05, "the frame should contain cloud"
+
+
+@pytest.mark.parametrize("alt,pitch", [(2.5, 0.0), (6.0, -20.0), (0.2, 45.0)])
+def test_camera_inside_above_below_layer(ctx, alt, pitch):
+    cam = W.Camera(position=(0.0, alt, 0.0), pitch=pitch, width=480, height=270)
+    f = Frame(ctx, cam, 60.0)
+    err = f.compare()
+    print(f"alt {alt}: " + ", ".join(f"{k}={v:.2e}" for k, v in err.items()))
+    assert all(v <= MEAN_TOL for v in err.values()), err
+
+
+@pytest.mark.parametrize("kind", [_abi.SKYR_MATERIAL_DEFAULT0, _abi.SKYR_MATERIAL_MINIMAL])
+def test_other_materials(ctx, kind):
+    cam = W.Camera(width=480, height=270)
+    f = Frame(ctx, cam, 45.0, material_kind=kind)
+    err = f.compare()
+    print(f"material {kind}: " + ", ".join(f"{k}={v:.2e}" for k, v in err.items()))
+    assert all(v <= MEAN_TOL for v in err.values()), err
+
+
+def test_fp16_luts_and_depth_buffer(ctx):
+    cam = W.Camera(width=480, height=270)
+    f = Frame(ctx, cam, 30.0, fmt=_abi.SKYR_FORMAT_RGBA16F)
+    # a synthetic depth buffer: geometry in the lower third of the view
+    depth = torch.ones((270, 480), dtype=torch.float32)
+    depth[:90] = 0.9995
+    d = depth.cuda()
+    rgba, dist = f.vc.render(f.atmo, f.view, f.sizes, f.luts, f.bn, depth=d)
+    ctx.synchronize()
+    host = {k: (t.desc, t.data.cpu().numpy()) for k, t in f.tex.items()}
+    L = f.luts
+    o_rgba, o_dist = orc.cloud_render(f.atmo, f.cloud, f.material, host, f.view, f.sizes,
+                                      L.transmittance[0].cpu().double().numpy(),
+                                      L.aerial_perspective_luminance[0].float().cpu().double().numpy(),
+                                      L.aerial_perspective_transmittance[0].float().cpu().double().numpy(),
+                                      f.bn.cpu().numpy(), depth=depth.numpy())
+    g = rgba.float().cpu().numpy().reshape(-1, 4)
+    assert mean_rel(g[:, :3], o_rgba[:, :3]) <= MEAN_TOL
+    assert mean_rel(g[:, 3], o_rgba[:, 3]) <= MEAN_TOL
+
+
+def test_expanded_layout_bytes(ctx):
+    for desc in (W.cloud_map_desc(64), W.base_noise_desc(16)):
+        t = NoiseTexture(desc).generate(ctx).expand(ctx, 1)
+        ctx.synchronize()
+        lvl = t.level(0)[0].cpu().numpy().astype(np.uint64)  # (d, h, w)
+        ex = t.expanded.cpu().numpy()
+        if desc.depth == 1:
+            q = ex.view(np.uint32).reshape(lvl.shape[1:]).astype(np.uint64)
+            l0 = lvl[0]
+            want = (l0 | (np.roll(l0, -1, 1) << 8) | (np.roll(l0, -1, 0) << 16) |
+                    (np.roll(np.roll(l0, -1, 0), -1, 1) << 24))
+        else:
+            q = ex.view(np.uint64).reshape(lvl.shape)
+            want = np.zeros_like(lvl)
+            for k in range(8):
+                c = np.roll(lvl, (-(k >> 2), -((k >> 1) & 1), -(k & 1)), axis=(0, 1, 2))
+                want |= c << np.uint64(8 * k)
+        np.testing.assert_array_equal(q, want)
+
+
+def test_expanded_layout_renders_like_plain_layout(ctx):
+    cam = W.Camera(width=480, height=270)
+    a = Frame(ctx, cam, 45.0, expand=True)
+    b = Frame(ctx, cam, 45.0, expand=False)
+    ga, gb = a.rgba.float().cpu().numpy(), b.rgba.float().cpu().numpy()
+    assert mean_rel(ga, gb) <= 1e-5
+
+
+def test_cloud_invalid_arguments(ctx):
+    import ctypes as C
+
+    f_cam = W.Camera(width=64, height=36)
+    atmo, s = W.earth_like_atmosphere(), W.plain_lut_sizes()
+    cp, m = W.frame_cloud_parameters(), W.frame_material()
+    v = W.frame_view(f_cam, 45.0)
+    lib = _abi.lib()
+    t = _abi.CloudTextures()  # missing textures for Material1
+    rc = lib.skyr_cloud_render(ctx.handle, C.byref(atmo), C.byref(cp), C.byref(m), C.byref(t), C.byref(v),
+                               C.byref(s), C.c_void_p(1), C.c_void_p(1), C.c_void_p(1), C.c_void_p(1), None, None,
+                               None)
+    assert rc == _abi.SKYR_EINVAL and b"texture" in lib.skyr_last_error()
+    bad = W.cloud_map_desc(500)
+    assert lib.skyr_noise_texture_levels(C.byref(bad)) == 0
+    rc = lib.skyr_noise_generate(ctx.handle, C.byref(bad), C.c_void_p(1))
+    assert rc == _abi.SKYR_EINVAL
