@@ -169,6 +169,27 @@ int skyr_update_lut_set(skyr_ctx* ctx, const skyr_atmosphere_parameters* params,
                         void* sky_view_luminance, void* sky_view_transmittance,
                         void* aerial_perspective_luminance, void* aerial_perspective_transmittance);
 
+/* Allocation-free form of skyr_update_lut_set, for callers that cannot let the
+ * library allocate device memory: hosts that own every device allocation
+ * through their own pool or budget, or frame loops that must not take
+ * cudaMalloc / cudaFree (cudaFree synchronises the device).  Same arguments,
+ * outputs and results as skyr_update_lut_set; the caller still allocates the
+ * outputs.  The per-set kernel constants go to a static device table of this
+ * library (SKYR_NOALLOC_MAX_SETS sets, under 100 KB, held by every GPU that
+ * loads the library until exit) instead of a cudaMalloc'ed one:
+ *   - n_sets above SKYR_NOALLOC_MAX_SETS is rejected with SKYR_EINVAL;
+ *   - the first call on a device looks up the table's device address
+ *     (cudaGetSymbolAddress) and should come before any stream capture;
+ *   - every call shares the one table, so calls whose GPU work overlaps
+ *     (two streams or contexts at once) race.
+ * No counterpart in the reference. */
+#define SKYR_NOALLOC_MAX_SETS 256
+int skyr_update_lut_set_noalloc(skyr_ctx* ctx, const skyr_atmosphere_parameters* params,
+                                const skyr_atmosphere_render_parameters* render, int n_sets,
+                                const skyr_lut_sizes* sizes, void* transmittance, void* multiscattering,
+                                void* sky_view_luminance, void* sky_view_transmittance,
+                                void* aerial_perspective_luminance, void* aerial_perspective_transmittance);
+
 #ifdef __cplusplus
 }
 #endif

@@ -256,3 +256,9 @@ _SIGNATURES.update({
 _SIGNATURES["skyr_cloud_render_counted"] = (
     C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters), C.POINTER(CloudMaterial),
               C.POINTER(CloudTextures), C.POINTER(CloudView), C.POINTER(LutSizes), P, P, P, P, P, P, P, P])
+
+# allocation-free LUT set (static device scratch, SKYR_NOALLOC_MAX_SETS sets)
+SKYR_NOALLOC_MAX_SETS = 256
+_SIGNATURES["skyr_update_lut_set_noalloc"] = (
+    C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(AtmosphereRenderParameters), C.c_int,
+              C.POINTER(LutSizes), P, P, P, P, P, P])
