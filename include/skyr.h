@@ -53,7 +53,8 @@ const char* skyr_last_error(void);
 /* sizeof() of the public structs, for binding layout checks:
  * 0 skyr_atmosphere_parameters, 1 skyr_atmosphere_render_parameters,
  * 2 skyr_lut_sizes, 3 skyr_noise_texture_desc, 4 skyr_cloud_material,
- * 5 skyr_cloud_textures, 6 skyr_cloud_parameters, 7 skyr_cloud_view;
+ * 5 skyr_cloud_textures, 6 skyr_cloud_parameters, 7 skyr_cloud_view,
+ * 8 skyr_density_grid, 9 skyr_grid_generator, 10 skyr_pathtrace_parameters;
  * further ids are listed beside later structs.
  * Returns 0 for an unknown id.  (No reference counterpart: ABI hygiene.) */
 size_t skyr_struct_size(int which);
@@ -66,6 +67,11 @@ int skyr_ctx_create(void* cuda_stream, skyr_ctx** out_ctx);
 int skyr_ctx_destroy(skyr_ctx* ctx);
 /* Block the host until all work queued on the context's stream is done. */
 int skyr_ctx_synchronize(skyr_ctx* ctx);
+/* Synchronise and report the context's device status word: SKYR_ETIMEOUT
+ * when a device loop stopped at its iteration bound since the last check
+ * (the word is then cleared), else SKYR_OK.  (No reference counterpart: the
+ * reference has no device-side error reporting.) */
+int skyr_ctx_check_status(skyr_ctx* ctx);
 
 /* ======================================================================== */
 /* Atmosphere                                                                */

@@ -220,3 +220,79 @@ def cloud_render(atmo, cloud, material, textures_host: dict, view, sizes, transm
                                    nthreads or threads(), _dp(rgba), _dp(dist))
     assert rc == 0
     return rgba, dist
+
+
+# ---------------------------------------------------------------------------
+# path tracer
+# ---------------------------------------------------------------------------
+U16 = C.POINTER(C.c_uint16)
+FP = C.POINTER(C.c_float)
+
+
+def _declare_pt(lb):
+    lb.oracle_grid_generate.restype = C.c_int
+    lb.oracle_grid_generate.argtypes = [P, C.c_int, C.c_int, D]
+    lb.oracle_grid_majorants.restype = C.c_int
+    lb.oracle_grid_majorants.argtypes = [P, U16, FP]
+    lb.oracle_pathtrace.restype = C.c_int
+    lb.oracle_pathtrace.argtypes = [P, P, P, P, P, P, P, P, P, D, D, D, D, D, C.c_uint, C.c_int, I32, C.c_int,
+                                    C.c_int, C.c_int, D, D]
+
+
+_EXT.append(_declare_pt)
+
+
+def grid_generate(gen, precision: int = 64, nthreads: int | None = None) -> np.ndarray:
+    out = np.zeros((gen.nz, gen.ny, gen.nx))
+    assert lib().oracle_grid_generate(_ref(gen), precision, nthreads or threads(), _dp(out)) == 0
+    return out
+
+
+def grid_majorants(grid_struct, data_half: np.ndarray) -> np.ndarray:
+    d = np.ascontiguousarray(data_half).view(np.uint16)
+    b = grid_struct.brick
+    shape = tuple((n + b - 1) // b for n in (grid_struct.nz, grid_struct.ny, grid_struct.nx))
+    out = np.zeros(shape, dtype=np.float32)
+    assert lib().oracle_grid_majorants(_ref(grid_struct), d.ctypes.data_as(U16), out.ctypes.data_as(FP)) == 0
+    return out
+
+
+def pathtrace(atmo, cloud, material, textures_host: dict | None, grid_struct, grid_half: np.ndarray | None,
+              majorant: np.ndarray | None, pt, view, env_view, sizes, luts: dict, frame_begin: int, n_frames: int,
+              pixels, precision: int = 64, nthreads: int | None = None):
+    """Per-pixel (sum, sum of squares) of n_frames path-traced frames."""
+    import skyrendering_gb300._abi as A
+
+    keep = []
+    t = A.CloudTextures()
+    for name, (desc, arr) in (textures_host or {}).items():
+        arr = np.ascontiguousarray(arr, dtype=np.uint8)
+        keep.append(arr)
+        setattr(t, name, arr.ctypes.data)
+        setattr(t, name + "_desc", desc)
+    g = None
+    if grid_struct is not None:
+        g = A.DensityGrid()
+        C.memmove(C.byref(g), C.byref(grid_struct), C.sizeof(g))
+        gh = np.ascontiguousarray(grid_half).view(np.uint16)
+        keep.append(gh)
+        g.data = gh.ctypes.data
+        if majorant is not None:
+            mj = np.ascontiguousarray(majorant, dtype=np.float32)
+            keep.append(mj)
+            g.majorant = mj.ctypes.data
+        else:
+            g.majorant = None
+    px = np.ascontiguousarray(pixels, dtype=np.int32)
+    n = len(px)
+    s, sq = np.zeros((n, 4)), np.zeros((n, 4))
+    arrs = [np.ascontiguousarray(luts[k], dtype=np.float64) for k in
+            ("transmittance", "sky_view_luminance", "sky_view_transmittance", "aerial_perspective_luminance",
+             "aerial_perspective_transmittance")]
+    mat = material if material is not None else None
+    rc = lib().oracle_pathtrace(_ref(atmo), _ref(cloud), _ref(mat) if mat is not None else _ref(A.CloudMaterial()),
+                                _ref(t), _ref(g) if g is not None else None, _ref(pt), _ref(view), _ref(env_view),
+                                _ref(sizes), *[_dp(a) for a in arrs], frame_begin, n_frames,
+                                px.ctypes.data_as(I32), n, precision, nthreads or threads(), _dp(s), _dp(sq))
+    assert rc == 0
+    return s, sq

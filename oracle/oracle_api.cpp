@@ -9,6 +9,7 @@
 #include "oracle_atmosphere.hpp"
 #include "oracle_cloud.hpp"
 #include "oracle_noise.hpp"
+#include "oracle_pathtrace.hpp"
 
 namespace {
 
@@ -268,6 +269,151 @@ int oracle_cloud_render(const skyr_atmosphere_parameters* atmo, const skyr_cloud
                                      threads, out_rgba, out_dist);
     return cloud_render_t<double>(atmo, cp, m, tx, v, s, tlut, apl, apt, blue_noise, depth, pixels, n_pixels,
                                   threads, out_rgba, out_dist);
+}
+
+}  // extern "C"
+
+// ---- path tracer -----------------------------------------------------------
+
+extern "C" {
+
+// Grid values (FP64 or FP32) of the synthetic generator, x fastest.
+int oracle_grid_generate(const skyr_grid_generator* g, int precision, int threads, double* out) {
+    parallel_for(g->ny * g->nz, threads, [&](int row) {
+        int y = row % g->ny, z = row / g->ny;
+        for (int x = 0; x < g->nx; ++x)
+            out[((size_t)z * g->ny + y) * g->nx + x] = precision == 32 ? (double)orc::grid_value<float>(*g, x, y, z)
+                                                                        : orc::grid_value<double>(*g, x, y, z);
+    });
+    return 0;
+}
+
+// Brick majorants of a host half grid (same definition as skyr_grid_majorants).
+int oracle_grid_majorants(const skyr_density_grid* gd, const uint16_t* data, float* out) {
+    int bs = gd->brick;
+    int bx = (gd->nx + bs - 1) / bs, by = (gd->ny + bs - 1) / bs, bz = (gd->nz + bs - 1) / bs;
+    for (int k = 0; k < bz; ++k)
+        for (int j = 0; j < by; ++j)
+            for (int i = 0; i < bx; ++i) {
+                float m = 0.f;
+                for (int z = k * bs - 1; z <= (k + 1) * bs; ++z)
+                    for (int y = j * bs - 1; y <= (j + 1) * bs; ++y)
+                        for (int x = i * bs - 1; x <= (i + 1) * bs; ++x) {
+                            if (x < 0 || y < 0 || z < 0 || x >= gd->nx || y >= gd->ny || z >= gd->nz) continue;
+                            m = std::max(m, orc::half_to_float(data[((size_t)z * gd->ny + y) * gd->nx + x]));
+                        }
+                out[((size_t)k * by + j) * bx + i] = m * gd->density;
+            }
+    return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+template <class T>
+int pathtrace_t(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                const skyr_cloud_material* m, const skyr_cloud_textures* tx, const skyr_density_grid* gd,
+                const skyr_pathtrace_parameters* pt, const skyr_cloud_view* v,
+                const skyr_atmosphere_render_parameters* ev, const skyr_lut_sizes* s, const double* tlut_in,
+                const double* svl_in, const double* svt_in, const double* apl_in, const double* apt_in,
+                unsigned frame_begin, int n_frames, const int* pixels, int n_pixels, int threads, double* sum,
+                double* sumsq) {
+    orc::AtmosphereOracle<T> O{orc::derive_atmosphere<T>(*atmo)};
+    orc::Image<T> tl = image_from<T>(tlut_in, s->transmittance_width, s->transmittance_height);
+    orc::Image<T> sl = image_from<T>(svl_in, s->sky_view_width, s->sky_view_height);
+    orc::Image<T> st = image_from<T>(svt_in, s->sky_view_width, s->sky_view_height);
+    int W = s->aerial_perspective_width, H = s->aerial_perspective_height, D = s->aerial_perspective_depth;
+    orc::Image<T> al = image_from<T>(apl_in, W, H, D), at = image_from<T>(apt_in, W, H, D);
+    orc::CloudOracle<T> C{O, orc::derive_cloud_frame<T>(*atmo, *cp, *m, *tx, *v), {}, {}, {}, {}, nullptr,
+                          nullptr, nullptr, nullptr};
+    auto set = [](orc::Tex8& t, const void* p, const skyr_noise_texture_desc& d, bool border) {
+        t.data = (const uint8_t*)p;
+        t.w = d.width; t.h = d.height; t.d = d.depth; t.channels = d.channels;
+        t.border = border;
+        t.init();
+    };
+    if (tx->cloud_map) set(C.cloud_map, tx->cloud_map, tx->cloud_map_desc, false);
+    if (tx->detail) set(C.detail, tx->detail, tx->detail_desc, false);
+    if (tx->displacement) set(C.displacement, tx->displacement, tx->displacement_desc, false);
+    if (tx->voxel) set(C.voxel, tx->voxel, tx->voxel_desc, true);
+    C.tlut = &tl;
+    C.ap_lum = &al;
+    C.ap_trans = &at;
+    orc::ViewLutOracle<T> V{O, orc::derive_render_frame<T>(*atmo, *ev)};
+    orc::PathTracerOracle<T> PT{O, C, V, &sl, &st, *pt};
+    // box: the flat AABB [-w, w]^2 x [bottom, top], clipped to the grid
+    T hw = T(pt->region_box_half_width);
+    PT.box_min = orc::V3<T>(-hw, -hw, C.F.bottom);
+    PT.box_max = orc::V3<T>(hw, hw, C.F.top);
+    if (gd && gd->data) {
+        PT.grid = (const uint16_t*)gd->data;
+        PT.nx = gd->nx; PT.ny = gd->ny; PT.nz = gd->nz;
+        PT.origin = orc::V3<T>(T(gd->origin[0]), T(gd->origin[1]), T(gd->origin[2]));
+        PT.voxel = T(gd->voxel_size);
+        PT.density = T(gd->density);
+        PT.maj = gd->majorant;
+        PT.brick = gd->brick;
+        PT.bx = (gd->nx + gd->brick - 1) / gd->brick;
+        PT.by = (gd->ny + gd->brick - 1) / gd->brick;
+        PT.bz = (gd->nz + gd->brick - 1) / gd->brick;
+        orc::V3<T> gmax = PT.origin + orc::V3<T>(T(gd->nx), T(gd->ny), T(gd->nz)) * PT.voxel;
+        for (int a = 0; a < 3; ++a) {
+            PT.box_min[a] = std::max(PT.box_min[a], PT.origin[a]);
+            PT.box_max[a] = std::min(PT.box_max[a], gmax[a]);
+        }
+    }
+    // kModelMatrix3: columns front, right, up of VolumetricCloud::Update (VolumetricCloud.cpp:188-200)
+    {
+        T R = T(atmo->bottom_radius);
+        orc::V3<T> center(T(0), -R, T(0));
+        orc::V3<T> up = orc::normalize(orc::v3f<T>(v->camera_position) - center);
+        orc::V3<T> front = orc::normalize(orc::cross(up, orc::V3<T>(T(1), T(0), T(0))));
+        orc::V3<T> right = orc::normalize(orc::cross(up, front));
+        for (int i = 0; i < 16; ++i) PT.model3.m[i] = T(0);
+        for (int r = 0; r < 3; ++r) {
+            PT.model3(r, 0) = front[r];
+            PT.model3(r, 1) = right[r];
+            PT.model3(r, 2) = up[r];
+        }
+        PT.model3(3, 3) = T(1);
+    }
+    parallel_for(n_pixels, threads, [&](int i) {
+        int p = pixels ? pixels[i] : i;
+        int px = p % v->width, py = p / v->width;
+        double a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
+        for (int f = 0; f < n_frames; ++f) {
+            T o[4];
+            PT.Pixel(px, py, v->width, v->height, frame_begin + (unsigned)f, o);
+            for (int k = 0; k < 4; ++k) {
+                a[k] += double(o[k]);
+                b[k] += double(o[k]) * double(o[k]);
+            }
+        }
+        for (int k = 0; k < 4; ++k) {
+            sum[(size_t)i * 4 + k] = a[k];
+            sumsq[(size_t)i * 4 + k] = b[k];
+        }
+    });
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_pathtrace(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                     const skyr_cloud_material* m, const skyr_cloud_textures* tx, const skyr_density_grid* gd,
+                     const skyr_pathtrace_parameters* pt, const skyr_cloud_view* v,
+                     const skyr_atmosphere_render_parameters* ev, const skyr_lut_sizes* s, const double* tlut,
+                     const double* svl, const double* svt, const double* apl, const double* apt,
+                     unsigned frame_begin, int n_frames, const int* pixels, int n_pixels, int precision,
+                     int threads, double* sum, double* sumsq) {
+    if (precision == 32)
+        return pathtrace_t<float>(atmo, cp, m, tx, gd, pt, v, ev, s, tlut, svl, svt, apl, apt, frame_begin, n_frames,
+                                  pixels, n_pixels, threads, sum, sumsq);
+    return pathtrace_t<double>(atmo, cp, m, tx, gd, pt, v, ev, s, tlut, svl, svt, apl, apt, frame_begin, n_frames,
+                               pixels, n_pixels, threads, sum, sumsq);
 }
 
 }  // extern "C"

@@ -92,6 +92,7 @@ _SIGNATURES = {
     "skyr_ctx_create": (C.c_int, [P, C.POINTER(P)]),
     "skyr_ctx_destroy": (C.c_int, [P]),
     "skyr_ctx_synchronize": (C.c_int, [P]),
+    "skyr_ctx_check_status": (C.c_int, [P]),
     "skyr_atmosphere_parameters_default": (C.c_int, [C.POINTER(AtmosphereParameters)]),
     "skyr_lut_bytes": (C.c_size_t, [C.POINTER(LutSizes), C.c_int]),
     "skyr_update_luts": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.c_int, C.POINTER(LutSizes), P, P]),
@@ -262,3 +263,46 @@ SKYR_NOALLOC_MAX_SETS = 256
 _SIGNATURES["skyr_update_lut_set_noalloc"] = (
     C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(AtmosphereRenderParameters), C.c_int,
               C.POINTER(LutSizes), P, P, P, P, P, P])
+
+
+# ---------------------------------------------------------------------------
+# skyr_pathtrace.h
+# ---------------------------------------------------------------------------
+SKYR_PRNG_WANG_HASH, SKYR_PRNG_PCG_HASH = 0, 1
+SKYR_ENV_OFF, SKYR_ENV_CONST_ENVIRONMENT_MAP, SKYR_ENV_GROUND_SINGLE_BOUNCE, SKYR_ENV_GROUND_MULTI_BOUNCE = range(4)
+
+
+class DensityGrid(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("origin", f3),
+                ("voxel_size", C.c_float), ("density", C.c_float), ("majorant", C.c_void_p), ("brick", C.c_int)]
+
+
+class GridGenerator(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("seed", C.c_int), ("base_frequency", C.c_int),
+                ("octaves", C.c_int), ("center", f3), ("radii", f3), ("inner", C.c_float),
+                ("threshold", C.c_float)]
+
+
+class PathtraceParameters(C.Structure):
+    """skyr_pathtrace_parameters (PathTracing::InitParam, src/SkyRendering/VolumetricCloud.h:104-114)."""
+
+    _fields_ = [("max_bounces", C.c_int), ("region_box_half_width", C.c_float), ("importance_sampling", C.c_int),
+                ("forward_phase_g", C.c_float), ("back_phase_g", C.c_float),
+                ("forward_scattering_ratio", C.c_float), ("prng", C.c_int), ("environment_lighting", C.c_int),
+                ("sigma_t_max", C.c_float), ("use_brick_majorants", C.c_int)]
+
+
+STRUCT_IDS.update({8: DensityGrid, 9: GridGenerator, 10: PathtraceParameters})
+_SIGNATURES.update({
+    "skyr_pathtrace_parameters_default": (C.c_int, [C.POINTER(PathtraceParameters)]),
+    "skyr_grid_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_int]),
+    "skyr_grid_generate": (C.c_int, [P, C.POINTER(GridGenerator), P]),
+    "skyr_grid_brick_count": (C.c_int, [C.c_int, C.c_int]),
+    "skyr_grid_majorants": (C.c_int, [P, C.POINTER(DensityGrid), P]),
+    "skyr_pathtrace": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                 C.POINTER(CloudMaterial), C.POINTER(CloudTextures), C.POINTER(DensityGrid),
+                                 C.POINTER(PathtraceParameters), C.POINTER(CloudView),
+                                 C.POINTER(AtmosphereRenderParameters), C.POINTER(LutSizes), P, P, P, P, P,
+                                 C.c_uint, C.c_int, P, P, P]),
+    "skyr_pathtrace_resolve": (C.c_int, [P, P, C.c_int, C.c_int, C.c_uint, P, P]),
+})

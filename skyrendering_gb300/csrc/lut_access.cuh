@@ -64,4 +64,25 @@ __device__ __forceinline__ float3 sun_visibility_lut(const AtmoConsts& A, const 
     return tr * (u * u * (3.f - 2.f * u));
 }
 
+// GL LINEAR + CLAMP_TO_EDGE fetch of a 3D LUT at continuous texel coordinate
+// (x, y, z) = (u*W - 0.5, ...), by the same clamp-first rule.
+template <class S>
+__device__ __forceinline__ float3 trilinear_clamp(const S* lut, int w, int h, int d, float x, float y, float z) {
+    x = fminf(fmaxf(x, 0.f), (float)(w - 1));
+    y = fminf(fmaxf(y, 0.f), (float)(h - 1));
+    z = fminf(fmaxf(z, 0.f), (float)(d - 1));
+    int x0 = min((int)x, w - 2), y0 = min((int)y, h - 2), z0 = min((int)z, d - 2);
+    float a = x - (float)x0, b = y - (float)y0, g = z - (float)z0;
+    float3 r[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        int base = ((z0 + k) * h + y0) * w + x0;
+        float3 t00 = load_lut_rgb(lut, base), t10 = load_lut_rgb(lut, base + 1);
+        float3 t01 = load_lut_rgb(lut, base + w), t11 = load_lut_rgb(lut, base + w + 1);
+        float3 top = t00 + (t10 - t00) * a, bot = t01 + (t11 - t01) * a;
+        r[k] = top + (bot - top) * b;
+    }
+    return r[0] + (r[1] - r[0]) * g;
+}
+
 }  // namespace skyr

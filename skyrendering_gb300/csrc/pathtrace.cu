@@ -1,0 +1,697 @@
+// pathtrace.cu — the volumetric-cloud path tracer
+// (VolumetricCloudPathTracing.comp) for sm_103a, the synthetic dense FP16
+// density grid and its 16^3-brick majorant grid.
+//
+// One thread traces the paths of one pixel for every requested frame.  The
+// path logic follows the reference (delta tracking, ratio-tracking next-event
+// estimation with a copied RNG context, HG importance sampling, the Lambert
+// ground bounce, the environment on escape).  Two GB300-side changes:
+//  * a dense FP16 grid with per-brick majorants walked by a 3D DDA replaces the
+//    single global majorant where the caller supplies them, so empty and thin
+//    regions cost few samples;
+//  * the environment is the sky-view LUT + ground term evaluated per direction
+//    (the math of ENVIRONMENT_LUMINANCE) instead of a pre-baked cube map.
+#include <cmath>
+#include <cstring>
+
+#include "../../include/skyr_pathtrace.h"
+#include "atmosphere_kernels.cuh"
+#include "cloud_internal.cuh"
+#include "cloud_material.cuh"
+#include "lut_access.cuh"
+#include "noise_device.cuh"
+#include "skyr_ctx.cuh"
+
+namespace skyr {
+
+// Upper bound on the samples of one free-flight / ratio-tracking walk.  A valid
+// scene needs ~sigma_max x chord samples (tens to hundreds); the cap only
+// stops pathological inputs, ends the path and raises the status flag.
+constexpr int kMaxTrackingSteps = 1 << 20;
+
+struct PtConsts {
+    float3 box_min, box_max;
+    int max_bounces, importance_sampling, prng, env;
+    float g_fwd, g_back, ratio, sigma_t_max;
+    int use_bricks;
+    // dense grid
+    const unsigned short* grid;
+    int nx, ny, nz;
+    float3 origin;
+    float inv_voxel, density;
+    const float* maj;
+    int bx, by, bz;
+    float brick_size;
+    // local -> world directions (kModelMatrix3 columns)
+    float3 m_front, m_right, m_up;
+    int sv_w, sv_h;
+    int width, height;
+    int x0, y0, x1, y1;
+    int* status;  // bit 0: a tracking walk hit kMaxTrackingSteps
+};
+
+__device__ __forceinline__ void flag_overrun(const PtConsts& P) {
+    if (P.status) atomicOr(P.status, 1);
+}
+
+__device__ __forceinline__ uint32_t pt_prng(const PtConsts& P, uint32_t s) {
+    return P.prng == SKYR_PRNG_WANG_HASH ? wang_hash(s) : pcg_hash(s);
+}
+
+// Random01 (PathTracing.comp:44-48): float(seed) / 2^32
+__device__ __forceinline__ float rand01(const PtConsts& P, uint32_t& seed) {
+    float r = (float)seed * 2.3283064365386963e-10f;
+    seed = pt_prng(P, seed);
+    return r;
+}
+
+__device__ __forceinline__ float grid_voxel(const PtConsts& P, int x, int y, int z) {
+    if ((unsigned)x >= (unsigned)P.nx || (unsigned)y >= (unsigned)P.ny || (unsigned)z >= (unsigned)P.nz) return 0.f;
+    unsigned short h = __ldg(P.grid + ((size_t)z * P.ny + y) * P.nx + x);
+    return __half2float(__ushort_as_half(h));
+}
+
+// trilinear between voxel centres, zero border
+__device__ __forceinline__ float grid_sigma(const PtConsts& P, float3 p) {
+    float gx = (p.x - P.origin.x) * P.inv_voxel - 0.5f;
+    float gy = (p.y - P.origin.y) * P.inv_voxel - 0.5f;
+    float gz = (p.z - P.origin.z) * P.inv_voxel - 0.5f;
+    float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
+    float a = gx - fx, b = gy - fy, c = gz - fz;
+    int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
+    float r[2];
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz) {
+        float t00 = grid_voxel(P, x0, y0, z0 + dz), t10 = grid_voxel(P, x0 + 1, y0, z0 + dz);
+        float t01 = grid_voxel(P, x0, y0 + 1, z0 + dz), t11 = grid_voxel(P, x0 + 1, y0 + 1, z0 + dz);
+        float top = fmaf(a, t10 - t00, t00), bot = fmaf(a, t11 - t01, t01);
+        r[dz] = fmaf(b, bot - top, top);
+    }
+    return fmaf(c, r[1] - r[0], r[0]) * P.density;
+}
+
+// SampleSigmaT(vec3 P) of the path tracer (PathTracing.comp:89-91): flat height01
+__device__ __forceinline__ float pt_sigma(const PtConsts& P, const CloudConsts& C, const MaterialConsts& M,
+                                          float3 p) {
+    if (P.grid) return grid_sigma(P, p);
+    float h01 = clamp01((p.z - C.bottom) * C.inv_layer);
+    float3 dc = p - C.cam;
+    return sigma_t(C, M, p, h01, sqrtf(dot3(dc, dc)));
+}
+
+// CloudRegionIntersect (PathTracing.comp:57-75)
+__device__ __forceinline__ void region(const PtConsts& P, float3 o, float3 d, float& t0, float& t1) {
+    float3 inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    float ax = (P.box_min.x - o.x) * inv.x, bx = (P.box_max.x - o.x) * inv.x;
+    float ay = (P.box_min.y - o.y) * inv.y, by = (P.box_max.y - o.y) * inv.y;
+    float az = (P.box_min.z - o.z) * inv.z, bz = (P.box_max.z - o.z) * inv.z;
+    t0 = fmaxf(0.f, fmaxf(fminf(ax, bx), fmaxf(fminf(ay, by), fminf(az, bz))));
+    t1 = fminf(1e7f, fminf(fmaxf(ax, bx), fminf(fmaxf(ay, by), fmaxf(az, bz))));
+}
+
+// 3D DDA over the majorant bricks
+struct Walk {
+    int i[3], s[3];
+    float tmax[3], tdel[3];
+};
+
+__device__ __forceinline__ void walk_init(const PtConsts& P, Walk& w, float3 o, float3 d, float t) {
+    float bs = P.brick_size;
+    float p[3] = {o.x + d.x * t, o.y + d.y * t, o.z + d.z * t};
+    float og[3] = {P.origin.x, P.origin.y, P.origin.z};
+    float dd[3] = {d.x, d.y, d.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        w.i[a] = (int)floorf((p[a] - og[a]) / bs);
+        if (dd[a] > 0.f) {
+            w.s[a] = 1;
+            w.tmax[a] = t + (og[a] + (float)(w.i[a] + 1) * bs - p[a]) / dd[a];
+            w.tdel[a] = bs / dd[a];
+        } else if (dd[a] < 0.f) {
+            w.s[a] = -1;
+            w.tmax[a] = t + (og[a] + (float)w.i[a] * bs - p[a]) / dd[a];
+            w.tdel[a] = -bs / dd[a];
+        } else {
+            w.s[a] = 0;
+            w.tmax[a] = 1e30f;
+            w.tdel[a] = 1e30f;
+        }
+    }
+}
+__device__ __forceinline__ float walk_exit(const Walk& w) { return fminf(w.tmax[0], fminf(w.tmax[1], w.tmax[2])); }
+__device__ __forceinline__ void walk_step(Walk& w) {
+    int a = w.tmax[0] <= w.tmax[1] ? (w.tmax[0] <= w.tmax[2] ? 0 : 2) : (w.tmax[1] <= w.tmax[2] ? 1 : 2);
+    // constant indices keep the walk in registers
+    if (a == 0) { w.i[0] += w.s[0]; w.tmax[0] += w.tdel[0]; }
+    else if (a == 1) { w.i[1] += w.s[1]; w.tmax[1] += w.tdel[1]; }
+    else { w.i[2] += w.s[2]; w.tmax[2] += w.tdel[2]; }
+}
+__device__ __forceinline__ float walk_majorant(const PtConsts& P, const Walk& w) {
+    if (w.i[0] < 0 || w.i[1] < 0 || w.i[2] < 0 || w.i[0] >= P.bx || w.i[1] >= P.by || w.i[2] >= P.bz) return 0.f;
+    return __ldg(P.maj + ((size_t)w.i[2] * P.by + w.i[1]) * P.bx + w.i[0]);
+}
+
+// free flight in [t, t_max] (delta tracking); true on a collision
+__device__ __forceinline__ bool free_flight(const PtConsts& P, const CloudConsts& C, const MaterialConsts& M,
+                                            uint32_t& seed, float3 o, float3 d, float& t, float t_max) {
+    if (!P.use_bricks) {
+        float smax = P.sigma_t_max;
+        for (int it = 0; it < kMaxTrackingSteps; ++it) {
+            if (smax <= 0.f) return false;
+            t += -logf(1.f - rand01(P, seed)) / smax;
+            if (!(t <= t_max)) return false;
+            float s = pt_sigma(P, C, M, o + d * t);
+            if (rand01(P, seed) < s / smax) return true;
+        }
+        flag_overrun(P);
+        return false;
+    }
+    Walk w;
+    walk_init(P, w, o, d, t);
+    for (int it = 0;; ++it) {
+        if (it >= kMaxTrackingSteps) {
+            flag_overrun(P);
+            return false;
+        }
+        float te = fminf(walk_exit(w), t_max);
+        float m = walk_majorant(P, w);
+        if (m > 0.f) {
+            float tt = t - logf(1.f - rand01(P, seed)) / m;
+            if (tt < te) {
+                t = tt;
+                float s = pt_sigma(P, C, M, o + d * t);
+                if (rand01(P, seed) < s / m) return true;
+                continue;
+            }
+        }
+        t = te;
+        if (!(t < t_max)) return false;
+        walk_step(w);
+    }
+}
+
+// TransmittanceEstimation (PathTracing.comp:135-151): ratio tracking with a
+// copy of the RNG state
+__device__ __forceinline__ float transmittance_estimation(const PtConsts& P, const CloudConsts& C,
+                                                          const MaterialConsts& M, uint32_t seed, float3 o,
+                                                          float3 d) {
+    float tr = 1.f;
+    float t0, t1;
+    region(P, o, d, t0, t1);
+    if (t0 >= t1) return tr;
+    float t = t0;
+    if (!P.use_bricks) {
+        float smax = P.sigma_t_max;
+        for (int it = 0;; ++it) {
+            if (it >= kMaxTrackingSteps) {
+                flag_overrun(P);
+                break;
+            }
+            t += -logf(1.f - rand01(P, seed)) / smax;
+            if (!(t <= t1)) break;
+            float s = pt_sigma(P, C, M, o + d * t);
+            tr *= 1.f - fmaxf(0.f, s / smax);
+        }
+        return clamp01(tr);
+    }
+    Walk w;
+    walk_init(P, w, o, d, t);
+    for (int it = 0;; ++it) {
+        if (it >= kMaxTrackingSteps) {
+            flag_overrun(P);
+            break;
+        }
+        float te = fminf(walk_exit(w), t1);
+        float m = walk_majorant(P, w);
+        if (m > 0.f) {
+            float tt = t - logf(1.f - rand01(P, seed)) / m;
+            if (tt < te) {
+                t = tt;
+                tr *= 1.f - fmaxf(0.f, pt_sigma(P, C, M, o + d * t) / m);
+                continue;
+            }
+        }
+        t = te;
+        if (!(t < t1)) break;
+        walk_step(w);
+    }
+    return clamp01(tr);
+}
+
+// GetSunVisibility(transmittance_texture, pos) x solar_illuminance, local frame
+__device__ __forceinline__ float3 sun_illuminance(const CloudConsts& C, const AtmoConsts& A, const float4* tlut,
+                                                  int tw, int th, float3 p) {
+    float rho2 = fmaf(p.x, p.x, fmaf(p.y, p.y, p.z * (p.z + 2.f * C.R)));
+    float r2 = fmaf(C.R, C.R, rho2);
+    float inv_r = rsqrtf(r2);
+    float r = r2 * inv_r;
+    float h = __fdividef(rho2, r + C.R);
+    float mu_s = fmaf(C.sun.x, p.x, fmaf(C.sun.y, p.y, C.sun.z * (p.z + C.R))) * inv_r;
+    return sun_visibility_lut(A, tlut, tw, th, r, rho2, h, mu_s) * A.solar_illuminance;
+}
+
+// ENVIRONMENT_LUMINANCE (AtmosphereRenderer.glsl:250-273) for world direction w:
+// GetCosLatLonFromViewDirection, GetSkyViewTextureUvFromCosLatLon (:113-145),
+// sky-view luminance + ground term x sky-view transmittance.
+template <class S>
+__device__ float3 environment(const PtConsts& P, const AtmoConsts& A, const ViewConsts& E, const float4* tlut,
+                              int tw, int th, const S* svl, const S* svt, float3 w) {
+    float cos_lat = dot3(E.up, w);
+    float3 lon = w - E.up * cos_lat;
+    float l2 = dot3(lon, lon);
+    float cos_lon = l2 == 0.f ? 1.f : dot3(lon, E.front) * rsqrtf(l2);
+    float r = E.cam_r;
+    float hd = acosf(sqrtf(fmaxf(E.cam_rho2, 0.f)) / r);
+    float hu = SKYR_PI - hd;
+    float lat = acosf(fminf(fmaxf(cos_lat, -1.f), 1.f));
+    float xl = lat < hu ? 0.5f - 0.5f * sqrtf(fmaxf(1.f - lat / hu, 0.f)) : sqrtf(fmaxf((lat - hu) / hd, 0.f)) * 0.5f + 0.5f;
+    float xo = sqrtf(fmaxf(0.5f - 0.5f * cos_lon, 0.f));
+    float x = xo * (float)(P.sv_w - 1), y = xl * (float)(P.sv_h - 1);
+    float3 lum = bilinear_clamp(svl, P.sv_w, P.sv_h, x, y);
+    float3 tr = bilinear_clamp(svt, P.sv_w, P.sv_h, x, y);
+    if (ray_hits_ground(r, E.cam_rho2, cos_lat)) {
+        float dist = dist_to_bottom(r, E.cam_rho2, cos_lat);
+        float mu_s_g = fmaf(r, dot3(E.sun, E.up), dist * dot3(E.sun, w)) / A.R;
+        float3 sv = sun_visibility_lut(A, tlut, tw, th, A.R, 0.f, 0.f, mu_s_g);
+        lum += (A.ground_albedo * sv * A.solar_illuminance * (clamp01(mu_s_g) / SKYR_PI)) * tr;
+    }
+    return lum;
+}
+
+__device__ __forceinline__ void onb(float3 n, float3& t0, float3& t1) {  // Common.glsl:45-50
+    float s = n.z >= 0.f ? 1.f : -1.f;
+    float a = -1.f / (s + n.z);
+    float b = n.x * n.y * a;
+    t0 = f3(1.f + s * n.x * n.x * a, s * b, -s * n.x);
+    t1 = f3(b, s + n.y * n.y * a, -n.y);
+}
+
+__device__ __forceinline__ float hg_pt(float c, float g) {
+    float a = 1.f - g * g;
+    float b = fmaf(-2.f * g, c, 1.f + g * g);
+    return (0.25f / SKYR_PI) * a / (b * sqrtf(b));
+}
+
+template <class S>
+__global__ void __launch_bounds__(128, 4) pathtrace_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
+                                                           PtConsts P, ViewConsts E,
+                                                           const float4* __restrict__ tlut, int tw, int th,
+                                                           const S* __restrict__ svl, const S* __restrict__ svt,
+                                                           const S* __restrict__ apl, const S* __restrict__ apt,
+                                                           unsigned frame_begin, int n_frames,
+                                                           float4* __restrict__ acc, float4* __restrict__ acc_sq) {
+    int px = P.x0 + blockIdx.x * 16 + (threadIdx.x & 15);
+    int py = P.y0 + blockIdx.y * 8 + (threadIdx.x >> 4);
+    if (px >= P.x1 || py >= P.y1) return;
+    float u = ((float)px + 0.5f) / (float)P.width, v = ((float)py + 0.5f) / (float)P.height;
+    float x = 2.f * u - 1.f, y = 2.f * v - 1.f;
+    float3 dir = C.a0 * x + C.a1 * y + C.af;  // NDC z = 1 (far plane)
+    float wv = fmaf(C.w0, x, fmaf(C.w1, y, C.wf));
+    float3 view = dir * (copysignf(1.f, wv) * rsqrtf(dot3(dir, dir)));
+    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f), sq = sum;
+    for (int f = 0; f < n_frames; ++f) {
+        uint32_t seed = pt_prng(P, pt_prng(P, pt_prng(P, (uint32_t)px) + (uint32_t)py) + frame_begin + (unsigned)f);
+        // Trace (PathTracing.comp:160-249)
+        float3 L = f3(0.f), thr = f3(1.f);
+        bool scattered = false;
+        float scattered_t = 0.f;
+        float alpha = 1.f;
+        float3 o = C.cam, d = view;
+        float c0, c1;
+        region(P, o, d, c0, c1);
+        if (c0 < c1) {
+            o = o + d * c0;
+            int istep = 0;
+            while (istep < P.max_bounces && fmaxf(thr.x, fmaxf(thr.y, thr.z)) > 0.f) {
+                float t0, t1;
+                region(P, o, d, t0, t1);
+                if (t0 >= t1) break;
+                float t = t0;
+                bool scatter = free_flight(P, C, M, seed, o, d, t, t1);
+                if (!scatter) {
+                    if (P.env == SKYR_ENV_OFF || !scattered) break;
+                    if (P.env == SKYR_ENV_CONST_ENVIRONMENT_MAP) {
+                        float3 wd = P.m_front * d.x + P.m_right * d.y + P.m_up * d.z;
+                        L += thr * environment(P, A, E, tlut, tw, th, svl, svt, wd);
+                        break;
+                    }
+                    float rho2 = fmaf(o.x, o.x, fmaf(o.y, o.y, o.z * (o.z + 2.f * C.R)));
+                    float r = sqrtf(fmaf(C.R, C.R, rho2));
+                    float mu = fmaf(d.x, o.x, fmaf(d.y, o.y, d.z * (o.z + C.R))) / r;
+                    if (!ray_hits_ground(r, rho2, mu)) {
+                        float3 wd = P.m_front * d.x + P.m_right * d.y + P.m_up * d.z;
+                        L += thr * environment(P, A, E, tlut, tw, th, svl, svt, wd);
+                        break;
+                    }
+                    o = o + d * dist_to_bottom(r, rho2, mu);
+                    float3 n = f3(o.x, o.y, o.z + C.R);
+                    n = n * rsqrtf(dot3(n, n));
+                    float ndl = dot3(n, C.sun);
+                    float3 bsdf = A.ground_albedo * (1.f / SKYR_PI);
+                    L += thr * (sun_illuminance(C, A, tlut, tw, th, o) * (bsdf * ndl) *
+                                transmittance_estimation(P, C, M, seed, o, C.sun));
+                    if (P.env == SKYR_ENV_GROUND_SINGLE_BOUNCE) break;
+                    // GenerateLambertSample (PathTracing.comp:119-129)
+                    float st = sqrtf(rand01(P, seed));
+                    float ct = sqrtf(clamp01(1.f - st * st));
+                    float3 b0, b1;
+                    onb(n, b0, b1);
+                    float sp, cp;
+                    sincosf(2.f * SKYR_PI * rand01(P, seed), &sp, &cp);
+                    d = b0 * (st * sp) + b1 * (st * cp) + n * ct;
+                    thr *= A.ground_albedo;
+                } else {
+                    if (!scattered) {
+                        float3 dc = C.cam - o;
+                        scattered_t = sqrtf(dot3(dc, dc));
+                    }
+                    scattered = true;
+                    o = o + d * t;
+                    float cs = dot3(d, C.sun);
+                    float ph = hg_pt(cs, P.g_back) * (1.f - P.ratio) + hg_pt(cs, P.g_fwd) * P.ratio;
+                    L += thr * (sun_illuminance(C, A, tlut, tw, th, o) *
+                                (ph * transmittance_estimation(P, C, M, seed, o, C.sun)));
+                    // GenerateHGSample (PathTracing.comp:98-117)
+                    if (P.importance_sampling) {
+                        float g = rand01(P, seed) < P.ratio ? P.g_fwd : P.g_back;
+                        float xi = rand01(P, seed);
+                        float opg = 1.f + g * g, omg = 1.f - g * g, o2g = 0.5f / g;
+                        float tt = omg / (1.f - g + 2.f * g * xi);
+                        float ct = o2g * (opg - tt * tt);
+                        float st = sqrtf(clamp01(1.f - ct * ct));
+                        float3 b0, b1;
+                        onb(d, b0, b1);
+                        float sp, cp;
+                        sincosf(2.f * SKYR_PI * rand01(P, seed), &sp, &cp);
+                        d = b0 * (st * sp) + b1 * (st * cp) + d * ct;
+                    } else {
+                        float phi = 2.f * SKYR_PI * rand01(P, seed);
+                        float c = 1.f - 2.f * rand01(P, seed);
+                        float s = sqrtf(clamp01(1.f - c * c));
+                        float sp, cp;
+                        sincosf(phi, &sp, &cp);
+                        float3 nd = f3(cp * s, sp * s, c);
+                        float cn = dot3(d, nd);
+                        float val = hg_pt(cn, P.g_back) * (1.f - P.ratio) + hg_pt(cn, P.g_fwd) * P.ratio;
+                        thr = thr * (val * 4.f * SKYR_PI);
+                        d = nd;
+                    }
+                }
+                ++istep;
+            }
+            alpha = scattered ? 0.f : 1.f;
+        }
+        if (scattered) {
+            // GetAerialPerspective (VolumetricCloudCommon.glsl:81-98) at the first scattering distance
+            float ta = scattered_t;
+            float mu = view.z;
+            if (C.atmo_in_space != 0.f) {
+                float r = C.R + C.cam.z, rm = r * mu;
+                float cc = (C.cam.z - A.thickness) * (r + A.top);
+                float disc = rm * rm - cc;
+                if (mu < 0.f && disc >= 0.f) ta -= fmaxf(cc / (-rm + sqrtf(disc)), 0.f);
+                else ta = 0.f;
+            }
+            float wz = sqrtf(fmaxf(ta, 0.f) * C.inv_ap_max_distance);
+            float ax = u * (float)(C.ap_w - 1), ay = v * (float)(C.ap_h - 1), az = wz * (float)(C.ap_d - 1);
+            float3 at = trilinear_clamp(apt, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
+            float3 al = trilinear_clamp(apl, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
+            L = L * at + al;
+        }
+        sum.x += L.x; sum.y += L.y; sum.z += L.z; sum.w += alpha;
+        sq.x += L.x * L.x; sq.y += L.y * L.y; sq.z += L.z * L.z; sq.w += alpha * alpha;
+    }
+    size_t pix = (size_t)py * P.width + px;
+    float4 a = acc[pix];
+    acc[pix] = make_float4(a.x + sum.x, a.y + sum.y, a.z + sum.z, a.w + sum.w);
+    if (acc_sq) {
+        float4 b = acc_sq[pix];
+        acc_sq[pix] = make_float4(b.x + sq.x, b.y + sq.y, b.z + sq.z, b.w + sq.w);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Synthetic grid and brick majorants
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) grid_generate_kernel(skyr_grid_generator g, unsigned short* __restrict__ out) {
+    size_t n = (size_t)g.nx * g.ny * g.nz;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / ((size_t)g.nx * g.ny));
+    float3 p = f3(((float)x + 0.5f) / (float)g.nx, ((float)y + 0.5f) / (float)g.ny, ((float)z + 0.5f) / (float)g.nz);
+    skyr_noise_create_info ci{g.seed, g.base_frequency, 1.f, 0.f};
+    float w = fbm(SKYR_NOISE_WORLEY, p, ci, g.octaves);
+    float3 q = f3((p.x - g.center[0]) / g.radii[0], (p.y - g.center[1]) / g.radii[1], (p.z - g.center[2]) / g.radii[2]);
+    float dd = sqrtf(dot3(q, q));
+    float env = 1.f - smoothstepf(g.inner, 1.f, dd);
+    float v = clamp01(w * env - g.threshold) / (1.f - g.threshold);
+    out[i] = __half_as_ushort(__float2half_rn(v));
+}
+
+// one warp per brick: max over the brick plus a one-voxel apron
+__global__ void __launch_bounds__(128) grid_majorant_kernel(const unsigned short* __restrict__ grid, int nx, int ny,
+                                                            int nz, int brick, int bx, int by, int bz, float density,
+                                                            float* __restrict__ out) {
+    int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (wid >= bx * by * bz) return;
+    int i = wid % bx, j = (wid / bx) % by, k = wid / (bx * by);
+    int e = brick + 2;
+    float m = 0.f;
+    for (int q = lane; q < e * e * e; q += 32) {
+        int x = i * brick - 1 + q % e, y = j * brick - 1 + (q / e) % e, z = k * brick - 1 + q / (e * e);
+        if ((unsigned)x < (unsigned)nx && (unsigned)y < (unsigned)ny && (unsigned)z < (unsigned)nz)
+            m = fmaxf(m, __half2float(__ushort_as_half(grid[((size_t)z * ny + y) * nx + x])));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) out[wid] = m * density;
+}
+
+__global__ void __launch_bounds__(256) pt_resolve_kernel(const float4* __restrict__ acc, int n, float inv_frames,
+                                                         const __half2* __restrict__ bg, __half2* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 a = acc[i];
+    float3 c = f3(0.f);
+    if (bg) {
+        uint2 raw = reinterpret_cast<const uint2*>(bg)[i];
+        float2 lo = __half22float2(*reinterpret_cast<__half2*>(&raw.x));
+        float2 hi = __half22float2(*reinterpret_cast<__half2*>(&raw.y));
+        c = f3(lo.x, lo.y, hi.x);
+    }
+    float w = a.w * inv_frames;
+    float3 col = c * w + f3(a.x, a.y, a.z) * inv_frames;
+    store_rgba(out, (size_t)i, col, 1.f);
+}
+
+}  // namespace skyr
+
+using namespace skyr;
+
+extern "C" {
+
+int skyr_pathtrace_parameters_default(skyr_pathtrace_parameters* p) {
+    if (!p) return set_error(SKYR_EINVAL, "null parameters");
+    // PathTracing::InitParam defaults (src/SkyRendering/VolumetricCloud.h:104-114)
+    *p = skyr_pathtrace_parameters{};
+    p->max_bounces = 128;
+    p->region_box_half_width = 100.f;
+    p->importance_sampling = 1;
+    p->forward_phase_g = 0.85f;
+    p->back_phase_g = -0.15f;
+    p->forward_scattering_ratio = 0.7f;
+    p->prng = SKYR_PRNG_PCG_HASH;
+    p->environment_lighting = SKYR_ENV_GROUND_MULTI_BOUNCE;
+    p->sigma_t_max = 15.f;  // VolumetricCloudDefaultMaterialCommon::density_
+    p->use_brick_majorants = 1;
+    return SKYR_OK;
+}
+
+size_t skyr_grid_bytes(int nx, int ny, int nz) {
+    if (nx < 1 || ny < 1 || nz < 1) return 0;
+    return (size_t)nx * ny * nz * 2;
+}
+
+int skyr_grid_brick_count(int n, int brick) {
+    if (n < 1 || brick < 1) return 0;
+    return (n + brick - 1) / brick;
+}
+
+int skyr_grid_generate(skyr_ctx* ctx, const skyr_grid_generator* g, void* out) {
+    if (!ctx || !g || !out) return set_error(SKYR_EINVAL, "null argument");
+    if (g->nx < 1 || g->ny < 1 || g->nz < 1 || (size_t)g->nx * g->ny * g->nz > (size_t(1) << 33))
+        return set_error(SKYR_EINVAL, "bad grid size");
+    if (g->octaves < 1 || g->octaves > 16 || g->base_frequency < 1 || ((long long)g->base_frequency << (g->octaves - 1)) > (1 << 20))
+        return set_error(SKYR_EINVAL, "bad grid noise frequency / octaves");
+    if (!(g->radii[0] > 0.f) || !(g->radii[1] > 0.f) || !(g->radii[2] > 0.f) || !(g->threshold < 1.f) ||
+        !(g->inner < 1.f))
+        return set_error(SKYR_EINVAL, "bad grid envelope");
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    size_t n = (size_t)g->nx * g->ny * g->nz;
+    grid_generate_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(*g,
+                                                                            reinterpret_cast<unsigned short*>(out));
+    return check_cuda(cudaGetLastError(), "grid generator kernel");
+}
+
+int skyr_grid_majorants(skyr_ctx* ctx, const skyr_density_grid* gd, float* out) {
+    if (!ctx || !gd || !gd->data || !out) return set_error(SKYR_EINVAL, "null argument");
+    if (gd->nx < 1 || gd->ny < 1 || gd->nz < 1 || gd->brick < 1) return set_error(SKYR_EINVAL, "bad grid");
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    int bx = skyr_grid_brick_count(gd->nx, gd->brick), by = skyr_grid_brick_count(gd->ny, gd->brick),
+        bz = skyr_grid_brick_count(gd->nz, gd->brick);
+    long long warps = (long long)bx * by * bz;
+    grid_majorant_kernel<<<(unsigned)((warps * 32 + 127) / 128), 128, 0, ctx->stream>>>(
+        reinterpret_cast<const unsigned short*>(gd->data), gd->nx, gd->ny, gd->nz, gd->brick, bx, by, bz,
+        gd->density, out);
+    return check_cuda(cudaGetLastError(), "grid majorant kernel");
+}
+
+int skyr_pathtrace(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                   const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                   const skyr_cloud_textures* textures, const skyr_density_grid* grid,
+                   const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
+                   const skyr_atmosphere_render_parameters* env_view, const skyr_lut_sizes* sizes,
+                   const void* transmittance, const void* sky_view_luminance, const void* sky_view_transmittance,
+                   const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
+                   unsigned frame_begin, int n_frames, const int* region_px, float* accumulation,
+                   float* accumulation_sq) {
+    if (!ctx || !atmosphere || !cloud || !pt || !view || !env_view || !sizes || !accumulation)
+        return set_error(SKYR_EINVAL, "null argument");
+    if (!transmittance || !sky_view_luminance || !sky_view_transmittance || !aerial_perspective_luminance ||
+        !aerial_perspective_transmittance)
+        return set_error(SKYR_EINVAL, "null LUT input");
+    if (n_frames < 0 || n_frames > (1 << 20)) return set_error(SKYR_EINVAL, "n_frames out of range");
+    if (pt->max_bounces < 0 || pt->environment_lighting < SKYR_ENV_OFF ||
+        pt->environment_lighting > SKYR_ENV_GROUND_MULTI_BOUNCE || pt->prng < 0 || pt->prng > 1)
+        return set_error(SKYR_EINVAL, "bad path tracer parameters");
+    if (!std::isfinite(pt->sigma_t_max) || pt->sigma_t_max < 0.f || !(std::fabs(pt->forward_phase_g) < 1.f) ||
+        !(std::fabs(pt->back_phase_g) < 1.f) || !(pt->forward_scattering_ratio >= 0.f) ||
+        !(pt->forward_scattering_ratio <= 1.f) || !std::isfinite(pt->region_box_half_width))
+        return set_error(SKYR_EINVAL, "path tracer parameters out of range");
+    if (pt->importance_sampling && (pt->forward_phase_g == 0.f || pt->back_phase_g == 0.f))
+        return set_error(SKYR_EINVAL, "HG importance sampling needs g != 0 (HenyeyGreensteinInvertcdf divides by g)");
+    bool use_grid = grid && grid->data;
+    if (!use_grid && !material) return set_error(SKYR_EINVAL, "need a density grid or a material");
+    if (use_grid && pt->use_brick_majorants && !grid->majorant)
+        return set_error(SKYR_EINVAL, "brick majorants requested but the grid has none");
+    if (!use_grid && pt->use_brick_majorants) return set_error(SKYR_ENOTSUP, "brick majorants need a density grid");
+    skyr_cloud_material mat_default;
+    skyr_cloud_textures tex_empty{};
+    if (!material) {
+        skyr_cloud_material_default(SKYR_MATERIAL_MINIMAL, &mat_default);
+        material = &mat_default;
+    }
+    if (!textures) textures = &tex_empty;
+    CloudConsts C;
+    MaterialConsts M;
+    if (int st = derive_cloud_consts(*atmosphere, *cloud, *material, *textures, *view, *sizes, C, M)) return st;
+    AtmoConsts A;
+    derive_atmo_consts(*atmosphere, A);
+    ViewConsts E;
+    derive_view_consts(*atmosphere, *env_view, E);
+    PtConsts P;
+    std::memset(&P, 0, sizeof(P));
+    float hw = pt->region_box_half_width;
+    P.box_min = make_float3(-hw, -hw, C.bottom);
+    P.box_max = make_float3(hw, hw, C.top);
+    P.max_bounces = pt->max_bounces;
+    P.importance_sampling = pt->importance_sampling;
+    P.prng = pt->prng;
+    P.env = pt->environment_lighting;
+    P.g_fwd = pt->forward_phase_g;
+    P.g_back = pt->back_phase_g;
+    P.ratio = pt->forward_scattering_ratio;
+    P.sigma_t_max = pt->sigma_t_max;
+    if (use_grid) {
+        if (grid->nx < 1 || grid->ny < 1 || grid->nz < 1 || !(grid->voxel_size > 0.f) || grid->brick < 1 ||
+            !std::isfinite(grid->density) || grid->density < 0.f || !std::isfinite(grid->origin[0]) ||
+            !std::isfinite(grid->origin[1]) || !std::isfinite(grid->origin[2]))
+            return set_error(SKYR_EINVAL, "bad density grid");
+        P.grid = reinterpret_cast<const unsigned short*>(grid->data);
+        P.nx = grid->nx;
+        P.ny = grid->ny;
+        P.nz = grid->nz;
+        P.origin = make_float3(grid->origin[0], grid->origin[1], grid->origin[2]);
+        P.inv_voxel = 1.f / grid->voxel_size;
+        P.density = grid->density;
+        P.maj = grid->majorant;
+        P.bx = skyr_grid_brick_count(grid->nx, grid->brick);
+        P.by = skyr_grid_brick_count(grid->ny, grid->brick);
+        P.bz = skyr_grid_brick_count(grid->nz, grid->brick);
+        P.brick_size = grid->voxel_size * (float)grid->brick;
+        P.use_bricks = pt->use_brick_majorants ? 1 : 0;
+        float gmax[3] = {grid->origin[0] + grid->nx * grid->voxel_size, grid->origin[1] + grid->ny * grid->voxel_size,
+                         grid->origin[2] + grid->nz * grid->voxel_size};
+        P.box_min = make_float3(fmaxf(P.box_min.x, grid->origin[0]), fmaxf(P.box_min.y, grid->origin[1]),
+                                fmaxf(P.box_min.z, grid->origin[2]));
+        P.box_max = make_float3(fminf(P.box_max.x, gmax[0]), fminf(P.box_max.y, gmax[1]), fminf(P.box_max.z, gmax[2]));
+    }
+    {
+        // kModelMatrix3 (VolumetricCloud.cpp:188-200, 515-519): local -> world directions
+        double R = atmosphere->bottom_radius;
+        double c[3] = {view->camera_position[0], view->camera_position[1] + R, view->camera_position[2]};
+        double cl = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        double up[3] = {c[0] / cl, c[1] / cl, c[2] / cl};
+        double fr[3] = {0.0, up[2], -up[1]};  // cross(up, (1,0,0))
+        double fl = std::sqrt(fr[1] * fr[1] + fr[2] * fr[2]);
+        fr[1] /= fl;
+        fr[2] /= fl;
+        double rt[3] = {up[1] * fr[2] - up[2] * fr[1], up[2] * fr[0] - up[0] * fr[2], up[0] * fr[1] - up[1] * fr[0]};
+        double rl = std::sqrt(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2]);
+        P.m_front = make_float3((float)fr[0], (float)fr[1], (float)fr[2]);
+        P.m_right = make_float3((float)(rt[0] / rl), (float)(rt[1] / rl), (float)(rt[2] / rl));
+        P.m_up = make_float3((float)up[0], (float)up[1], (float)up[2]);
+    }
+    P.sv_w = sizes->sky_view_width;
+    P.sv_h = sizes->sky_view_height;
+    P.width = view->width;
+    P.height = view->height;
+    if (region_px) {
+        P.x0 = std::max(region_px[0], 0);
+        P.y0 = std::max(region_px[1], 0);
+        P.x1 = std::min(region_px[2], view->width);
+        P.y1 = std::min(region_px[3], view->height);
+    } else {
+        P.x0 = P.y0 = 0;
+        P.x1 = view->width;
+        P.y1 = view->height;
+    }
+    if (P.x1 <= P.x0 || P.y1 <= P.y0 || n_frames == 0) return SKYR_OK;
+    if (sizes->sky_view_width < 2 || sizes->sky_view_height < 2) return set_error(SKYR_EINVAL, "bad sky-view size");
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    if (int e = ensure_status(ctx)) return e;
+    P.status = ctx->d_status;
+    dim3 gridd((P.x1 - P.x0 + 15) / 16, (P.y1 - P.y0 + 7) / 8);
+    const float4* T = reinterpret_cast<const float4*>(transmittance);
+    float4* acc = reinterpret_cast<float4*>(accumulation);
+    float4* acc2 = reinterpret_cast<float4*>(accumulation_sq);
+    if (sizes->format == SKYR_FORMAT_RGBA16F) {
+        using S = __half2;
+        pathtrace_kernel<S><<<gridd, 128, 0, ctx->stream>>>(
+            C, M, A, P, E, T, sizes->transmittance_width, sizes->transmittance_height,
+            reinterpret_cast<const S*>(sky_view_luminance), reinterpret_cast<const S*>(sky_view_transmittance),
+            reinterpret_cast<const S*>(aerial_perspective_luminance),
+            reinterpret_cast<const S*>(aerial_perspective_transmittance), frame_begin, n_frames, acc, acc2);
+    } else {
+        using S = float4;
+        pathtrace_kernel<S><<<gridd, 128, 0, ctx->stream>>>(
+            C, M, A, P, E, T, sizes->transmittance_width, sizes->transmittance_height,
+            reinterpret_cast<const S*>(sky_view_luminance), reinterpret_cast<const S*>(sky_view_transmittance),
+            reinterpret_cast<const S*>(aerial_perspective_luminance),
+            reinterpret_cast<const S*>(aerial_perspective_transmittance), frame_begin, n_frames, acc, acc2);
+    }
+    return check_cuda(cudaGetLastError(), "path tracer kernel");
+}
+
+int skyr_pathtrace_resolve(skyr_ctx* ctx, const float* accumulation, int width, int height, unsigned frames,
+                           const void* background_rgba16f, void* out_rgba16f) {
+    if (!ctx || !accumulation || !out_rgba16f) return set_error(SKYR_EINVAL, "null argument");
+    if (width < 1 || height < 1 || frames < 1) return set_error(SKYR_EINVAL, "bad size or frame count");
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    int n = width * height;
+    pt_resolve_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(
+        reinterpret_cast<const float4*>(accumulation), n, 1.f / (float)frames,
+        reinterpret_cast<const __half2*>(background_rgba16f), reinterpret_cast<__half2*>(out_rgba16f));
+    return check_cuda(cudaGetLastError(), "path tracer resolve kernel");
+}
+
+}  // extern "C"

@@ -1,5 +1,5 @@
 // skyr_modules.cu — lifetime of the per-context scratch buffers.
-#include "../../include/skyr_cloud.h"
+#include "../../include/skyr_pathtrace.h"
 #include "skyr_ctx.cuh"
 
 namespace skyr {
@@ -13,7 +13,32 @@ void ctx_release_resources(skyr_ctx* ctx) {
     ctx->cloud_scratch_bytes = ctx->pt_scratch_bytes = 0;
 }
 
+int ensure_status(skyr_ctx* ctx) {
+    if (ctx->d_status) return SKYR_OK;
+    cudaError_t e = cudaMalloc(&ctx->d_status, sizeof(int));
+    if (e != cudaSuccess) {
+        ctx->d_status = nullptr;
+        return check_cuda(e, "cudaMalloc(status word)");
+    }
+    return check_cuda(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream), "clear status word");
+}
+
 }  // namespace skyr
+
+extern "C" int skyr_ctx_check_status(skyr_ctx* ctx) {
+    using namespace skyr;
+    if (!ctx) return set_error(SKYR_EINVAL, "null context");
+    if (!ctx->d_status) return SKYR_OK;
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    int v = 0;
+    if (int e = check_cuda(cudaMemcpyAsync(&v, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
+                           "read status word"))
+        return e;
+    if (int e = check_cuda(cudaStreamSynchronize(ctx->stream), "synchronize")) return e;
+    if (v == 0) return SKYR_OK;
+    if (int e = check_cuda(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream), "clear status word")) return e;
+    return set_error(SKYR_ETIMEOUT, "a device loop hit its iteration bound (status 0x%x)", v);
+}
 
 size_t skyr_struct_size_ext(int which) {
     switch (which) {
@@ -22,6 +47,9 @@ size_t skyr_struct_size_ext(int which) {
         case 5: return sizeof(skyr_cloud_textures);
         case 6: return sizeof(skyr_cloud_parameters);
         case 7: return sizeof(skyr_cloud_view);
+        case 8: return sizeof(skyr_density_grid);
+        case 9: return sizeof(skyr_grid_generator);
+        case 10: return sizeof(skyr_pathtrace_parameters);
         default: return 0;
     }
 }

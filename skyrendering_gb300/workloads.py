@@ -260,3 +260,58 @@ def frame_view(cam: Camera, sun_zenith_deg: float, sun_azimuth_deg: float = 60.0
     v.frame_id = 0.0
     v.aerial_perspective_lut_max_distance = ap_max_distance
     return v
+
+
+# ---------------------------------------------------------------------------
+# Voxel path-tracer scene: a synthetic dense FP16 grid spanning 1 km along its
+# longest axis, max extinction 40/km, 1.5 km in front of the camera
+# ---------------------------------------------------------------------------
+PT_GRID_DIMS = (512, 640, 352)  # x, y (horizontal), z (up)
+PT_EXTENT_KM = 1.0  # along the longest axis (640 voxels)
+PT_SIGMA_MAX = 40.0
+
+
+def pt_grid_generator(dims=PT_GRID_DIMS, seed=0x5EED) -> _abi.GridGenerator:
+    """Seeded 4-octave Worley fBm inside a soft ellipsoid."""
+    g = _abi.GridGenerator()
+    g.nx, g.ny, g.nz = dims
+    g.seed, g.base_frequency, g.octaves = seed, 4, 4
+    g.center[:] = [0.5, 0.5, 0.45]
+    g.radii[:] = [0.46, 0.46, 0.42]
+    g.inner, g.threshold = 0.55, 0.15
+    return g
+
+
+def pt_grid_placement(dims=PT_GRID_DIMS):
+    """(origin, voxel_size) of the grid in the local z-up cloud frame (km)."""
+    voxel = PT_EXTENT_KM / max(dims)
+    ex, ey, ez = (n * voxel for n in dims)
+    return (1.5, -0.5 * ey, 1.5), voxel
+
+
+def pt_cloud_parameters(dims=PT_GRID_DIMS) -> _abi.CloudParameters:
+    c = frame_cloud_parameters()
+    origin, voxel = pt_grid_placement(dims)
+    c.bottom_altitude = origin[2]
+    c.thickness = dims[2] * voxel
+    return c
+
+
+def pt_parameters() -> _abi.PathtraceParameters:
+    """HG g = 0.857 single lobe, albedo 1, up to 128 bounces, brick majorants."""
+    p = _abi.PathtraceParameters()
+    _abi.call("skyr_pathtrace_parameters_default", C_ref(p))
+    p.forward_phase_g = 0.857
+    p.forward_scattering_ratio = 1.0
+    p.region_box_half_width = 3.0
+    p.sigma_t_max = PT_SIGMA_MAX
+    p.max_bounces = 128
+    return p
+
+
+def pt_camera(width=1024, height=1024) -> Camera:
+    """Mid-cloud altitude, looking along local +x (world -z) at the grid."""
+    origin, voxel = pt_grid_placement()
+    alt = origin[2] + 0.5 * PT_GRID_DIMS[2] * voxel
+    return Camera(position=(0.0, alt, 0.0), yaw=-90.0, pitch=0.0, fovy=35.0, width=width, height=height,
+                  z_near=0.01, z_far=1000.0)
