@@ -58,6 +58,10 @@ T grid_value(const skyr_grid_generator& g, int x, int y, int z) {
     return v;
 }
 
+// Cap on the samples of one tracking walk, as in the CUDA path tracer: the walk
+// ends (free flight: no collision) when it is reached.
+constexpr int kMaxTrackingSteps = 1 << 20;
+
 template <class T>
 struct PathTracerOracle {
     const AtmosphereOracle<T>& O;
@@ -160,10 +164,12 @@ struct PathTracerOracle {
         w.i[a] += w.s[a];
         w.tmax[a] += w.tdel[a];
     }
-    T walk_majorant(const Walk& w) const {
-        if (w.i[0] < 0 || w.i[1] < 0 || w.i[2] < 0 || w.i[0] >= bx || w.i[1] >= by || w.i[2] >= bz) return T(0);
-        return T(maj[((size_t)w.i[2] * by + w.i[1]) * bx + w.i[0]]);
+    T walk_majorant(const Walk& w) const {  // boundary brick for rounding at the box faces
+        int i = std::min(std::max(w.i[0], 0), bx - 1), j = std::min(std::max(w.i[1], 0), by - 1),
+            k = std::min(std::max(w.i[2], 0), bz - 1);
+        return T(maj[((size_t)k * by + j) * bx + i]);
     }
+    T sample_tau(uint32_t& seed) const { return -std::log(T(1) - rand(seed)); }
 
     bool use_bricks() const { return grid && maj && P.use_brick_majorants; }
 
@@ -171,30 +177,34 @@ struct PathTracerOracle {
     bool free_flight(uint32_t& seed, V3<T> o, V3<T> d, T& t, T t_max) const {
         if (!use_bricks()) {
             T smax = T(P.sigma_t_max);
-            while (true) {
+            for (int it = 0; it < kMaxTrackingSteps; ++it) {
                 if (smax <= T(0)) return false;
                 t += -std::log(T(1) - rand(seed)) / smax;
                 if (t > t_max) return false;
                 T s = SampleSigmaT(o + d * t);
                 if (rand(seed) < s / smax) return true;
             }
+            return false;
         }
+        // one exponential optical depth per tentative collision, spent brick by brick
         Walk w;
         walk_init(w, o, d, t);
-        while (true) {
+        T tau = sample_tau(seed);
+        for (int it = 0;; ++it) {
+            if (it >= kMaxTrackingSteps) return false;
             T te = std::min(walk_exit(w), t_max);
             T m = walk_majorant(w);
-            if (m > T(0)) {
-                T tt = t - std::log(T(1) - rand(seed)) / m;
-                if (tt < te) {
-                    t = tt;
-                    T s = SampleSigmaT(o + d * t);
-                    if (rand(seed) < s / m) return true;
-                    continue;
-                }
+            T seg = (te - t) * m;
+            if (tau < seg) {
+                t += tau / m;
+                T s = SampleSigmaT(o + d * t);
+                if (rand(seed) < s / m) return true;
+                tau = sample_tau(seed);
+                continue;
             }
+            tau -= seg;
             t = te;
-            if (t >= t_max) return false;
+            if (!(t < t_max)) return false;
             walk_step(w);
         }
     }
@@ -209,7 +219,7 @@ struct PathTracerOracle {
         T t = t0;
         if (!use_bricks()) {
             T smax = T(P.sigma_t_max);
-            while (true) {
+            for (int it = 0; it < kMaxTrackingSteps; ++it) {
                 t += -std::log(T(1) - rand(seed)) / smax;
                 if (t > t1) break;
                 T s = SampleSigmaT(o + d * t);
@@ -219,19 +229,20 @@ struct PathTracerOracle {
         }
         Walk w;
         walk_init(w, o, d, t);
-        while (true) {
+        T tau = sample_tau(seed);
+        for (int it = 0; it < kMaxTrackingSteps; ++it) {
             T te = std::min(walk_exit(w), t1);
             T m = walk_majorant(w);
-            if (m > T(0)) {
-                T tt = t - std::log(T(1) - rand(seed)) / m;
-                if (tt < te) {
-                    t = tt;
-                    tr *= T(1) - std::max(T(0), SampleSigmaT(o + d * t) / m);
-                    continue;
-                }
+            T seg = (te - t) * m;
+            if (tau < seg) {
+                t += tau / m;
+                tr *= T(1) - std::max(T(0), SampleSigmaT(o + d * t) / m);
+                tau = sample_tau(seed);
+                continue;
             }
+            tau -= seg;
             t = te;
-            if (t >= t1) break;
+            if (!(t < t1)) break;
             walk_step(w);
         }
         return clampg(tr, T(0), T(1));

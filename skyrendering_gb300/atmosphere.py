@@ -38,6 +38,11 @@ class Context:
     def synchronize(self) -> None:
         _abi.call("skyr_ctx_synchronize", self._ctx)
 
+    def check_status(self) -> None:
+        """Synchronise and raise SkyrError if a kernel of this context raised
+        its device status word (a tracking walk that hit its iteration cap)."""
+        _abi.call("skyr_ctx_check_status", self._ctx)
+
     def close(self) -> None:
         if self._ctx:
             _abi.call("skyr_ctx_destroy", self._ctx)

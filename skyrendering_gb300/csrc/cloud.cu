@@ -373,7 +373,8 @@ __device__ __forceinline__ void shell_intersect(const CloudConsts& C, float mu, 
     }
 }
 
-template <class S, bool COUNT>
+// counters (optional): the frame's raymarch samples and density evaluations
+template <class S>
 __global__ void __launch_bounds__(128, 4) cloud_render_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
                                                            const float4* __restrict__ tlut, int tw, int th,
                                                            const S* __restrict__ ap_lum,
@@ -410,9 +411,13 @@ __global__ void __launch_bounds__(128, 4) cloud_render_kernel(CloudConsts C, Mat
     float jitter = j - floorf(j);
     March mk{1.f, 0.f, 0.f, 0.f, 0.f, 0u, 0u};
     float rmu = (C.R + C.cam.z) * mu;
-    march_segment(C, M, view, it[0], it[1], ent[0], 2.f * (rmu + it[0]), jitter, ph_back, ph_fwd, mk);
-    if (it[3] - it[2] > 0.f)
-        march_segment(C, M, view, it[2], it[3], ent[1], 2.f * (rmu + it[2]), jitter, ph_back, ph_fwd, mk);
+    // the (up to) two shell segments share one inlined copy of the march
+#pragma unroll 1
+    for (int sg = 0; sg < 2; ++sg) {
+        float t0 = sg ? it[2] : it[0], t1 = sg ? it[3] : it[1];
+        if (sg && !(t1 - t0 > 0.f)) break;
+        march_segment(C, M, view, t0, t1, sg ? ent[1] : ent[0], 2.f * (rmu + t0), jitter, ph_back, ph_fwd, mk);
+    }
 
     float avg_t = mk.wsum == 0.f ? frag_dist : mk.wsum / mk.trans_sum;
     float3 ap = C.cam + view * avg_t;
@@ -454,7 +459,7 @@ __global__ void __launch_bounds__(128, 4) cloud_render_kernel(CloudConsts C, Mat
         reinterpret_cast<uint2*>(out_rgba)[pix] = raw;
     }
     if (out_dist) out_dist[pix] = avg_t;
-    if constexpr (COUNT) {
+    if (counters) {
         unsigned long long a = mk.samples, b = mk.evals;
         for (int o = 16; o > 0; o >>= 1) {
             a += __shfl_xor_sync(__activemask(), a, o);
@@ -476,7 +481,6 @@ extern "C" {
 }  // extern "C"
 
 namespace {
-template <bool COUNT>
 int cloud_render_impl(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
                       const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
                       const skyr_cloud_textures* textures, const skyr_cloud_view* view,
@@ -510,13 +514,13 @@ int cloud_render_impl(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmospher
     dim3 grid((view->width + 15) / 16, (view->height + 7) / 8);
     const float4* T = reinterpret_cast<const float4*>(transmittance);
     if (sizes->format == SKYR_FORMAT_RGBA16F) {
-        cloud_render_kernel<__half2, COUNT><<<grid, 128, 0, ctx->stream>>>(
+        cloud_render_kernel<__half2><<<grid, 128, 0, ctx->stream>>>(
             C, M, A, T, sizes->transmittance_width, sizes->transmittance_height,
             reinterpret_cast<const __half2*>(aerial_perspective_luminance),
             reinterpret_cast<const __half2*>(aerial_perspective_transmittance), blue_noise, depth,
             reinterpret_cast<__half2*>(out_rgba), out_distance, counters);
     } else {
-        cloud_render_kernel<float4, COUNT><<<grid, 128, 0, ctx->stream>>>(
+        cloud_render_kernel<float4><<<grid, 128, 0, ctx->stream>>>(
             C, M, A, T, sizes->transmittance_width, sizes->transmittance_height,
             reinterpret_cast<const float4*>(aerial_perspective_luminance),
             reinterpret_cast<const float4*>(aerial_perspective_transmittance), blue_noise, depth,
@@ -534,7 +538,7 @@ int skyr_cloud_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmospher
                       const skyr_lut_sizes* sizes, const void* transmittance,
                       const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
                       const float* blue_noise, const float* depth, void* out_rgba, float* out_distance) {
-    return cloud_render_impl<false>(ctx, atmosphere, cloud, material, textures, view, sizes, transmittance,
+    return cloud_render_impl(ctx, atmosphere, cloud, material, textures, view, sizes, transmittance,
                                     aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise,
                                     depth, out_rgba, out_distance, nullptr);
 }
@@ -548,7 +552,7 @@ int skyr_cloud_render_counted(skyr_ctx* ctx, const skyr_atmosphere_parameters* a
                               const float* depth, void* out_rgba, float* out_distance,
                               unsigned long long* counters) {
     if (!counters) return set_error(SKYR_EINVAL, "null counters");
-    return cloud_render_impl<true>(ctx, atmosphere, cloud, material, textures, view, sizes, transmittance,
+    return cloud_render_impl(ctx, atmosphere, cloud, material, textures, view, sizes, transmittance,
                                    aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise,
                                    depth, out_rgba, out_distance, counters);
 }

@@ -47,6 +47,7 @@ struct PtConsts {
     int sv_w, sv_h;
     int width, height;
     int x0, y0, x1, y1;
+    int tiles_x, n_items;  // work items of one frame (8x4 pixel tiles x 32)
     int* status;  // bit 0: a tracking walk hit kMaxTrackingSteps
 };
 
@@ -90,13 +91,20 @@ __device__ __forceinline__ float grid_sigma(const PtConsts& P, float3 p) {
     return fmaf(c, r[1] - r[0], r[0]) * P.density;
 }
 
-// SampleSigmaT(vec3 P) of the path tracer (PathTracing.comp:89-91): flat height01
-__device__ __forceinline__ float pt_sigma(const PtConsts& P, const CloudConsts& C, const MaterialConsts& M,
-                                          float3 p) {
-    if (P.grid) return grid_sigma(P, p);
+// The material plug-ins' SampleSigmaT with the path tracer's flat height01.
+// Kept out of line: it holds every material's texture sampling, and the dense
+// grid is the path tracer's fast path.
+__device__ __noinline__ float material_sigma(const CloudConsts& C, const MaterialConsts& M, float3 p) {
     float h01 = clamp01((p.z - C.bottom) * C.inv_layer);
     float3 dc = p - C.cam;
     return sigma_t(C, M, p, h01, sqrtf(dot3(dc, dc)));
+}
+
+// SampleSigmaT(vec3 P) of the path tracer (PathTracing.comp:89-91)
+__device__ __forceinline__ float pt_sigma(const PtConsts& P, const CloudConsts& C, const MaterialConsts& M,
+                                          float3 p) {
+    if (P.grid) return grid_sigma(P, p);
+    return material_sigma(C, M, p);
 }
 
 // CloudRegionIntersect (PathTracing.comp:57-75)
@@ -146,9 +154,17 @@ __device__ __forceinline__ void walk_step(Walk& w) {
     else if (a == 1) { w.i[1] += w.s[1]; w.tmax[1] += w.tdel[1]; }
     else { w.i[2] += w.s[2]; w.tmax[2] += w.tdel[2]; }
 }
+// The walk runs inside the region box, which lies within the grid; an index
+// one brick outside can only come from rounding at the box faces and takes the
+// majorant of the boundary brick.
 __device__ __forceinline__ float walk_majorant(const PtConsts& P, const Walk& w) {
-    if (w.i[0] < 0 || w.i[1] < 0 || w.i[2] < 0 || w.i[0] >= P.bx || w.i[1] >= P.by || w.i[2] >= P.bz) return 0.f;
-    return __ldg(P.maj + ((size_t)w.i[2] * P.by + w.i[1]) * P.bx + w.i[0]);
+    int i = min(max(w.i[0], 0), P.bx - 1), j = min(max(w.i[1], 0), P.by - 1), k = min(max(w.i[2], 0), P.bz - 1);
+    return __ldg(P.maj + ((size_t)k * P.by + j) * P.bx + i);
+}
+
+// Exponential optical depth of one majorant collision: -log(1 - xi)
+__device__ __forceinline__ float sample_tau(const PtConsts& P, uint32_t& seed) {
+    return -logf(1.f - rand01(P, seed));
 }
 
 // free flight in [t, t_max] (delta tracking); true on a collision
@@ -166,27 +182,34 @@ __device__ __forceinline__ bool free_flight(const PtConsts& P, const CloudConsts
         flag_overrun(P);
         return false;
     }
+    // Piecewise-constant majorant: one exponential optical depth per tentative
+    // collision, spent brick by brick (tau -= m * length), so a brick crossing
+    // costs no logarithm.  The brick steps form their own inner loop, so that
+    // the lanes of a warp run the density evaluation together.
     Walk w;
     walk_init(P, w, o, d, t);
-    for (int it = 0;; ++it) {
-        if (it >= kMaxTrackingSteps) {
-            flag_overrun(P);
-            return false;
-        }
-        float te = fminf(walk_exit(w), t_max);
-        float m = walk_majorant(P, w);
-        if (m > 0.f) {
-            float tt = t - logf(1.f - rand01(P, seed)) / m;
-            if (tt < te) {
-                t = tt;
-                float s = pt_sigma(P, C, M, o + d * t);
-                if (rand01(P, seed) < s / m) return true;
-                continue;
+    float tau = sample_tau(P, seed);
+    int it = 0;
+    for (;;) {
+        float m;
+        for (;;) {
+            if (++it > kMaxTrackingSteps) {
+                flag_overrun(P);
+                return false;
             }
+            float te = fminf(walk_exit(w), t_max);
+            m = walk_majorant(P, w);
+            float seg = (te - t) * m;
+            if (tau < seg) break;
+            tau -= seg;
+            t = te;
+            if (!(t < t_max)) return false;
+            walk_step(w);
         }
-        t = te;
-        if (!(t < t_max)) return false;
-        walk_step(w);
+        t += tau / m;
+        float s = pt_sigma(P, C, M, o + d * t);
+        if (rand01(P, seed) < s / m) return true;
+        tau = sample_tau(P, seed);
     }
 }
 
@@ -216,24 +239,33 @@ __device__ __forceinline__ float transmittance_estimation(const PtConsts& P, con
     }
     Walk w;
     walk_init(P, w, o, d, t);
-    for (int it = 0;; ++it) {
-        if (it >= kMaxTrackingSteps) {
-            flag_overrun(P);
-            break;
-        }
-        float te = fminf(walk_exit(w), t1);
-        float m = walk_majorant(P, w);
-        if (m > 0.f) {
-            float tt = t - logf(1.f - rand01(P, seed)) / m;
-            if (tt < te) {
-                t = tt;
-                tr *= 1.f - fmaxf(0.f, pt_sigma(P, C, M, o + d * t) / m);
-                continue;
+    float tau = sample_tau(P, seed);
+    int it = 0;
+    for (;;) {
+        float m;
+        bool done = false;
+        for (;;) {
+            if (++it > kMaxTrackingSteps) {
+                flag_overrun(P);
+                done = true;
+                break;
             }
+            float te = fminf(walk_exit(w), t1);
+            m = walk_majorant(P, w);
+            float seg = (te - t) * m;
+            if (tau < seg) break;
+            tau -= seg;
+            t = te;
+            if (!(t < t1)) {
+                done = true;
+                break;
+            }
+            walk_step(w);
         }
-        t = te;
-        if (!(t < t1)) break;
-        walk_step(w);
+        if (done) break;
+        t += tau / m;
+        tr *= 1.f - fmaxf(0.f, pt_sigma(P, C, M, o + d * t) / m);
+        tau = sample_tau(P, seed);
     }
     return clamp01(tr);
 }
@@ -292,6 +324,185 @@ __device__ __forceinline__ float hg_pt(float c, float g) {
     return (0.25f / SKYR_PI) * a / (b * sqrtf(b));
 }
 
+// Work items of one frame: the region in 8x4 pixel tiles, 32 items per tile
+// (items past the region's right / bottom edge are skipped).
+__device__ __forceinline__ bool item_pixel(const PtConsts& P, int item, int& px, int& py) {
+    int tile = item >> 5, k = item & 31;
+    px = P.x0 + (tile % P.tiles_x) * 8 + (k & 7);
+    py = P.y0 + (tile / P.tiles_x) * 4 + (k >> 3);
+    return px < P.x1 && py < P.y1;
+}
+
+// Primary ray through the pixel centre at NDC z = 1 (far plane); also the
+// texture coordinates of the pixel for the aerial-perspective lookup.
+__device__ __forceinline__ float3 primary_dir(const CloudConsts& C, const PtConsts& P, int px, int py, float& u,
+                                              float& v) {
+    u = ((float)px + 0.5f) / (float)P.width;
+    v = ((float)py + 0.5f) / (float)P.height;
+    float x = 2.f * u - 1.f, y = 2.f * v - 1.f;
+    float3 dir = C.a0 * x + C.a1 * y + C.af;
+    float wv = fmaf(C.w0, x, fmaf(C.w1, y, C.wf));
+    return dir * (copysignf(1.f, wv) * rsqrtf(dot3(dir, dir)));
+}
+
+// One path of Trace (PathTracing.comp:160-249) in flight on one lane.
+struct PathState {
+    float3 o, d, L, thr;
+    uint32_t seed;
+    int px, py, istep;
+    float scattered_t;
+    bool scattered;
+};
+
+// Sample of a finished path: GetAerialPerspective (VolumetricCloudCommon.glsl:
+// 81-98) at the first scattering distance; a = 1 when the path never scattered.
+template <class S>
+__device__ __forceinline__ float4 path_sample(const CloudConsts& C, const AtmoConsts& A, const PtConsts& P,
+                                              const S* apl, const S* apt, const PathState& ps) {
+    float u, v;
+    float3 view = primary_dir(C, P, ps.px, ps.py, u, v);
+    float3 L = ps.L;
+    if (ps.scattered) {
+        float ta = ps.scattered_t;
+        float mu = view.z;
+        if (C.atmo_in_space != 0.f) {
+            float r = C.R + C.cam.z, rm = r * mu;
+            float cc = (C.cam.z - A.thickness) * (r + A.top);
+            float disc = rm * rm - cc;
+            if (mu < 0.f && disc >= 0.f) ta -= fmaxf(cc / (-rm + sqrtf(disc)), 0.f);
+            else ta = 0.f;
+        }
+        float wz = sqrtf(fmaxf(ta, 0.f) * C.inv_ap_max_distance);
+        float ax = u * (float)(C.ap_w - 1), ay = v * (float)(C.ap_h - 1), az = wz * (float)(C.ap_d - 1);
+        float3 at = trilinear_clamp(apt, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
+        float3 al = trilinear_clamp(apl, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
+        L = L * at + al;
+    }
+    return make_float4(L.x, L.y, L.z, ps.scattered ? 0.f : 1.f);
+}
+
+// Start the path of pixel (px, py) for `frame`; false when it ends at once
+// (the view ray misses the cloud region, or no bounces are allowed).
+__device__ __forceinline__ bool start_path(const CloudConsts& C, const PtConsts& P, unsigned frame, PathState& ps) {
+    ps.seed = pt_prng(P, pt_prng(P, pt_prng(P, (uint32_t)ps.px) + (uint32_t)ps.py) + frame);
+    float u, v;
+    ps.d = primary_dir(C, P, ps.px, ps.py, u, v);
+    ps.L = f3(0.f);
+    ps.thr = f3(1.f);
+    ps.scattered = false;
+    ps.scattered_t = 0.f;
+    ps.istep = 0;
+    float c0, c1;
+    region(P, C.cam, ps.d, c0, c1);
+    ps.o = C.cam + ps.d * c0;
+    return c0 < c1 && P.max_bounces > 0;
+}
+
+// One iteration of Trace's bounce loop; false when the path ends.
+template <class S>
+__device__ __forceinline__ bool bounce(const CloudConsts& C, const MaterialConsts& M, const AtmoConsts& A,
+                                       const PtConsts& P, const ViewConsts& E, const float4* tlut, int tw, int th,
+                                       const S* svl, const S* svt, PathState& ps) {
+    float t0, t1;
+    region(P, ps.o, ps.d, t0, t1);
+    if (t0 >= t1) return false;
+    float t = t0;
+    bool scatter = free_flight(P, C, M, ps.seed, ps.o, ps.d, t, t1);
+    if (!scatter) {
+        if (P.env == SKYR_ENV_OFF || !ps.scattered) return false;
+        if (P.env == SKYR_ENV_CONST_ENVIRONMENT_MAP) {
+            float3 wd = P.m_front * ps.d.x + P.m_right * ps.d.y + P.m_up * ps.d.z;
+            ps.L += ps.thr * environment(P, A, E, tlut, tw, th, svl, svt, wd);
+            return false;
+        }
+        float3 o = ps.o, d = ps.d;
+        float rho2 = fmaf(o.x, o.x, fmaf(o.y, o.y, o.z * (o.z + 2.f * C.R)));
+        float r = sqrtf(fmaf(C.R, C.R, rho2));
+        float mu = fmaf(d.x, o.x, fmaf(d.y, o.y, d.z * (o.z + C.R))) / r;
+        if (!ray_hits_ground(r, rho2, mu)) {
+            float3 wd = P.m_front * d.x + P.m_right * d.y + P.m_up * d.z;
+            ps.L += ps.thr * environment(P, A, E, tlut, tw, th, svl, svt, wd);
+            return false;
+        }
+        o = o + d * dist_to_bottom(r, rho2, mu);
+        float3 n = f3(o.x, o.y, o.z + C.R);
+        n = n * rsqrtf(dot3(n, n));
+        float ndl = dot3(n, C.sun);
+        float3 bsdf = A.ground_albedo * (1.f / SKYR_PI);
+        ps.L += ps.thr * (sun_illuminance(C, A, tlut, tw, th, o) * (bsdf * ndl) *
+                          transmittance_estimation(P, C, M, ps.seed, o, C.sun));
+        if (P.env == SKYR_ENV_GROUND_SINGLE_BOUNCE) return false;
+        // GenerateLambertSample (PathTracing.comp:119-129)
+        float st = sqrtf(rand01(P, ps.seed));
+        float ct = sqrtf(clamp01(1.f - st * st));
+        float3 b0, b1;
+        onb(n, b0, b1);
+        float sp, cp;
+        sincosf(2.f * SKYR_PI * rand01(P, ps.seed), &sp, &cp);
+        ps.o = o;
+        ps.d = b0 * (st * sp) + b1 * (st * cp) + n * ct;
+        ps.thr *= A.ground_albedo;
+    } else {
+        if (!ps.scattered) {
+            float3 dc = C.cam - ps.o;
+            ps.scattered_t = sqrtf(dot3(dc, dc));
+        }
+        ps.scattered = true;
+        ps.o = ps.o + ps.d * t;
+        float3 d = ps.d;
+        float cs = dot3(d, C.sun);
+        float ph = hg_pt(cs, P.g_back) * (1.f - P.ratio) + hg_pt(cs, P.g_fwd) * P.ratio;
+        ps.L += ps.thr * (sun_illuminance(C, A, tlut, tw, th, ps.o) *
+                          (ph * transmittance_estimation(P, C, M, ps.seed, ps.o, C.sun)));
+        // GenerateHGSample (PathTracing.comp:98-117)
+        if (P.importance_sampling) {
+            float g = rand01(P, ps.seed) < P.ratio ? P.g_fwd : P.g_back;
+            float xi = rand01(P, ps.seed);
+            float opg = 1.f + g * g, omg = 1.f - g * g, o2g = 0.5f / g;
+            float tt = omg / (1.f - g + 2.f * g * xi);
+            float ct = o2g * (opg - tt * tt);
+            float st = sqrtf(clamp01(1.f - ct * ct));
+            float3 b0, b1;
+            onb(d, b0, b1);
+            float sp, cp;
+            sincosf(2.f * SKYR_PI * rand01(P, ps.seed), &sp, &cp);
+            ps.d = b0 * (st * sp) + b1 * (st * cp) + d * ct;
+        } else {
+            float phi = 2.f * SKYR_PI * rand01(P, ps.seed);
+            float c = 1.f - 2.f * rand01(P, ps.seed);
+            float s = sqrtf(clamp01(1.f - c * c));
+            float sp, cp;
+            sincosf(phi, &sp, &cp);
+            float3 nd = f3(cp * s, sp * s, c);
+            float cn = dot3(d, nd);
+            float val = hg_pt(cn, P.g_back) * (1.f - P.ratio) + hg_pt(cn, P.g_fwd) * P.ratio;
+            ps.thr = ps.thr * (val * 4.f * SKYR_PI);
+            ps.d = nd;
+        }
+    }
+    ++ps.istep;
+    return ps.istep < P.max_bounces && fmaxf(ps.thr.x, fmaxf(ps.thr.y, ps.thr.z)) > 0.f;
+}
+
+// Persistent path tracer with path regeneration.  A work item is one path:
+// (frame, pixel) in frame-major order.  A warp takes kWarpChunk items at a
+// time from the call's counter, and a lane whose path has ended starts the next
+// item of its warp's chunk at the top of the next bounce iteration, so lanes do
+// not idle behind the warp's longest path and the SMs stay full until the
+// call's items run out.  Samples are added to the accumulation buffers with
+// float atomics: the frames of one call may be summed in any order (the sums
+// agree to rounding, not bit for bit, between runs).
+constexpr int kWarpChunk = 32;
+
+template <class S>
+__device__ __forceinline__ void deposit(const CloudConsts& C, const AtmoConsts& A, const PtConsts& P, const S* apl,
+                                        const S* apt, const PathState& ps, float4* acc, float4* acc_sq) {
+    float4 x = path_sample(C, A, P, apl, apt, ps);
+    size_t pix = (size_t)ps.py * P.width + ps.px;
+    atomicAdd(acc + pix, x);
+    if (acc_sq) atomicAdd(acc_sq + pix, make_float4(x.x * x.x, x.y * x.y, x.z * x.z, x.w * x.w));
+}
+
 template <class S>
 __global__ void __launch_bounds__(128, 4) pathtrace_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
                                                            PtConsts P, ViewConsts E,
@@ -299,144 +510,60 @@ __global__ void __launch_bounds__(128, 4) pathtrace_kernel(CloudConsts C, Materi
                                                            const S* __restrict__ svl, const S* __restrict__ svt,
                                                            const S* __restrict__ apl, const S* __restrict__ apt,
                                                            unsigned frame_begin, int n_frames,
-                                                           float4* __restrict__ acc, float4* __restrict__ acc_sq) {
-    int px = P.x0 + blockIdx.x * 16 + (threadIdx.x & 15);
-    int py = P.y0 + blockIdx.y * 8 + (threadIdx.x >> 4);
-    if (px >= P.x1 || py >= P.y1) return;
-    float u = ((float)px + 0.5f) / (float)P.width, v = ((float)py + 0.5f) / (float)P.height;
-    float x = 2.f * u - 1.f, y = 2.f * v - 1.f;
-    float3 dir = C.a0 * x + C.a1 * y + C.af;  // NDC z = 1 (far plane)
-    float wv = fmaf(C.w0, x, fmaf(C.w1, y, C.wf));
-    float3 view = dir * (copysignf(1.f, wv) * rsqrtf(dot3(dir, dir)));
-    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f), sq = sum;
-    for (int f = 0; f < n_frames; ++f) {
-        uint32_t seed = pt_prng(P, pt_prng(P, pt_prng(P, (uint32_t)px) + (uint32_t)py) + frame_begin + (unsigned)f);
-        // Trace (PathTracing.comp:160-249)
-        float3 L = f3(0.f), thr = f3(1.f);
-        bool scattered = false;
-        float scattered_t = 0.f;
-        float alpha = 1.f;
-        float3 o = C.cam, d = view;
-        float c0, c1;
-        region(P, o, d, c0, c1);
-        if (c0 < c1) {
-            o = o + d * c0;
-            int istep = 0;
-            while (istep < P.max_bounces && fmaxf(thr.x, fmaxf(thr.y, thr.z)) > 0.f) {
-                float t0, t1;
-                region(P, o, d, t0, t1);
-                if (t0 >= t1) break;
-                float t = t0;
-                bool scatter = free_flight(P, C, M, seed, o, d, t, t1);
-                if (!scatter) {
-                    if (P.env == SKYR_ENV_OFF || !scattered) break;
-                    if (P.env == SKYR_ENV_CONST_ENVIRONMENT_MAP) {
-                        float3 wd = P.m_front * d.x + P.m_right * d.y + P.m_up * d.z;
-                        L += thr * environment(P, A, E, tlut, tw, th, svl, svt, wd);
-                        break;
-                    }
-                    float rho2 = fmaf(o.x, o.x, fmaf(o.y, o.y, o.z * (o.z + 2.f * C.R)));
-                    float r = sqrtf(fmaf(C.R, C.R, rho2));
-                    float mu = fmaf(d.x, o.x, fmaf(d.y, o.y, d.z * (o.z + C.R))) / r;
-                    if (!ray_hits_ground(r, rho2, mu)) {
-                        float3 wd = P.m_front * d.x + P.m_right * d.y + P.m_up * d.z;
-                        L += thr * environment(P, A, E, tlut, tw, th, svl, svt, wd);
-                        break;
-                    }
-                    o = o + d * dist_to_bottom(r, rho2, mu);
-                    float3 n = f3(o.x, o.y, o.z + C.R);
-                    n = n * rsqrtf(dot3(n, n));
-                    float ndl = dot3(n, C.sun);
-                    float3 bsdf = A.ground_albedo * (1.f / SKYR_PI);
-                    L += thr * (sun_illuminance(C, A, tlut, tw, th, o) * (bsdf * ndl) *
-                                transmittance_estimation(P, C, M, seed, o, C.sun));
-                    if (P.env == SKYR_ENV_GROUND_SINGLE_BOUNCE) break;
-                    // GenerateLambertSample (PathTracing.comp:119-129)
-                    float st = sqrtf(rand01(P, seed));
-                    float ct = sqrtf(clamp01(1.f - st * st));
-                    float3 b0, b1;
-                    onb(n, b0, b1);
-                    float sp, cp;
-                    sincosf(2.f * SKYR_PI * rand01(P, seed), &sp, &cp);
-                    d = b0 * (st * sp) + b1 * (st * cp) + n * ct;
-                    thr *= A.ground_albedo;
-                } else {
-                    if (!scattered) {
-                        float3 dc = C.cam - o;
-                        scattered_t = sqrtf(dot3(dc, dc));
-                    }
-                    scattered = true;
-                    o = o + d * t;
-                    float cs = dot3(d, C.sun);
-                    float ph = hg_pt(cs, P.g_back) * (1.f - P.ratio) + hg_pt(cs, P.g_fwd) * P.ratio;
-                    L += thr * (sun_illuminance(C, A, tlut, tw, th, o) *
-                                (ph * transmittance_estimation(P, C, M, seed, o, C.sun)));
-                    // GenerateHGSample (PathTracing.comp:98-117)
-                    if (P.importance_sampling) {
-                        float g = rand01(P, seed) < P.ratio ? P.g_fwd : P.g_back;
-                        float xi = rand01(P, seed);
-                        float opg = 1.f + g * g, omg = 1.f - g * g, o2g = 0.5f / g;
-                        float tt = omg / (1.f - g + 2.f * g * xi);
-                        float ct = o2g * (opg - tt * tt);
-                        float st = sqrtf(clamp01(1.f - ct * ct));
-                        float3 b0, b1;
-                        onb(d, b0, b1);
-                        float sp, cp;
-                        sincosf(2.f * SKYR_PI * rand01(P, seed), &sp, &cp);
-                        d = b0 * (st * sp) + b1 * (st * cp) + d * ct;
-                    } else {
-                        float phi = 2.f * SKYR_PI * rand01(P, seed);
-                        float c = 1.f - 2.f * rand01(P, seed);
-                        float s = sqrtf(clamp01(1.f - c * c));
-                        float sp, cp;
-                        sincosf(phi, &sp, &cp);
-                        float3 nd = f3(cp * s, sp * s, c);
-                        float cn = dot3(d, nd);
-                        float val = hg_pt(cn, P.g_back) * (1.f - P.ratio) + hg_pt(cn, P.g_fwd) * P.ratio;
-                        thr = thr * (val * 4.f * SKYR_PI);
-                        d = nd;
-                    }
+                                                           int* __restrict__ counter, float4* __restrict__ acc,
+                                                           float4* __restrict__ acc_sq) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int n_total = P.n_items * n_frames;
+    int chunk_next = 0, chunk_end = 0;  // warp-uniform
+    bool exhausted = false;             // warp-uniform
+    bool active = false;
+    PathState ps;
+    ps.px = ps.py = 0;
+    for (;;) {
+        // hand the warp's next items to idle lanes
+        unsigned idle = __ballot_sync(full, !active);
+        while (idle && !exhausted) {
+            if (chunk_next >= chunk_end) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(counter, kWarpChunk);
+                base = __shfl_sync(full, base, 0);
+                if (base >= n_total) {
+                    exhausted = true;
+                    break;
                 }
-                ++istep;
+                chunk_next = base;
+                chunk_end = min(base + kWarpChunk, n_total);
             }
-            alpha = scattered ? 0.f : 1.f;
-        }
-        if (scattered) {
-            // GetAerialPerspective (VolumetricCloudCommon.glsl:81-98) at the first scattering distance
-            float ta = scattered_t;
-            float mu = view.z;
-            if (C.atmo_in_space != 0.f) {
-                float r = C.R + C.cam.z, rm = r * mu;
-                float cc = (C.cam.z - A.thickness) * (r + A.top);
-                float disc = rm * rm - cc;
-                if (mu < 0.f && disc >= 0.f) ta -= fmaxf(cc / (-rm + sqrtf(disc)), 0.f);
-                else ta = 0.f;
+            int take = min(__popc(idle), chunk_end - chunk_next);
+            int rank = __popc(idle & ((1u << lane) - 1u));
+            if (!active && rank < take) {
+                int item = chunk_next + rank;
+                int f = item / P.n_items;
+                if (item_pixel(P, item - f * P.n_items, ps.px, ps.py)) {
+                    active = start_path(C, P, frame_begin + (unsigned)f, ps);
+                    if (!active) deposit(C, A, P, apl, apt, ps, acc, acc_sq);
+                }
             }
-            float wz = sqrtf(fmaxf(ta, 0.f) * C.inv_ap_max_distance);
-            float ax = u * (float)(C.ap_w - 1), ay = v * (float)(C.ap_h - 1), az = wz * (float)(C.ap_d - 1);
-            float3 at = trilinear_clamp(apt, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
-            float3 al = trilinear_clamp(apl, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
-            L = L * at + al;
+            chunk_next += take;
+            idle = __ballot_sync(full, !active);
         }
-        sum.x += L.x; sum.y += L.y; sum.z += L.z; sum.w += alpha;
-        sq.x += L.x * L.x; sq.y += L.y * L.y; sq.z += L.z * L.z; sq.w += alpha * alpha;
-    }
-    size_t pix = (size_t)py * P.width + px;
-    float4 a = acc[pix];
-    acc[pix] = make_float4(a.x + sum.x, a.y + sum.y, a.z + sum.z, a.w + sum.w);
-    if (acc_sq) {
-        float4 b = acc_sq[pix];
-        acc_sq[pix] = make_float4(b.x + sq.x, b.y + sq.y, b.z + sq.z, b.w + sq.w);
+        if (!__any_sync(full, active)) break;
+        if (active && !bounce(C, M, A, P, E, tlut, tw, th, svl, svt, ps)) {
+            deposit(C, A, P, apl, apt, ps, acc, acc_sq);
+            active = false;
+        }
     }
 }
 
 // ---------------------------------------------------------------------------
 // Synthetic grid and brick majorants
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) grid_generate_kernel(skyr_grid_generator g, unsigned short* __restrict__ out) {
-    size_t n = (size_t)g.nx * g.ny * g.nz;
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// voxels [first, end) of the grid (the host splits the grid into short launches)
+__global__ void __launch_bounds__(128) grid_generate_kernel(skyr_grid_generator g, size_t first, size_t end,
+                                                            unsigned short* __restrict__ out) {
+    size_t i = first + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= end) return;
     int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / ((size_t)g.nx * g.ny));
     float3 p = f3(((float)x + 0.5f) / (float)g.nx, ((float)y + 0.5f) / (float)g.ny, ((float)z + 0.5f) / (float)g.nz);
     skyr_noise_create_info ci{g.seed, g.base_frequency, 1.f, 0.f};
@@ -527,9 +654,15 @@ int skyr_grid_generate(skyr_ctx* ctx, const skyr_grid_generator* g, void* out) {
         return set_error(SKYR_EINVAL, "bad grid envelope");
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     size_t n = (size_t)g->nx * g->ny * g->nz;
-    grid_generate_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(*g,
-                                                                            reinterpret_cast<unsigned short*>(out));
-    return check_cuda(cudaGetLastError(), "grid generator kernel");
+    // about 16 M voxels (~0.15 s of 4-octave Worley) per launch
+    const size_t chunk = (size_t)1 << 24;
+    for (size_t first = 0; first < n; first += chunk) {
+        size_t end = std::min(n, first + chunk);
+        grid_generate_kernel<<<(unsigned)((end - first + 127) / 128), 128, 0, ctx->stream>>>(
+            *g, first, end, reinterpret_cast<unsigned short*>(out));
+        if (int e = check_cuda(cudaGetLastError(), "grid generator kernel")) return e;
+    }
+    return SKYR_OK;
 }
 
 int skyr_grid_majorants(skyr_ctx* ctx, const skyr_density_grid* gd, float* out) {
@@ -660,26 +793,36 @@ int skyr_pathtrace(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     if (int e = ensure_status(ctx)) return e;
     P.status = ctx->d_status;
-    dim3 gridd((P.x1 - P.x0 + 15) / 16, (P.y1 - P.y0 + 7) / 8);
+    P.tiles_x = (P.x1 - P.x0 + 7) / 8;
+    long long items = (long long)P.tiles_x * ((P.y1 - P.y0 + 3) / 4) * 32;
+    if (items * n_frames > (1LL << 30))
+        return set_error(SKYR_EINVAL, "path tracer region x frames too large for one call (2^30 paths)");
+    P.n_items = (int)items;
+    // the call's work counter
+    if (int e = ensure_pt_scratch(ctx, sizeof(int))) return e;
+    int* counter = reinterpret_cast<int*>(ctx->pt_scratch);
+    if (int e = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), ctx->stream), "clear work counter")) return e;
     const float4* T = reinterpret_cast<const float4*>(transmittance);
     float4* acc = reinterpret_cast<float4*>(accumulation);
     float4* acc2 = reinterpret_cast<float4*>(accumulation_sq);
-    if (sizes->format == SKYR_FORMAT_RGBA16F) {
-        using S = __half2;
-        pathtrace_kernel<S><<<gridd, 128, 0, ctx->stream>>>(
+    auto launch = [&](auto tag) -> int {
+        using S = decltype(tag);
+        auto kernel = pathtrace_kernel<S>;
+        int per_sm = 0, sms = 0;
+        if (int e = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0), "occupancy"))
+            return e;
+        if (int e = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "SM count"))
+            return e;
+        long long blocks = std::min<long long>((long long)std::max(per_sm, 1) * sms, (items * n_frames + 127) / 128);
+        kernel<<<(unsigned)blocks, 128, 0, ctx->stream>>>(
             C, M, A, P, E, T, sizes->transmittance_width, sizes->transmittance_height,
             reinterpret_cast<const S*>(sky_view_luminance), reinterpret_cast<const S*>(sky_view_transmittance),
             reinterpret_cast<const S*>(aerial_perspective_luminance),
-            reinterpret_cast<const S*>(aerial_perspective_transmittance), frame_begin, n_frames, acc, acc2);
-    } else {
-        using S = float4;
-        pathtrace_kernel<S><<<gridd, 128, 0, ctx->stream>>>(
-            C, M, A, P, E, T, sizes->transmittance_width, sizes->transmittance_height,
-            reinterpret_cast<const S*>(sky_view_luminance), reinterpret_cast<const S*>(sky_view_transmittance),
-            reinterpret_cast<const S*>(aerial_perspective_luminance),
-            reinterpret_cast<const S*>(aerial_perspective_transmittance), frame_begin, n_frames, acc, acc2);
-    }
-    return check_cuda(cudaGetLastError(), "path tracer kernel");
+            reinterpret_cast<const S*>(aerial_perspective_transmittance), frame_begin, n_frames, counter, acc, acc2);
+        if (int e = check_cuda(cudaGetLastError(), "path tracer kernel")) return e;
+        return SKYR_OK;
+    };
+    return sizes->format == SKYR_FORMAT_RGBA16F ? launch(__half2{}) : launch(float4{});
 }
 
 int skyr_pathtrace_resolve(skyr_ctx* ctx, const float* accumulation, int width, int height, unsigned frames,

@@ -28,6 +28,7 @@ int ensure_job_table(skyr_ctx* ctx, size_t bytes);
 void ctx_release_resources(skyr_ctx* ctx);
 // Device status word of the context (allocated on first use, zeroed).
 int ensure_status(skyr_ctx* ctx);
+int ensure_pt_scratch(skyr_ctx* ctx, size_t bytes);
 // Argument validation of the LUT entry points (skyr_api.cu).
 int validate_atmosphere(const skyr_atmosphere_parameters* p, int i);
 int validate_render(const skyr_atmosphere_render_parameters* r, const skyr_atmosphere_parameters* p, int i);

@@ -1,4 +1,6 @@
 // skyr_modules.cu — lifetime of the per-context scratch buffers.
+#include <algorithm>
+
 #include "../../include/skyr_pathtrace.h"
 #include "skyr_ctx.cuh"
 
@@ -11,6 +13,24 @@ void ctx_release_resources(skyr_ctx* ctx) {
     ctx->cloud_scratch = ctx->pt_scratch = nullptr;
     ctx->d_status = nullptr;
     ctx->cloud_scratch_bytes = ctx->pt_scratch_bytes = 0;
+}
+
+// Grow-only per-context scratch of the path tracer (its per-frame work counters).
+int ensure_pt_scratch(skyr_ctx* ctx, size_t bytes) {
+    if (ctx->pt_scratch_bytes >= bytes) return SKYR_OK;
+    if (ctx->pt_scratch) {
+        if (int e = check_cuda(cudaStreamSynchronize(ctx->stream), "synchronize before growing scratch")) return e;
+        cudaFree(ctx->pt_scratch);
+        ctx->pt_scratch = nullptr;
+        ctx->pt_scratch_bytes = 0;
+    }
+    size_t want = std::max(bytes, (size_t)4096);
+    if (int e = check_cuda(cudaMalloc(&ctx->pt_scratch, want), "cudaMalloc(path tracer scratch)")) {
+        ctx->pt_scratch = nullptr;
+        return e;
+    }
+    ctx->pt_scratch_bytes = want;
+    return SKYR_OK;
 }
 
 int ensure_status(skyr_ctx* ctx) {

@@ -1,0 +1,99 @@
+"""Fixed hot-path cases for profilers: set one case up, run it a given number of
+times on one stream, synchronise and exit 0.
+
+    python -m skyrendering_gb300.profile_cases luts  --iters 3
+    python -m skyrendering_gb300.profile_cases cloud --iters 3
+    python -m skyrendering_gb300.profile_cases pt    --iters 2 [--global-majorant] [--size 1024] [--frames 4]
+
+Cases (seeded synthetic inputs from workloads.py):
+  luts   the plain LUT set (T 256x64, MS 32x32, SV 192x108, AP 32^3) of the
+         1 km / 60 deg / sun-zenith-45 frame;
+  cloud  that LUT set once, then the 1920x1080 per-pixel cloud raymarch;
+  pt     the 512x640x352 FP16 Worley-fBm grid (max extinction 40/km), its 16^3
+         brick majorants and the LUT set once, then `frames` path-traced
+         frames of the size x size view per iteration, in one launch (128
+         bounces, HG 0.857).
+The per-iteration CUDA-event time is printed for orientation; it is not a
+benchmark figure (bench.py is).
+"""
+from __future__ import annotations
+
+import argparse
+
+import torch
+
+from . import workloads as W
+from .atmosphere import Context, LutSet, update_lut_set
+from .cloud import NoiseTexture, VolumetricCloud, blue_noise_tile, prepare_textures, textures_struct
+from .pathtrace import DensityGrid, PathTracer
+
+SUN_ZENITH = 45.0
+
+
+def lut_case(ctx, cam):
+    atmo, sizes = W.earth_like_atmosphere(), W.plain_lut_sizes()
+    render = W.render_parameters(cam, SUN_ZENITH)
+    luts = LutSet.allocate(sizes, 1)
+    return atmo, sizes, render, luts, lambda: update_lut_set(ctx, atmo, render, sizes, luts)
+
+
+def cloud_case(ctx):
+    cam = W.frame_camera()
+    atmo, sizes, render, luts, lut_step = lut_case(ctx, cam)
+    lut_step()
+    tex = {"cloud_map": NoiseTexture(W.cloud_map_desc()).generate(ctx),
+           "detail": NoiseTexture(W.base_noise_desc()).generate(ctx)}
+    material = W.frame_material()
+    prepare_textures(ctx, material.type, tex)
+    bn = blue_noise_tile().cuda()
+    view = W.frame_view(cam, SUN_ZENITH)
+    vc = VolumetricCloud(ctx, W.frame_cloud_parameters(), material, textures_struct(**tex))
+    rgba = torch.empty((view.height, view.width, 4), dtype=torch.float16, device="cuda")
+    dist = torch.empty((view.height, view.width), dtype=torch.float32, device="cuda")
+    return lambda: vc.render(atmo, view, sizes, luts, bn, out_rgba=rgba, out_distance=dist)
+
+
+def pt_case(ctx, size: int, global_majorant: bool, frames: int):
+    cam = W.pt_camera(size, size)
+    atmo, sizes, render, luts, lut_step = lut_case(ctx, cam)
+    lut_step()
+    origin, voxel = W.pt_grid_placement()
+    grid = DensityGrid(*W.PT_GRID_DIMS, origin=origin, voxel_size=voxel, density=1.0)
+    grid.generate(ctx, W.pt_grid_generator()).normalize_extinction(ctx, W.PT_SIGMA_MAX)
+    pt = W.pt_parameters()
+    pt.use_brick_majorants = 0 if global_majorant else 1
+    tracer = PathTracer(ctx, pt, W.pt_cloud_parameters(), W.frame_view(cam, SUN_ZENITH), render, sizes, grid=grid)
+    return lambda: tracer.render(atmo, luts, frames)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["luts", "cloud", "pt"])
+    ap.add_argument("--iters", type=int, default=3)
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--global-majorant", action="store_true")
+    ap.add_argument("--frames", type=int, default=4)
+    a = ap.parse_args(argv)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = Context(stream)
+    if a.case == "luts":
+        step = lut_case(ctx, W.frame_camera())[-1]
+    elif a.case == "cloud":
+        step = cloud_case(ctx)
+    else:
+        step = pt_case(ctx, a.size, a.global_majorant, a.frames)
+    torch.cuda.synchronize()
+    for i in range(a.iters):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        print(f"{a.case} iteration {i}: {e0.elapsed_time(e1):.3f} ms")
+    ctx.check_status()
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
