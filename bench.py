@@ -109,10 +109,12 @@ def peaks():
 
 
 def ncu_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
-    f = ROOT / "profiles" / "ncu_dram_bytes.json"
+    """dram__bytes_read.sum + dram__bytes_write.sum of one launch of `kernel`
+    from the committed ncu capture (profiles/dram_bytes_per_launch.json)."""
+    f = ROOT / "profiles" / "dram_bytes_per_launch.json"
     if f.exists():
-        return json.loads(f.read_text()).get(kernel)
+        e = json.loads(f.read_text()).get(kernel)
+        return None if e is None else e.get("bytes")
     return None
 
 
