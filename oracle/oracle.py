@@ -296,3 +296,52 @@ def pathtrace(atmo, cloud, material, textures_host: dict | None, grid_struct, gr
                                 px.ctypes.data_as(I32), n, precision, nthreads or threads(), _dp(s), _dp(sq))
     assert rc == 0
     return s, sq
+
+
+# ---------------------------------------------------------------------------
+# surrogate network
+# ---------------------------------------------------------------------------
+def _declare_mlp(lb):
+    lb.oracle_mlp_predict.restype = C.c_int
+    lb.oracle_mlp_predict.argtypes = [FP, FP, C.c_int, C.c_int, C.c_int, D]
+    lb.oracle_mlp_gradient.restype = C.c_double
+    lb.oracle_mlp_gradient.argtypes = [FP, FP, FP, C.c_int, C.c_double, C.c_double, C.c_int, D]
+    lb.oracle_mlp_adam.restype = None
+    lb.oracle_mlp_adam.argtypes = [D, D, D, D, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+    lb.oracle_mlp_param_count.restype = C.c_int
+
+
+_EXT.append(_declare_mlp)
+
+
+def _fp(a: np.ndarray):
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(FP)
+
+
+def mlp_predict(params: np.ndarray, x: np.ndarray, mirror: bool = True, nthreads: int | None = None) -> np.ndarray:
+    """FP64 forward of the surrogate network: x[n][43] -> y[n][3]."""
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    xx = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.zeros((len(xx), 3))
+    assert lib().oracle_mlp_predict(_fp(p), _fp(xx), len(xx), int(mirror), nthreads or threads(), _dp(y)) == 0
+    return y
+
+
+def mlp_gradient(params: np.ndarray, x: np.ndarray, t: np.ndarray, label_scale: float = 1.0,
+                 loss_eps: float = 1e-2, mirror: bool = True):
+    """(loss, gradient[15491]) of the mean relative-L2 loss, FP64."""
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    xx = np.ascontiguousarray(x, dtype=np.float32)
+    tt = np.ascontiguousarray(t, dtype=np.float32)
+    g = np.zeros(lib().oracle_mlp_param_count())
+    loss = lib().oracle_mlp_gradient(_fp(p), _fp(xx), _fp(tt), len(xx), label_scale, loss_eps, int(mirror), _dp(g))
+    return loss, g
+
+
+def mlp_adam(p: np.ndarray, m: np.ndarray, v: np.ndarray, g: np.ndarray, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8,
+             step: int = 1):
+    """In-place FP64 Adam step on float64 arrays."""
+    for a in (p, m, v, g):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    lib().oracle_mlp_adam(_dp(p), _dp(m), _dp(v), _dp(g), len(p), lr, b1, b2, eps, step)

@@ -417,3 +417,41 @@ int oracle_pathtrace(const skyr_atmosphere_parameters* atmo, const skyr_cloud_pa
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// surrogate network (oracle_mlp.hpp)
+// ---------------------------------------------------------------------------
+#include "oracle_mlp.hpp"
+
+extern "C" {
+
+// y[n][3] = MLP(x[n][43]) in FP64 (BF16 rounding points mirrored when `mirror`)
+int oracle_mlp_predict(const float* params, const float* x, int n, int mirror, int threads, double* y) {
+    orc::MlpOracle net(params, mirror != 0);
+    parallel_for(n, threads, [&](int s) {
+        double xd[orc::kMlpIn];
+        for (int i = 0; i < orc::kMlpIn; ++i) xd[i] = x[(size_t)s * orc::kMlpIn + i];
+        net.predict(xd, y + (size_t)s * orc::kMlpOut);
+    });
+    return 0;
+}
+
+// gradient of the mean relative-L2 loss (grad[15491] overwritten); returns the loss
+double oracle_mlp_gradient(const float* params, const float* x, const float* t, int n, double label_scale,
+                           double loss_eps, int mirror, double* grad) {
+    orc::MlpOracle net(params, mirror != 0);
+    std::vector<double> xd((size_t)n * orc::kMlpIn), td((size_t)n * orc::kMlpOut);
+    for (size_t i = 0; i < xd.size(); ++i) xd[i] = x[i];
+    for (size_t i = 0; i < td.size(); ++i) td[i] = t[i];
+    std::fill(grad, grad + orc::kMlpParams, 0.0);
+    return net.gradient(xd.data(), td.data(), n, label_scale, loss_eps, grad);
+}
+
+void oracle_mlp_adam(double* p, double* m, double* v, const double* g, int n, double lr, double b1, double b2,
+                     double eps, int step) {
+    orc::adam_step(p, m, v, g, n, lr, b1, b2, eps, step);
+}
+
+int oracle_mlp_param_count(void) { return orc::kMlpParams; }
+
+}  // extern "C"

@@ -306,3 +306,34 @@ _SIGNATURES.update({
                                  C.c_uint, C.c_int, P, P, P]),
     "skyr_pathtrace_resolve": (C.c_int, [P, P, C.c_int, C.c_int, C.c_uint, P, P]),
 })
+
+
+# ---------------------------------------------------------------------------
+# skyr_mlp.h
+# ---------------------------------------------------------------------------
+SKYR_MLP_INPUTS, SKYR_MLP_RECORD, SKYR_MLP_WIDTH, SKYR_MLP_OUTPUTS, SKYR_MLP_PARAMS = 43, 48, 64, 3, 15491
+
+
+class MlpHparams(C.Structure):
+    _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
+                ("label_scale", C.c_float), ("loss_epsilon", C.c_float)]
+
+
+STRUCT_IDS.update({11: MlpHparams})
+_SIGNATURES.update({
+    "skyr_mlp_hparams_default": (C.c_int, [C.POINTER(MlpHparams)]),
+    "skyr_mlp_param_count": (C.c_size_t, []),
+    "skyr_mlp_packed_bytes": (C.c_size_t, []),
+    "skyr_mlp_init_params": (C.c_int, [C.c_uint64, P]),
+    "skyr_mlp_pack": (C.c_int, [P, P, C.c_float, P]),
+    "skyr_mlp_infer": (C.c_int, [P, P, P, C.c_int, P]),
+    "skyr_mlp_gradient": (C.c_int, [P, P, C.POINTER(MlpHparams), P, P, C.c_int, P, P]),
+    "skyr_mlp_trainer_create": (C.c_int, [P, P, C.POINTER(MlpHparams), C.POINTER(P)]),
+    "skyr_mlp_trainer_destroy": (C.c_int, [P]),
+    "skyr_mlp_train_step": (C.c_int, [P, P, P, C.c_int, P]),
+    "skyr_mlp_trainer_params": (P, [P]),
+    "skyr_mlp_trainer_packed": (P, [P]),
+    "skyr_mlp_trainer_steps": (C.c_int, [P]),
+    "skyr_mlp_trainer_copy_params": (C.c_int, [P, P]),
+    "skyr_mlp_trainer_copy_packed": (C.c_int, [P, P]),
+})

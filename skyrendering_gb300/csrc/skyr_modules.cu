@@ -1,6 +1,7 @@
 // skyr_modules.cu — lifetime of the per-context scratch buffers.
 #include <algorithm>
 
+#include "../../include/skyr_mlp.h"
 #include "../../include/skyr_pathtrace.h"
 #include "skyr_ctx.cuh"
 
@@ -70,6 +71,7 @@ size_t skyr_struct_size_ext(int which) {
         case 8: return sizeof(skyr_density_grid);
         case 9: return sizeof(skyr_grid_generator);
         case 10: return sizeof(skyr_pathtrace_parameters);
+        case 11: return sizeof(skyr_mlp_hparams);
         default: return 0;
     }
 }
