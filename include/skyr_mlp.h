@@ -77,6 +77,8 @@ int skyr_mlp_train_step(skyr_mlp_trainer* tr, const uint16_t* x, const float* t,
 const float* skyr_mlp_trainer_params(const skyr_mlp_trainer* tr);
 const void* skyr_mlp_trainer_packed(const skyr_mlp_trainer* tr);
 int skyr_mlp_trainer_steps(const skyr_mlp_trainer* tr);
+/* Change the Adam step size for the following steps (learning-rate schedules). */
+int skyr_mlp_trainer_set_learning_rate(skyr_mlp_trainer* tr, float learning_rate);
 /* Copy the current parameters (FP32[SKYR_MLP_PARAMS]) / packed network into
  * caller device buffers, ordered on the trainer's stream. */
 int skyr_mlp_trainer_copy_params(const skyr_mlp_trainer* tr, float* out);

@@ -84,7 +84,8 @@ int skyr_grid_majorants(skyr_ctx* ctx, const skyr_density_grid* grid, float* out
  * accumulates the per-frame results (rgb luminance, a = 1 when the path never
  * scattered) into `accumulation` (device float4 per pixel of the view, +=)
  * and, when `accumulation_sq` is not NULL, their squares into it (+=; for
- * variance estimates).
+ * variance estimates).  The frames of one call are added in no fixed order
+ * (float atomics): sums agree to rounding, not bit for bit, between runs.
  * The density comes from `grid` (dense FP16, may be NULL) else from
  * `material` / `textures` (the reference's material plug-ins).  The
  * environment is the sky-view LUT lookup plus ground term of the
@@ -99,6 +100,39 @@ int skyr_pathtrace(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
                    const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
                    unsigned frame_begin, int n_frames, const int* region, float* accumulation,
                    float* accumulation_sq);
+
+/* skyr_pathtrace over a list of pixels (y * width + x, device ints; entries
+ * outside the view are skipped) instead of a rectangle: the fallback of the
+ * surrogate renderer path-traces only the pixels it flags.  No reference
+ * counterpart. */
+int skyr_pathtrace_pixels(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                          const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                          const skyr_cloud_textures* textures, const skyr_density_grid* grid,
+                          const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
+                          const skyr_atmosphere_render_parameters* env_view, const skyr_lut_sizes* sizes,
+                          const void* transmittance, const void* sky_view_luminance,
+                          const void* sky_view_transmittance, const void* aerial_perspective_luminance,
+                          const void* aerial_perspective_transmittance, unsigned frame_begin, int n_frames,
+                          const int* pixels, int n_pixels, float* accumulation, float* accumulation_sq);
+
+/* In-scattered radiance at points of a density grid, beyond single scattering
+ * of the sun: for each point i (device float[6]: local position p, unit
+ * direction w) `n_paths` paths start at p in a direction drawn from the phase
+ * function about w -- as if a path travelling along w had just scattered at p,
+ * that event being the first of max_bounces -- and continue as in
+ * skyr_pathtrace (next-event estimation at later scattering events, the
+ * environment on escape).  Their radiance is added to out[i] (device float[3],
+ * +=); divided by n_paths it estimates the order >= 2 in-scattered radiance at
+ * p toward -w.  Frame ids frame_begin.. seed the paths.  No reference
+ * counterpart: the training targets of the multiple-scattering surrogate. */
+int skyr_pathtrace_points(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                          const skyr_cloud_parameters* cloud, const skyr_density_grid* grid,
+                          const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
+                          const skyr_atmosphere_render_parameters* env_view, const skyr_lut_sizes* sizes,
+                          const void* transmittance, const void* sky_view_luminance,
+                          const void* sky_view_transmittance, const void* aerial_perspective_luminance,
+                          const void* aerial_perspective_transmittance, unsigned frame_begin, int n_paths,
+                          const float* points, int n_points, float* out);
 
 /* The display pass (VolumetricCloudPathTracing.comp:288-296): for every pixel
  * out = background * (acc.a / frames) + acc.rgb / frames, half4 output; the

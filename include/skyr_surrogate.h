@@ -1,0 +1,104 @@
+/*
+ * skyr_surrogate.h — C ABI of the surrogate-shaded voxel cloud: a 128-step
+ * raymarch through the dense density grid in which single scattering of the
+ * sun is computed and order >= 2 in-scattered radiance comes from the network
+ * of skyr_mlp.h, evaluated inside the march.  No counterpart in the reference
+ * (it stands in for the multiple-scattering heuristic of
+ * VolumetricCloudRender.comp:125-130, and for the path tracer of
+ * VolumetricCloudPathTracing.comp when an image is wanted fast).
+ * Conventions as in skyr.h; positions in the local cloud frame of skyr_cloud.h.
+ *
+ * Network inputs (one feature record, SKYR_MLP_RECORD bf16):
+ *   0       extinction at the point / sigma_ref
+ *   1..32   extinction at the point + d_k * sun, d_k = span * 0.01 * 1000^(k/31)
+ *   33..40  extinction at the point + 0.1 * span * (+-1, +-1, +-1) / sqrt(3)
+ *   41      height of the point within the grid box, 0 (bottom) .. 1 (top)
+ *   42      cos(view direction, sun direction)
+ *   43..47  zero
+ * span = the grid's longest edge.  Features 0..41 are taken at the nodes of a
+ * coarse lattice (every `stride` voxels) and interpolated trilinearly, the same
+ * way for training points and for the raymarch.
+ */
+#ifndef SKYR_SURROGATE_H_
+#define SKYR_SURROGATE_H_
+
+#include "skyr_mlp.h"
+#include "skyr_pathtrace.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Feature lattice of one (grid, sun direction) pair (struct id 12). */
+typedef struct skyr_feature_volume {
+    void* data;        /* device: records [nodes][48] bf16, then sun optical depth [nodes] f32 */
+    int stride;        /* voxels between lattice nodes */
+    int nx, ny, nz;    /* nodes per axis: (grid n + stride - 1) / stride + 1 */
+    float sigma_ref;   /* extinctions are divided by this */
+    float sun[3];      /* local sun direction the lattice was built for */
+} skyr_feature_volume;
+
+/* Raymarch settings (struct id 13). */
+typedef struct skyr_surrogate_parameters {
+    int steps;              /* uniform steps through the grid box (128) */
+    int use_network;        /* 0: single scattering only (the ablation) */
+    float network_error;    /* relative error of the network when error_table is NULL */
+    float min_transmittance;/* a ray ends below this view transmittance (1e-4) */
+    /* Optional device float[SKYR_SURROGATE_ERROR_BINS^2]: relative error of the
+     * network by (feature 0, mean of features 1..8) bins over [0, 1]^2, row =
+     * feature-0 bin (calibrated on validation points); NULL: network_error. */
+    const float* error_table;
+} skyr_surrogate_parameters;
+
+#define SKYR_SURROGATE_ERROR_BINS 8
+
+int skyr_surrogate_parameters_default(skyr_surrogate_parameters* p);
+
+/* Device bytes of the lattice for `grid` at `stride`; fills the node counts. */
+size_t skyr_feature_volume_bytes(const skyr_density_grid* grid, int stride, skyr_feature_volume* fv);
+
+/* Build the lattice of `grid` for the sun of `view` (angles, and the frame of
+ * `atmosphere` / `cloud`): features 0..41 per node and the optical depth to
+ * the sun (a midpoint march at half the voxel edge to the grid box's exit).
+ * fv->data (skyr_feature_volume_bytes), fv->stride and fv->sigma_ref are the
+ * caller's; the node counts and fv->sun are filled in. */
+int skyr_feature_volume_build(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                              const skyr_cloud_parameters* cloud, const skyr_density_grid* grid,
+                              const skyr_cloud_view* view, skyr_feature_volume* fv);
+
+/* Training points of a grid (device float[n][6]: position, unit direction):
+ * half are where rays from random outside points first collide (delta tracking
+ * against the grid's largest extinction `sigma_max`, direction = the ray's),
+ * half uniform in the grid box where the extinction is >= sigma_min (uniform
+ * direction).  Seeded. */
+int skyr_surrogate_sample_points(skyr_ctx* ctx, const skyr_density_grid* grid, float sigma_max, float sigma_min,
+                                 uint64_t seed, int n, float* points);
+
+/* Feature records of points (device float[n][6]) from a lattice. */
+int skyr_surrogate_records(skyr_ctx* ctx, const skyr_density_grid* grid, const skyr_feature_volume* fv,
+                           const float* points, int n, uint16_t* records);
+
+/* Bin of a feature record in the error table (row-major index), for host-side
+ * calibration: device records[n] -> device int bins[n]. */
+int skyr_surrogate_error_bins(skyr_ctx* ctx, const uint16_t* records, int n, int* bins);
+
+/* The surrogate image of `view` (pixels as skyr_pathtrace): per pixel
+ * out_rgba = (luminance rgb, view transmittance), aerial perspective applied at
+ * the transmittance-weighted mean depth; the phase function, the sun and the
+ * atmosphere as in skyr_pathtrace with `pt`.  out_error (device float per
+ * pixel, may be NULL) receives an absolute error estimate: the network's
+ * contribution to the luminance, each step weighted by the relative error of
+ * its error-table bin (or by network_error).  `packed` is the network
+ * (skyr_mlp_pack) or NULL when use_network is 0. */
+int skyr_surrogate_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                          const skyr_cloud_parameters* cloud, const skyr_density_grid* grid,
+                          const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
+                          const skyr_lut_sizes* sizes, const void* transmittance,
+                          const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
+                          const skyr_feature_volume* fv, const void* packed, const skyr_surrogate_parameters* sp,
+                          float* out_rgba, float* out_error);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SKYR_SURROGATE_H_ */

@@ -345,3 +345,86 @@ def mlp_adam(p: np.ndarray, m: np.ndarray, v: np.ndarray, g: np.ndarray, lr=1e-3
     for a in (p, m, v, g):
         assert a.dtype == np.float64 and a.flags.c_contiguous
     lib().oracle_mlp_adam(_dp(p), _dp(m), _dp(v), _dp(g), len(p), lr, b1, b2, eps, step)
+
+
+# ---------------------------------------------------------------------------
+# surrogate: grid lookups, point-source paths, the surrogate raymarch
+# ---------------------------------------------------------------------------
+def _declare_surrogate(lb):
+    lb.oracle_grid_sigma.restype = C.c_int
+    lb.oracle_grid_sigma.argtypes = [P, D, C.c_int, D]
+    lb.oracle_point_radiance.restype = C.c_int
+    lb.oracle_point_radiance.argtypes = [P, P, P, P, P, P, P, D, D, D, D, D, C.c_uint, C.c_int, D, C.c_int, C.c_int,
+                                         D, D]
+    lb.oracle_surrogate_render.restype = C.c_int
+    lb.oracle_surrogate_render.argtypes = [P, P, P, P, P, P, D, D, D, U16, FP, P, FP, C.c_double, C.c_int, C.c_int,
+                                           C.c_double, C.c_double, I32, C.c_int, C.c_int, D, D]
+
+
+_EXT.append(_declare_surrogate)
+
+
+def _grid_copy(grid_struct, data_half, keep):
+    import skyrendering_gb300._abi as A
+
+    g = A.DensityGrid()
+    C.memmove(C.byref(g), C.byref(grid_struct), C.sizeof(g))
+    gh = np.ascontiguousarray(data_half).view(np.uint16)
+    keep.append(gh)
+    g.data = gh.ctypes.data
+    g.majorant = None
+    return g
+
+
+def grid_sigma(grid_struct, data_half: np.ndarray, points: np.ndarray) -> np.ndarray:
+    """FP64 trilinear extinction of the FP16 grid at points[n][3]."""
+    keep = []
+    g = _grid_copy(grid_struct, data_half, keep)
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    out = np.zeros(len(pts))
+    assert lib().oracle_grid_sigma(_ref(g), _dp(pts), len(pts), _dp(out)) == 0
+    return out
+
+
+def _lut_arrays(luts: dict, names):
+    return [np.ascontiguousarray(luts[k], dtype=np.float64) for k in names]
+
+
+def point_radiance(atmo, cloud, grid_struct, data_half, pt, view, env_view, sizes, luts: dict, frame_begin: int,
+                   n_paths: int, points: np.ndarray, nthreads: int | None = None):
+    """Per point (sum, sum of squares) of n_paths point-source path radiances."""
+    keep = []
+    g = _grid_copy(grid_struct, data_half, keep)
+    arrs = _lut_arrays(luts, ("transmittance", "sky_view_luminance", "sky_view_transmittance",
+                              "aerial_perspective_luminance", "aerial_perspective_transmittance"))
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    s, sq = np.zeros((len(pts), 3)), np.zeros((len(pts), 3))
+    rc = lib().oracle_point_radiance(_ref(atmo), _ref(cloud), _ref(g), _ref(pt), _ref(view), _ref(env_view),
+                                     _ref(sizes), *[_dp(a) for a in arrs], frame_begin, n_paths, _dp(pts), len(pts),
+                                     nthreads or threads(), _dp(s), _dp(sq))
+    assert rc == 0
+    return s, sq
+
+
+def surrogate_render(atmo, cloud, grid_struct, data_half, pt, view, sizes, luts: dict, lattice: np.ndarray, fv,
+                     params: np.ndarray, out_scale: float, steps: int, use_network: bool, min_t: float,
+                     rel_err: float, pixels, nthreads: int | None = None):
+    """FP64 surrogate raymarch of listed pixels over the GPU-built lattice bytes:
+    (out[n][4] = rgb, transmittance; err[n])."""
+    keep = []
+    g = _grid_copy(grid_struct, data_half, keep)
+    arrs = _lut_arrays(luts, ("transmittance", "aerial_perspective_luminance", "aerial_perspective_transmittance"))
+    nodes = fv.nx * fv.ny * fv.nz
+    raw = np.ascontiguousarray(lattice, dtype=np.uint8)
+    rec = np.ascontiguousarray(raw[: nodes * 96].view(np.uint16))
+    tau = np.ascontiguousarray(raw[nodes * 96: nodes * 100].view(np.float32))
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    px = np.ascontiguousarray(pixels, dtype=np.int32)
+    out, err = np.zeros((len(px), 4)), np.zeros(len(px))
+    rc = lib().oracle_surrogate_render(_ref(atmo), _ref(cloud), _ref(g), _ref(pt), _ref(view), _ref(sizes),
+                                       *[_dp(a) for a in arrs], rec.ctypes.data_as(U16), tau.ctypes.data_as(FP),
+                                       _ref(fv), p.ctypes.data_as(FP), out_scale, steps, int(use_network), min_t,
+                                       rel_err, px.ctypes.data_as(I32), len(px), nthreads or threads(), _dp(out),
+                                       _dp(err))
+    assert rc == 0
+    return out, err

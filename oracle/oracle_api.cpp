@@ -3,6 +3,7 @@
 // loaded by tests/ and bench.py through ctypes.  Parity status: unpinned
 // (see oracle_math.hpp).
 #include <atomic>
+#include <memory>
 #include <cstring>
 #include <thread>
 
@@ -10,6 +11,7 @@
 #include "oracle_cloud.hpp"
 #include "oracle_noise.hpp"
 #include "oracle_pathtrace.hpp"
+#include "../include/skyr_surrogate.h"
 
 namespace {
 
@@ -311,60 +313,67 @@ int oracle_grid_majorants(const skyr_density_grid* gd, const uint16_t* data, flo
 
 namespace {
 
+// The path-tracer oracle and everything it references, built from the ABI
+// structs (one heap object: the members refer to one another).
 template <class T>
-int pathtrace_t(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
-                const skyr_cloud_material* m, const skyr_cloud_textures* tx, const skyr_density_grid* gd,
-                const skyr_pathtrace_parameters* pt, const skyr_cloud_view* v,
-                const skyr_atmosphere_render_parameters* ev, const skyr_lut_sizes* s, const double* tlut_in,
-                const double* svl_in, const double* svt_in, const double* apl_in, const double* apt_in,
-                unsigned frame_begin, int n_frames, const int* pixels, int n_pixels, int threads, double* sum,
-                double* sumsq) {
-    orc::AtmosphereOracle<T> O{orc::derive_atmosphere<T>(*atmo)};
-    orc::Image<T> tl = image_from<T>(tlut_in, s->transmittance_width, s->transmittance_height);
-    orc::Image<T> sl = image_from<T>(svl_in, s->sky_view_width, s->sky_view_height);
-    orc::Image<T> st = image_from<T>(svt_in, s->sky_view_width, s->sky_view_height);
-    int W = s->aerial_perspective_width, H = s->aerial_perspective_height, D = s->aerial_perspective_depth;
-    orc::Image<T> al = image_from<T>(apl_in, W, H, D), at = image_from<T>(apt_in, W, H, D);
-    orc::CloudOracle<T> C{O, orc::derive_cloud_frame<T>(*atmo, *cp, *m, *tx, *v), {}, {}, {}, {}, nullptr,
-                          nullptr, nullptr, nullptr};
-    auto set = [](orc::Tex8& t, const void* p, const skyr_noise_texture_desc& d, bool border) {
-        t.data = (const uint8_t*)p;
-        t.w = d.width; t.h = d.height; t.d = d.depth; t.channels = d.channels;
-        t.border = border;
-        t.init();
-    };
-    if (tx->cloud_map) set(C.cloud_map, tx->cloud_map, tx->cloud_map_desc, false);
-    if (tx->detail) set(C.detail, tx->detail, tx->detail_desc, false);
-    if (tx->displacement) set(C.displacement, tx->displacement, tx->displacement_desc, false);
-    if (tx->voxel) set(C.voxel, tx->voxel, tx->voxel_desc, true);
-    C.tlut = &tl;
-    C.ap_lum = &al;
-    C.ap_trans = &at;
-    orc::ViewLutOracle<T> V{O, orc::derive_render_frame<T>(*atmo, *ev)};
-    orc::PathTracerOracle<T> PT{O, C, V, &sl, &st, *pt};
-    // box: the flat AABB [-w, w]^2 x [bottom, top], clipped to the grid
-    T hw = T(pt->region_box_half_width);
-    PT.box_min = orc::V3<T>(-hw, -hw, C.F.bottom);
-    PT.box_max = orc::V3<T>(hw, hw, C.F.top);
-    if (gd && gd->data) {
-        PT.grid = (const uint16_t*)gd->data;
-        PT.nx = gd->nx; PT.ny = gd->ny; PT.nz = gd->nz;
-        PT.origin = orc::V3<T>(T(gd->origin[0]), T(gd->origin[1]), T(gd->origin[2]));
-        PT.voxel = T(gd->voxel_size);
-        PT.density = T(gd->density);
-        PT.maj = gd->majorant;
-        PT.brick = gd->brick;
-        PT.bx = (gd->nx + gd->brick - 1) / gd->brick;
-        PT.by = (gd->ny + gd->brick - 1) / gd->brick;
-        PT.bz = (gd->nz + gd->brick - 1) / gd->brick;
-        orc::V3<T> gmax = PT.origin + orc::V3<T>(T(gd->nx), T(gd->ny), T(gd->nz)) * PT.voxel;
-        for (int a = 0; a < 3; ++a) {
-            PT.box_min[a] = std::max(PT.box_min[a], PT.origin[a]);
-            PT.box_max[a] = std::min(PT.box_max[a], gmax[a]);
+struct PtWorld {
+    orc::AtmosphereOracle<T> O;
+    orc::Image<T> tl, sl, st, al, at;
+    orc::CloudOracle<T> C;
+    orc::ViewLutOracle<T> V;
+    orc::PathTracerOracle<T> PT;
+
+    PtWorld(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp, const skyr_cloud_material* m,
+            const skyr_cloud_textures* tx, const skyr_density_grid* gd, const skyr_pathtrace_parameters* pt,
+            const skyr_cloud_view* v, const skyr_atmosphere_render_parameters* ev, const skyr_lut_sizes* s,
+            const double* tlut_in, const double* svl_in, const double* svt_in, const double* apl_in,
+            const double* apt_in)
+        : O{orc::derive_atmosphere<T>(*atmo)},
+          tl(image_from<T>(tlut_in, s->transmittance_width, s->transmittance_height)),
+          sl(svl_in ? image_from<T>(svl_in, s->sky_view_width, s->sky_view_height) : orc::Image<T>{}),
+          st(svt_in ? image_from<T>(svt_in, s->sky_view_width, s->sky_view_height) : orc::Image<T>{}),
+          al(image_from<T>(apl_in, s->aerial_perspective_width, s->aerial_perspective_height,
+                           s->aerial_perspective_depth)),
+          at(image_from<T>(apt_in, s->aerial_perspective_width, s->aerial_perspective_height,
+                           s->aerial_perspective_depth)),
+          C{O, orc::derive_cloud_frame<T>(*atmo, *cp, *m, *tx, *v), {}, {}, {}, {}, nullptr, nullptr, nullptr, nullptr},
+          V{O, orc::derive_render_frame<T>(*atmo, *ev)},
+          PT{O, C, V, &sl, &st, *pt} {
+        auto set = [](orc::Tex8& t, const void* p, const skyr_noise_texture_desc& d, bool border) {
+            t.data = (const uint8_t*)p;
+            t.w = d.width; t.h = d.height; t.d = d.depth; t.channels = d.channels;
+            t.border = border;
+            t.init();
+        };
+        if (tx->cloud_map) set(C.cloud_map, tx->cloud_map, tx->cloud_map_desc, false);
+        if (tx->detail) set(C.detail, tx->detail, tx->detail_desc, false);
+        if (tx->displacement) set(C.displacement, tx->displacement, tx->displacement_desc, false);
+        if (tx->voxel) set(C.voxel, tx->voxel, tx->voxel_desc, true);
+        C.tlut = &tl;
+        C.ap_lum = &al;
+        C.ap_trans = &at;
+        // box: the flat AABB [-w, w]^2 x [bottom, top], clipped to the grid
+        T hw = T(pt->region_box_half_width);
+        PT.box_min = orc::V3<T>(-hw, -hw, C.F.bottom);
+        PT.box_max = orc::V3<T>(hw, hw, C.F.top);
+        if (gd && gd->data) {
+            PT.grid = (const uint16_t*)gd->data;
+            PT.nx = gd->nx; PT.ny = gd->ny; PT.nz = gd->nz;
+            PT.origin = orc::V3<T>(T(gd->origin[0]), T(gd->origin[1]), T(gd->origin[2]));
+            PT.voxel = T(gd->voxel_size);
+            PT.density = T(gd->density);
+            PT.maj = gd->majorant;
+            PT.brick = gd->brick;
+            PT.bx = (gd->nx + gd->brick - 1) / gd->brick;
+            PT.by = (gd->ny + gd->brick - 1) / gd->brick;
+            PT.bz = (gd->nz + gd->brick - 1) / gd->brick;
+            orc::V3<T> gmax = PT.origin + orc::V3<T>(T(gd->nx), T(gd->ny), T(gd->nz)) * PT.voxel;
+            for (int a = 0; a < 3; ++a) {
+                PT.box_min[a] = std::max(PT.box_min[a], PT.origin[a]);
+                PT.box_max[a] = std::min(PT.box_max[a], gmax[a]);
+            }
         }
-    }
-    // kModelMatrix3: columns front, right, up of VolumetricCloud::Update (VolumetricCloud.cpp:188-200)
-    {
+        // kModelMatrix3: columns front, right, up of VolumetricCloud::Update (VolumetricCloud.cpp:188-200)
         T R = T(atmo->bottom_radius);
         orc::V3<T> center(T(0), -R, T(0));
         orc::V3<T> up = orc::normalize(orc::v3f<T>(v->camera_position) - center);
@@ -378,6 +387,19 @@ int pathtrace_t(const skyr_atmosphere_parameters* atmo, const skyr_cloud_paramet
         }
         PT.model3(3, 3) = T(1);
     }
+};
+
+template <class T>
+int pathtrace_t(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                const skyr_cloud_material* m, const skyr_cloud_textures* tx, const skyr_density_grid* gd,
+                const skyr_pathtrace_parameters* pt, const skyr_cloud_view* v,
+                const skyr_atmosphere_render_parameters* ev, const skyr_lut_sizes* s, const double* tlut_in,
+                const double* svl_in, const double* svt_in, const double* apl_in, const double* apt_in,
+                unsigned frame_begin, int n_frames, const int* pixels, int n_pixels, int threads, double* sum,
+                double* sumsq) {
+    auto W = std::make_unique<PtWorld<T>>(atmo, cp, m, tx, gd, pt, v, ev, s, tlut_in, svl_in, svt_in, apl_in,
+                                          apt_in);
+    const orc::PathTracerOracle<T>& PT = W->PT;
     parallel_for(n_pixels, threads, [&](int i) {
         int p = pixels ? pixels[i] : i;
         int px = p % v->width, py = p / v->width;
@@ -453,5 +475,182 @@ void oracle_mlp_adam(double* p, double* m, double* v, const double* g, int n, do
 }
 
 int oracle_mlp_param_count(void) { return orc::kMlpParams; }
+
+}  // extern "C"
+
+
+// ---------------------------------------------------------------------------
+// surrogate: grid lookups, point-source paths, the surrogate raymarch
+// ---------------------------------------------------------------------------
+namespace {
+
+skyr_cloud_material minimal_material() {
+    skyr_cloud_material m{};
+    m.type = SKYR_MATERIAL_MINIMAL;
+    m.density = 1.f;
+    return m;
+}
+
+inline uint32_t pcg(uint32_t v) { return orc::PCGHash(v); }
+
+inline float bf16_of(double x) { return orc::bf16_round((float)x); }
+
+}  // namespace
+
+extern "C" {
+
+// trilinear extinction of the grid at points[n][3]
+int oracle_grid_sigma(const skyr_density_grid* gd, const double* points, int n, double* out) {
+    orc::V3<double> o(gd->origin[0], gd->origin[1], gd->origin[2]);
+    for (int i = 0; i < n; ++i) {
+        orc::V3<double> p(points[3 * i], points[3 * i + 1], points[3 * i + 2]);
+        out[i] = orc::grid_trilinear<double>((const uint16_t*)gd->data, gd->nx, gd->ny, gd->nz, o,
+                                             (double)gd->voxel_size, (double)gd->density, p);
+    }
+    return 0;
+}
+
+// sum over paths k in [0, n_paths) of the point-source radiance of points[n][6]
+int oracle_point_radiance(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                          const skyr_density_grid* gd, const skyr_pathtrace_parameters* pt, const skyr_cloud_view* v,
+                          const skyr_atmosphere_render_parameters* ev, const skyr_lut_sizes* s, const double* tlut,
+                          const double* svl, const double* svt, const double* apl, const double* apt,
+                          unsigned frame_begin, int n_paths, const double* points, int n, int threads, double* sum,
+                          double* sumsq) {
+    skyr_cloud_material m = minimal_material();
+    skyr_cloud_textures tx{};
+    auto W = std::make_unique<PtWorld<double>>(atmo, cp, &m, &tx, gd, pt, v, ev, s, tlut, svl, svt, apl, apt);
+    parallel_for(n, threads, [&](int i) {
+        const double* q = points + 6 * (size_t)i;
+        orc::V3<double> p(q[0], q[1], q[2]), w(q[3], q[4], q[5]);
+        double a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+        for (int k = 0; k < n_paths; ++k) {
+            orc::V3<double> L = W->PT.PointPath((uint32_t)i, frame_begin + (unsigned)k, p, w);
+            for (int c = 0; c < 3; ++c) {
+                a[c] += L[c];
+                b[c] += L[c] * L[c];
+            }
+        }
+        for (int c = 0; c < 3; ++c) {
+            sum[3 * (size_t)i + c] = a[c];
+            sumsq[3 * (size_t)i + c] = b[c];
+        }
+    });
+    return 0;
+}
+
+// The surrogate raymarch of skyr_surrogate_render for listed pixels, in FP64
+// over the GPU-built feature lattice (records bf16 [nodes][48] then sun
+// optical depth f32 [nodes]); the network is oracle_mlp.hpp with the BF16
+// rounding points mirrored.  out[n][4] = (luminance rgb, transmittance),
+// err[n] = the error estimate with a single relative error `rel_err`.
+int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                            const skyr_density_grid* gd, const skyr_pathtrace_parameters* pt,
+                            const skyr_cloud_view* v, const skyr_lut_sizes* s, const double* tlut,
+                            const double* apl, const double* apt, const uint16_t* lattice_rec,
+                            const float* lattice_tau, const skyr_feature_volume* fv, const float* params,
+                            double out_scale, int steps, int use_network, double min_t, double rel_err,
+                            const int* pixels, int n, int threads, double* out, double* err) {
+    skyr_cloud_material m = minimal_material();
+    skyr_cloud_textures tx{};
+    skyr_atmosphere_render_parameters ev{};
+    ev.sun_direction_theta = v->sun_direction_theta;
+    ev.sun_direction_phi = v->sun_direction_phi;
+    std::memcpy(ev.camera_position, v->camera_position, sizeof(ev.camera_position));
+    std::memcpy(ev.view_projection, v->view_projection, sizeof(ev.view_projection));
+    ev.sky_view_lut_steps = 1;
+    ev.aerial_perspective_lut_steps = 1;
+    ev.aerial_perspective_lut_max_distance = v->aerial_perspective_lut_max_distance;
+    auto W = std::make_unique<PtWorld<double>>(atmo, cp, &m, &tx, gd, pt, v, &ev, s, tlut, nullptr, nullptr, apl, apt);
+    const orc::PathTracerOracle<double>& PT = W->PT;
+    const auto& F = W->C.F;
+    orc::MlpOracle net(params, true);
+    const double cell = (double)gd->voxel_size * fv->stride;
+    const orc::V3<double> og(gd->origin[0], gd->origin[1], gd->origin[2]);
+    const orc::V3<double> sun(fv->sun[0], fv->sun[1], fv->sun[2]);
+    auto lattice = [&](orc::V3<double> x, double f[42], double& tau) {
+        orc::V3<double> g = (x - og) / cell;
+        int i0[3];
+        double fr[3];
+        int nn[3] = {fv->nx, fv->ny, fv->nz};
+        for (int a = 0; a < 3; ++a) {
+            i0[a] = std::min(std::max((int)std::floor(g[a]), 0), nn[a] - 2);
+            fr[a] = std::min(std::max(g[a] - i0[a], 0.0), 1.0);
+        }
+        for (int k = 0; k < 42; ++k) f[k] = 0.0;
+        tau = 0.0;
+        for (int c = 0; c < 8; ++c) {
+            int d[3] = {c & 1, (c >> 1) & 1, c >> 2};
+            double w = 1.0;
+            for (int a = 0; a < 3; ++a) w *= d[a] ? fr[a] : 1.0 - fr[a];
+            size_t node = ((size_t)(i0[2] + d[2]) * fv->ny + (i0[1] + d[1])) * fv->nx + (i0[0] + d[0]);
+            tau += w * lattice_tau[node];
+            for (int k = 0; k < 42; ++k) f[k] += w * orc::bf16_to_float(lattice_rec[node * 48 + k]);
+        }
+    };
+    const double gb = pt->back_phase_g, gf = pt->forward_phase_g, ratio = pt->forward_scattering_ratio;
+    auto hg = [](double c, double g) { return (0.25 / orc::kPi) * (1 - g * g) / std::pow(1 + g * g - 2 * g * c, 1.5); };
+    parallel_for(n, threads, [&](int i) {
+        int pix = pixels[i];
+        int px = pix % v->width, py = pix / v->width;
+        double u = (px + 0.5) / v->width, vv = (py + 0.5) / v->height;
+        orc::V3<double> frag = orc::projective_mul(F.inv_mvp, orc::V3<double>(u * 2 - 1, vv * 2 - 1, 1.0));
+        orc::V3<double> dir = orc::normalize(frag - F.cam);
+        double t0, t1;
+        PT.region(F.cam, dir, t0, t1);
+        double T = 1, errs = 0, wsum = 0, wt = 0;
+        orc::V3<double> L(0.0);
+        if (t0 < t1) {
+            double dt = (t1 - t0) / steps;
+            uint32_t js = pcg((uint32_t)(py * v->width + px) * 747796405u + 2891336453u);
+            double jitter = (double)(js >> 8) / 16777216.0;
+            double mu = orc::dot(dir, sun);
+            double ph = hg(mu, gb) * (1 - ratio) + hg(mu, gf) * ratio;
+            for (int k = 0; k < steps && T > min_t; ++k) {
+                double t = t0 + (k + jitter) * dt;
+                orc::V3<double> x = F.cam + dir * t;
+                double sigma = PT.grid_sigma(x);
+                if (!(sigma > 0)) continue;
+                double f[42], tau;
+                lattice(x, f, tau);
+                orc::V3<double> ms(0.0);
+                if (use_network) {
+                    double rec[43], y[3];
+                    for (int q = 0; q < 42; ++q) rec[q] = bf16_of(f[q]);
+                    rec[42] = bf16_of(mu);
+                    net.predict(rec, y);
+                    for (int c = 0; c < 3; ++c) ms[c] = std::max(y[c] * (double)(float)out_scale, 0.0);
+                }
+                orc::V3<double> ss = PT.sun_illuminance(x) * (ph * std::exp(-tau));
+                double dT = std::exp(-sigma * dt), w = T * (1 - dT);
+                L = L + (ss + ms) * w;
+                errs += w * (ms[0] + ms[1] + ms[2]) / 3.0 * rel_err;
+                wsum += w;
+                wt += w * t;
+                T *= dT;
+            }
+        }
+        if (wsum > 0) {
+            double ta = wt / wsum;
+            double r = F.cam.z + F.R, mu = dir.z;
+            if (r > W->O.A.top_radius) {
+                double disc = r * r * (mu * mu - 1) + W->O.A.top_radius * W->O.A.top_radius;
+                if (mu < 0 && disc >= 0) ta -= std::max(-r * mu - std::sqrt(std::max(disc, 0.0)), 0.0);
+                else ta = 0;
+            }
+            double wz = std::sqrt(std::max(ta, 0.0) / F.ap_max_distance);
+            const orc::Image<double>& al = *W->C.ap_lum;
+            double uu = 0.5 / al.w + u * (1 - 1.0 / al.w), vq = 0.5 / al.h + vv * (1 - 1.0 / al.h),
+                   ww = 0.5 / al.d + wz * (1 - 1.0 / al.d);
+            orc::V3<double> at = orc::sample_linear_clamp3(*W->C.ap_trans, uu, vq, ww);
+            orc::V3<double> alum = orc::sample_linear_clamp3(al, uu, vq, ww);
+            L = L * at + alum * (1 - T);
+        }
+        for (int c = 0; c < 3; ++c) out[4 * (size_t)i + c] = L[c];
+        out[4 * (size_t)i + 3] = T;
+        err[i] = errs;
+    });
+    return 0;
+}
 
 }  // extern "C"

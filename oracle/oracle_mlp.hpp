@@ -45,6 +45,12 @@ inline float bf16_round(float x) {
     std::memcpy(&r, &u, 4);
     return r;
 }
+inline double bf16_to_float(uint16_t h) {
+    uint32_t u = (uint32_t)h << 16;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
 inline double bfr(double x, bool mirror) { return mirror ? (double)bf16_round((float)x) : x; }
 
 struct MlpOracle {

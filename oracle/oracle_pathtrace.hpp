@@ -62,6 +62,26 @@ T grid_value(const skyr_grid_generator& g, int x, int y, int z) {
 // ends (free flight: no collision) when it is reached.
 constexpr int kMaxTrackingSteps = 1 << 20;
 
+// Trilinear extinction of a dense FP16 grid between voxel centres, zero border
+// (the voxel material's CLAMP_TO_BORDER sampler, VolumetricCloudVoxelMaterial.cpp:25-31)
+template <class T>
+T grid_trilinear(const uint16_t* g, int nx, int ny, int nz, V3<T> origin, T voxel, T density, V3<T> p) {
+    auto at = [&](int x, int y, int z) -> T {
+        if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) return T(0);
+        return T(half_to_float(g[((size_t)z * ny + y) * nx + x]));
+    };
+    V3<T> q = (p - origin) / voxel - V3<T>(T(0.5));
+    T fx = std::floor(q.x), fy = std::floor(q.y), fz = std::floor(q.z);
+    T a = q.x - fx, b = q.y - fy, c = q.z - fz;
+    int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
+    T r = 0;
+    for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx)
+                r += (dx ? a : T(1) - a) * (dy ? b : T(1) - b) * (dz ? c : T(1) - c) * at(x0 + dx, y0 + dy, z0 + dz);
+    return r * density;
+}
+
 template <class T>
 struct PathTracerOracle {
     const AtmosphereOracle<T>& O;
@@ -94,19 +114,7 @@ struct PathTracerOracle {
         return T(half_to_float(grid[((size_t)z * ny + y) * nx + x]));
     }
 
-    T grid_sigma(V3<T> p) const {
-        V3<T> g = (p - origin) / voxel - V3<T>(T(0.5));
-        T fx = std::floor(g.x), fy = std::floor(g.y), fz = std::floor(g.z);
-        T a = g.x - fx, b = g.y - fy, c = g.z - fz;
-        int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
-        T r = 0;
-        for (int dz = 0; dz < 2; ++dz)
-            for (int dy = 0; dy < 2; ++dy)
-                for (int dx = 0; dx < 2; ++dx)
-                    r += (dx ? a : T(1) - a) * (dy ? b : T(1) - b) * (dz ? c : T(1) - c) *
-                         voxel_at(x0 + dx, y0 + dy, z0 + dz);
-        return r * density;
-    }
+    T grid_sigma(V3<T> p) const { return grid_trilinear<T>(grid, nx, ny, nz, origin, voxel, density, p); }
 
     // SampleSigmaT(vec3 P) (PathTracing.comp:89-91): flat height01
     T SampleSigmaT(V3<T> p) const {
@@ -294,21 +302,31 @@ struct PathTracerOracle {
         return V3<T>(std::cos(phi) * s, std::sin(phi) * s, c);
     }
 
-    // Trace (PathTracing.comp:160-249); returns (L, a)
-    void Trace(uint32_t& seed, V3<T> view, V3<T>& L_out, T& a_out, bool& has_scattered, T& scattered_t) const {
-        V3<T> L(T(0)), thr(T(1));
-        has_scattered = false;
-        scattered_t = T(0);
-        V3<T> o = Cl.F.cam, d = view;
-        T c0, c1;
-        region(o, d, c0, c1);
-        if (c0 >= c1) {
-            L_out = L;
-            a_out = thr.x;  // vec4(L, throughput) takes throughput.x
-            return;
+    // GenerateHGSample (PathTracing.comp:98-117) about d, or a uniform direction
+    // weighted by the phase function
+    void scatter_direction(uint32_t& seed, V3<T>& d, V3<T>& thr) const {
+        if (P.importance_sampling) {
+            T g = rand(seed) < T(P.forward_scattering_ratio) ? T(P.forward_phase_g) : T(P.back_phase_g);
+            T xi = rand(seed);
+            T opg = T(1) + g * g, omg = T(1) - g * g, o2g = T(0.5) / g;
+            T tt = omg / (T(1) - g + T(2) * g * xi);
+            T ct = o2g * (opg - tt * tt);
+            T st = std::sqrt(clampg(T(1) - ct * ct, T(0), T(1)));
+            V3<T> b0, b1;
+            basis(d, b0, b1);
+            T phi = T(2) * T(kPi) * rand(seed);
+            d = b0 * (st * std::sin(phi)) + b1 * (st * std::cos(phi)) + d * ct;
+        } else {
+            V3<T> nd = uniform_sphere(seed);
+            T val = GetPhase(dot(d, nd));
+            thr *= val * T(4) * T(kPi);
+            d = nd;
         }
-        o = o + d * c0;
-        int istep = 0;
+    }
+
+    // The bounce loop of Trace (PathTracing.comp:180-247) from state (o, d, thr, istep)
+    void trace_from(uint32_t& seed, V3<T> o, V3<T> d, V3<T> thr, int istep, V3<T>& L, bool& has_scattered,
+                    T& scattered_t) const {
         const int env = P.environment_lighting;
         while (istep < P.max_bounces && std::max(thr.x, std::max(thr.y, thr.z)) > T(0)) {
             T t0, t1;
@@ -351,29 +369,42 @@ struct PathTracerOracle {
                 o = o + d * t;
                 T ph = GetPhase(dot(d, Cl.F.sun));
                 L += thr * (sun_illuminance(o) * ph * TransmittanceEstimation(seed, o, Cl.F.sun));
-                // GenerateHGSample (PathTracing.comp:98-117)
-                if (P.importance_sampling) {
-                    T g = rand(seed) < T(P.forward_scattering_ratio) ? T(P.forward_phase_g) : T(P.back_phase_g);
-                    T xi = rand(seed);
-                    T opg = T(1) + g * g, omg = T(1) - g * g, o2g = T(0.5) / g;
-                    T tt = omg / (T(1) - g + T(2) * g * xi);
-                    T ct = o2g * (opg - tt * tt);
-                    T st = std::sqrt(clampg(T(1) - ct * ct, T(0), T(1)));
-                    V3<T> b0, b1;
-                    basis(d, b0, b1);
-                    T phi = T(2) * T(kPi) * rand(seed);
-                    d = b0 * (st * std::sin(phi)) + b1 * (st * std::cos(phi)) + d * ct;
-                } else {
-                    V3<T> nd = uniform_sphere(seed);
-                    T val = GetPhase(dot(d, nd));
-                    thr *= val * T(4) * T(kPi);
-                    d = nd;
-                }
+                scatter_direction(seed, d, thr);
             }
             ++istep;
         }
+    }
+
+    // Trace (PathTracing.comp:160-249); returns (L, a)
+    void Trace(uint32_t& seed, V3<T> view, V3<T>& L_out, T& a_out, bool& has_scattered, T& scattered_t) const {
+        V3<T> L(T(0)), thr(T(1));
+        has_scattered = false;
+        scattered_t = T(0);
+        V3<T> o = Cl.F.cam, d = view;
+        T c0, c1;
+        region(o, d, c0, c1);
+        if (c0 >= c1) {
+            L_out = L;
+            a_out = thr.x;  // vec4(L, throughput) takes throughput.x
+            return;
+        }
+        o = o + d * c0;
+        trace_from(seed, o, d, thr, 0, L, has_scattered, scattered_t);
         L_out = L;
         a_out = has_scattered ? T(0) : T(1);
+    }
+
+    // Point source (skyr_pathtrace_points): a path that has just scattered at p
+    // while travelling along w; its radiance (no aerial perspective)
+    V3<T> PointPath(uint32_t i, uint32_t frame, V3<T> p, V3<T> w) const {
+        uint32_t seed = prng(prng(prng(i) + 0x2545F491u) + frame);
+        V3<T> d = w, thr(T(1)), L(T(0));
+        scatter_direction(seed, d, thr);
+        if (P.max_bounces <= 1) return L;
+        bool sc = true;
+        T st = T(0);
+        trace_from(seed, p, d, thr, 1, L, sc, st);
+        return L;
     }
 
     // main (PathTracing.comp:255-284) for one frame of one pixel

@@ -305,6 +305,15 @@ _SIGNATURES.update({
                                  C.POINTER(AtmosphereRenderParameters), C.POINTER(LutSizes), P, P, P, P, P,
                                  C.c_uint, C.c_int, P, P, P]),
     "skyr_pathtrace_resolve": (C.c_int, [P, P, C.c_int, C.c_int, C.c_uint, P, P]),
+    "skyr_pathtrace_pixels": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                        C.POINTER(CloudMaterial), C.POINTER(CloudTextures), C.POINTER(DensityGrid),
+                                        C.POINTER(PathtraceParameters), C.POINTER(CloudView),
+                                        C.POINTER(AtmosphereRenderParameters), C.POINTER(LutSizes), P, P, P, P, P,
+                                        C.c_uint, C.c_int, P, C.c_int, P, P]),
+    "skyr_pathtrace_points": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                        C.POINTER(DensityGrid), C.POINTER(PathtraceParameters), C.POINTER(CloudView),
+                                        C.POINTER(AtmosphereRenderParameters), C.POINTER(LutSizes), P, P, P, P, P,
+                                        C.c_uint, C.c_int, P, C.c_int, P]),
 })
 
 
@@ -336,4 +345,38 @@ _SIGNATURES.update({
     "skyr_mlp_trainer_steps": (C.c_int, [P]),
     "skyr_mlp_trainer_copy_params": (C.c_int, [P, P]),
     "skyr_mlp_trainer_copy_packed": (C.c_int, [P, P]),
+    "skyr_mlp_trainer_set_learning_rate": (C.c_int, [P, C.c_float]),
+})
+
+
+# ---------------------------------------------------------------------------
+# skyr_surrogate.h
+# ---------------------------------------------------------------------------
+class FeatureVolume(C.Structure):
+    _fields_ = [("data", P), ("stride", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("sigma_ref", C.c_float), ("sun", C.c_float * 3)]
+
+
+class SurrogateParameters(C.Structure):
+    _fields_ = [("steps", C.c_int), ("use_network", C.c_int), ("network_error", C.c_float),
+                ("min_transmittance", C.c_float), ("error_table", P)]
+
+
+SKYR_SURROGATE_ERROR_BINS = 8
+
+
+STRUCT_IDS.update({12: FeatureVolume, 13: SurrogateParameters})
+_SIGNATURES.update({
+    "skyr_surrogate_parameters_default": (C.c_int, [C.POINTER(SurrogateParameters)]),
+    "skyr_feature_volume_bytes": (C.c_size_t, [C.POINTER(DensityGrid), C.c_int, C.POINTER(FeatureVolume)]),
+    "skyr_feature_volume_build": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                            C.POINTER(DensityGrid), C.POINTER(CloudView), C.POINTER(FeatureVolume)]),
+    "skyr_surrogate_sample_points": (C.c_int, [P, C.POINTER(DensityGrid), C.c_float, C.c_float, C.c_uint64, C.c_int,
+                                               P]),
+    "skyr_surrogate_records": (C.c_int, [P, C.POINTER(DensityGrid), C.POINTER(FeatureVolume), P, C.c_int, P]),
+    "skyr_surrogate_error_bins": (C.c_int, [P, P, C.c_int, P]),
+    "skyr_surrogate_render": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                        C.POINTER(DensityGrid), C.POINTER(PathtraceParameters), C.POINTER(CloudView),
+                                        C.POINTER(LutSizes), P, P, P, C.POINTER(FeatureVolume), P,
+                                        C.POINTER(SurrogateParameters), P, P]),
 })

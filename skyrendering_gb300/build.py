@@ -42,7 +42,7 @@ def _flags(extra: list[str] | None = None) -> list[str]:
 def _needs(obj: Path, src: Path) -> bool:
     if not obj.exists():
         return True
-    deps = [src] + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "skyr.h"]
+    deps = [src] + list(CSRC.glob("*.cuh")) + list((PKG.parent / "include").glob("*.h"))
     t = obj.stat().st_mtime
     return any(d.stat().st_mtime > t for d in deps if d.exists())
 

@@ -584,6 +584,13 @@ const float* skyr_mlp_trainer_params(const skyr_mlp_trainer* tr) { return tr ? t
 const void* skyr_mlp_trainer_packed(const skyr_mlp_trainer* tr) { return tr ? tr->packed : nullptr; }
 int skyr_mlp_trainer_steps(const skyr_mlp_trainer* tr) { return tr ? tr->steps : -1; }
 
+int skyr_mlp_trainer_set_learning_rate(skyr_mlp_trainer* tr, float learning_rate) {
+    if (!tr) return set_error(SKYR_EINVAL, "null trainer");
+    if (!(learning_rate > 0.f) || !std::isfinite(learning_rate)) return set_error(SKYR_EINVAL, "bad learning rate");
+    tr->h.learning_rate = learning_rate;
+    return SKYR_OK;
+}
+
 int skyr_mlp_trainer_copy_params(const skyr_mlp_trainer* tr, float* out) {
     if (!tr || !out) return set_error(SKYR_EINVAL, "null argument");
     if (int e = check_cuda(cudaSetDevice(tr->ctx->device), "cudaSetDevice")) return e;

@@ -2,10 +2,11 @@
 // (VolumetricCloudPathTracing.comp) for sm_103a, the synthetic dense FP16
 // density grid and its 16^3-brick majorant grid.
 //
-// One thread traces the paths of one pixel for every requested frame.  The
-// path logic follows the reference (delta tracking, ratio-tracking next-event
-// estimation with a copied RNG context, HG importance sampling, the Lambert
-// ground bounce, the environment on escape).  Two GB300-side changes:
+// A persistent kernel traces one path per (frame, pixel) work item with path
+// regeneration.  The path logic follows the reference (delta tracking,
+// ratio-tracking next-event estimation with a copied RNG context, HG importance
+// sampling, the Lambert ground bounce, the environment on escape).  Two
+// GB300-side changes:
 //  * a dense FP16 grid with per-brick majorants walked by a 3D DDA replaces the
 //    single global majorant where the caller supplies them, so empty and thin
 //    regions cost few samples;
@@ -21,75 +22,9 @@
 #include "lut_access.cuh"
 #include "noise_device.cuh"
 #include "skyr_ctx.cuh"
+#include "voxel_device.cuh"
 
 namespace skyr {
-
-// Upper bound on the samples of one free-flight / ratio-tracking walk.  A valid
-// scene needs ~sigma_max x chord samples (tens to hundreds); the cap only
-// stops pathological inputs, ends the path and raises the status flag.
-constexpr int kMaxTrackingSteps = 1 << 20;
-
-struct PtConsts {
-    float3 box_min, box_max;
-    int max_bounces, importance_sampling, prng, env;
-    float g_fwd, g_back, ratio, sigma_t_max;
-    int use_bricks;
-    // dense grid
-    const unsigned short* grid;
-    int nx, ny, nz;
-    float3 origin;
-    float inv_voxel, density;
-    const float* maj;
-    int bx, by, bz;
-    float brick_size;
-    // local -> world directions (kModelMatrix3 columns)
-    float3 m_front, m_right, m_up;
-    int sv_w, sv_h;
-    int width, height;
-    int x0, y0, x1, y1;
-    int tiles_x, n_items;  // work items of one frame (8x4 pixel tiles x 32)
-    int* status;  // bit 0: a tracking walk hit kMaxTrackingSteps
-};
-
-__device__ __forceinline__ void flag_overrun(const PtConsts& P) {
-    if (P.status) atomicOr(P.status, 1);
-}
-
-__device__ __forceinline__ uint32_t pt_prng(const PtConsts& P, uint32_t s) {
-    return P.prng == SKYR_PRNG_WANG_HASH ? wang_hash(s) : pcg_hash(s);
-}
-
-// Random01 (PathTracing.comp:44-48): float(seed) / 2^32
-__device__ __forceinline__ float rand01(const PtConsts& P, uint32_t& seed) {
-    float r = (float)seed * 2.3283064365386963e-10f;
-    seed = pt_prng(P, seed);
-    return r;
-}
-
-__device__ __forceinline__ float grid_voxel(const PtConsts& P, int x, int y, int z) {
-    if ((unsigned)x >= (unsigned)P.nx || (unsigned)y >= (unsigned)P.ny || (unsigned)z >= (unsigned)P.nz) return 0.f;
-    unsigned short h = __ldg(P.grid + ((size_t)z * P.ny + y) * P.nx + x);
-    return __half2float(__ushort_as_half(h));
-}
-
-// trilinear between voxel centres, zero border
-__device__ __forceinline__ float grid_sigma(const PtConsts& P, float3 p) {
-    float gx = (p.x - P.origin.x) * P.inv_voxel - 0.5f;
-    float gy = (p.y - P.origin.y) * P.inv_voxel - 0.5f;
-    float gz = (p.z - P.origin.z) * P.inv_voxel - 0.5f;
-    float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
-    float a = gx - fx, b = gy - fy, c = gz - fz;
-    int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
-    float r[2];
-#pragma unroll
-    for (int dz = 0; dz < 2; ++dz) {
-        float t00 = grid_voxel(P, x0, y0, z0 + dz), t10 = grid_voxel(P, x0 + 1, y0, z0 + dz);
-        float t01 = grid_voxel(P, x0, y0 + 1, z0 + dz), t11 = grid_voxel(P, x0 + 1, y0 + 1, z0 + dz);
-        float top = fmaf(a, t10 - t00, t00), bot = fmaf(a, t11 - t01, t01);
-        r[dz] = fmaf(b, bot - top, top);
-    }
-    return fmaf(c, r[1] - r[0], r[0]) * P.density;
-}
 
 // The material plug-ins' SampleSigmaT with the path tracer's flat height01.
 // Kept out of line: it holds every material's texture sampling, and the dense
@@ -105,16 +40,6 @@ __device__ __forceinline__ float pt_sigma(const PtConsts& P, const CloudConsts& 
                                           float3 p) {
     if (P.grid) return grid_sigma(P, p);
     return material_sigma(C, M, p);
-}
-
-// CloudRegionIntersect (PathTracing.comp:57-75)
-__device__ __forceinline__ void region(const PtConsts& P, float3 o, float3 d, float& t0, float& t1) {
-    float3 inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
-    float ax = (P.box_min.x - o.x) * inv.x, bx = (P.box_max.x - o.x) * inv.x;
-    float ay = (P.box_min.y - o.y) * inv.y, by = (P.box_max.y - o.y) * inv.y;
-    float az = (P.box_min.z - o.z) * inv.z, bz = (P.box_max.z - o.z) * inv.z;
-    t0 = fmaxf(0.f, fmaxf(fminf(ax, bx), fmaxf(fminf(ay, by), fminf(az, bz))));
-    t1 = fminf(1e7f, fminf(fmaxf(ax, bx), fminf(fmaxf(ay, by), fmaxf(az, bz))));
 }
 
 // 3D DDA over the majorant bricks
@@ -270,18 +195,6 @@ __device__ __forceinline__ float transmittance_estimation(const PtConsts& P, con
     return clamp01(tr);
 }
 
-// GetSunVisibility(transmittance_texture, pos) x solar_illuminance, local frame
-__device__ __forceinline__ float3 sun_illuminance(const CloudConsts& C, const AtmoConsts& A, const float4* tlut,
-                                                  int tw, int th, float3 p) {
-    float rho2 = fmaf(p.x, p.x, fmaf(p.y, p.y, p.z * (p.z + 2.f * C.R)));
-    float r2 = fmaf(C.R, C.R, rho2);
-    float inv_r = rsqrtf(r2);
-    float r = r2 * inv_r;
-    float h = __fdividef(rho2, r + C.R);
-    float mu_s = fmaf(C.sun.x, p.x, fmaf(C.sun.y, p.y, C.sun.z * (p.z + C.R))) * inv_r;
-    return sun_visibility_lut(A, tlut, tw, th, r, rho2, h, mu_s) * A.solar_illuminance;
-}
-
 // ENVIRONMENT_LUMINANCE (AtmosphereRenderer.glsl:250-273) for world direction w:
 // GetCosLatLonFromViewDirection, GetSkyViewTextureUvFromCosLatLon (:113-145),
 // sky-view luminance + ground term x sky-view transmittance.
@@ -310,39 +223,19 @@ __device__ float3 environment(const PtConsts& P, const AtmoConsts& A, const View
     return lum;
 }
 
-__device__ __forceinline__ void onb(float3 n, float3& t0, float3& t1) {  // Common.glsl:45-50
-    float s = n.z >= 0.f ? 1.f : -1.f;
-    float a = -1.f / (s + n.z);
-    float b = n.x * n.y * a;
-    t0 = f3(1.f + s * n.x * n.x * a, s * b, -s * n.x);
-    t1 = f3(b, s + n.y * n.y * a, -n.y);
-}
-
-__device__ __forceinline__ float hg_pt(float c, float g) {
-    float a = 1.f - g * g;
-    float b = fmaf(-2.f * g, c, 1.f + g * g);
-    return (0.25f / SKYR_PI) * a / (b * sqrtf(b));
-}
-
 // Work items of one frame: the region in 8x4 pixel tiles, 32 items per tile
 // (items past the region's right / bottom edge are skipped).
 __device__ __forceinline__ bool item_pixel(const PtConsts& P, int item, int& px, int& py) {
+    if (P.pixel_list) {  // out-of-range entries are skipped
+        int pix = __ldg(P.pixel_list + item);
+        px = pix % P.width;
+        py = pix / P.width;
+        return pix >= 0 && py < P.height;
+    }
     int tile = item >> 5, k = item & 31;
     px = P.x0 + (tile % P.tiles_x) * 8 + (k & 7);
     py = P.y0 + (tile / P.tiles_x) * 4 + (k >> 3);
     return px < P.x1 && py < P.y1;
-}
-
-// Primary ray through the pixel centre at NDC z = 1 (far plane); also the
-// texture coordinates of the pixel for the aerial-perspective lookup.
-__device__ __forceinline__ float3 primary_dir(const CloudConsts& C, const PtConsts& P, int px, int py, float& u,
-                                              float& v) {
-    u = ((float)px + 0.5f) / (float)P.width;
-    v = ((float)py + 0.5f) / (float)P.height;
-    float x = 2.f * u - 1.f, y = 2.f * v - 1.f;
-    float3 dir = C.a0 * x + C.a1 * y + C.af;
-    float wv = fmaf(C.w0, x, fmaf(C.w1, y, C.wf));
-    return dir * (copysignf(1.f, wv) * rsqrtf(dot3(dir, dir)));
 }
 
 // One path of Trace (PathTracing.comp:160-249) in flight on one lane.
@@ -396,6 +289,56 @@ __device__ __forceinline__ bool start_path(const CloudConsts& C, const PtConsts&
     region(P, C.cam, ps.d, c0, c1);
     ps.o = C.cam + ps.d * c0;
     return c0 < c1 && P.max_bounces > 0;
+}
+
+// New direction after a scattering event at ps.o: GenerateHGSample
+// (PathTracing.comp:98-117) with importance sampling, else a uniform sphere
+// direction weighted by the phase function.
+__device__ __forceinline__ void sample_scatter(const PtConsts& P, PathState& ps) {
+    float3 d = ps.d;
+    if (P.importance_sampling) {
+        float g = rand01(P, ps.seed) < P.ratio ? P.g_fwd : P.g_back;
+        float xi = rand01(P, ps.seed);
+        float opg = 1.f + g * g, omg = 1.f - g * g, o2g = 0.5f / g;
+        float tt = omg / (1.f - g + 2.f * g * xi);
+        float ct = o2g * (opg - tt * tt);
+        float st = sqrtf(clamp01(1.f - ct * ct));
+        float3 b0, b1;
+        onb(d, b0, b1);
+        float sp, cp;
+        sincosf(2.f * SKYR_PI * rand01(P, ps.seed), &sp, &cp);
+        ps.d = b0 * (st * sp) + b1 * (st * cp) + d * ct;
+    } else {
+        float phi = 2.f * SKYR_PI * rand01(P, ps.seed);
+        float c = 1.f - 2.f * rand01(P, ps.seed);
+        float s = sqrtf(clamp01(1.f - c * c));
+        float sp, cp;
+        sincosf(phi, &sp, &cp);
+        float3 nd = f3(cp * s, sp * s, c);
+        float cn = dot3(d, nd);
+        float val = hg_pt(cn, P.g_back) * (1.f - P.ratio) + hg_pt(cn, P.g_fwd) * P.ratio;
+        ps.thr = ps.thr * (val * 4.f * SKYR_PI);
+        ps.d = nd;
+    }
+}
+
+// Path of a point source: it starts at points[i] with a direction drawn from
+// the phase function about the point's direction, as if a path travelling
+// along it had just scattered there (that event counts as the first bounce).
+__device__ __forceinline__ bool start_point_path(const PtConsts& P, unsigned frame, int i, PathState& ps) {
+    ps.px = i;
+    ps.py = 0;
+    ps.seed = pt_prng(P, pt_prng(P, pt_prng(P, (uint32_t)i) + 0x2545F491u) + frame);
+    const float* q = P.points + 6 * (size_t)i;
+    ps.o = f3(__ldg(q), __ldg(q + 1), __ldg(q + 2));
+    ps.d = f3(__ldg(q + 3), __ldg(q + 4), __ldg(q + 5));
+    ps.L = f3(0.f);
+    ps.thr = f3(1.f);
+    ps.scattered = true;
+    ps.scattered_t = 0.f;
+    ps.istep = 1;
+    sample_scatter(P, ps);
+    return P.max_bounces > 1;
 }
 
 // One iteration of Trace's bounce loop; false when the path ends.
@@ -454,31 +397,7 @@ __device__ __forceinline__ bool bounce(const CloudConsts& C, const MaterialConst
         float ph = hg_pt(cs, P.g_back) * (1.f - P.ratio) + hg_pt(cs, P.g_fwd) * P.ratio;
         ps.L += ps.thr * (sun_illuminance(C, A, tlut, tw, th, ps.o) *
                           (ph * transmittance_estimation(P, C, M, ps.seed, ps.o, C.sun)));
-        // GenerateHGSample (PathTracing.comp:98-117)
-        if (P.importance_sampling) {
-            float g = rand01(P, ps.seed) < P.ratio ? P.g_fwd : P.g_back;
-            float xi = rand01(P, ps.seed);
-            float opg = 1.f + g * g, omg = 1.f - g * g, o2g = 0.5f / g;
-            float tt = omg / (1.f - g + 2.f * g * xi);
-            float ct = o2g * (opg - tt * tt);
-            float st = sqrtf(clamp01(1.f - ct * ct));
-            float3 b0, b1;
-            onb(d, b0, b1);
-            float sp, cp;
-            sincosf(2.f * SKYR_PI * rand01(P, ps.seed), &sp, &cp);
-            ps.d = b0 * (st * sp) + b1 * (st * cp) + d * ct;
-        } else {
-            float phi = 2.f * SKYR_PI * rand01(P, ps.seed);
-            float c = 1.f - 2.f * rand01(P, ps.seed);
-            float s = sqrtf(clamp01(1.f - c * c));
-            float sp, cp;
-            sincosf(phi, &sp, &cp);
-            float3 nd = f3(cp * s, sp * s, c);
-            float cn = dot3(d, nd);
-            float val = hg_pt(cn, P.g_back) * (1.f - P.ratio) + hg_pt(cn, P.g_fwd) * P.ratio;
-            ps.thr = ps.thr * (val * 4.f * SKYR_PI);
-            ps.d = nd;
-        }
+        sample_scatter(P, ps);
     }
     ++ps.istep;
     return ps.istep < P.max_bounces && fmaxf(ps.thr.x, fmaxf(ps.thr.y, ps.thr.z)) > 0.f;
@@ -497,6 +416,13 @@ constexpr int kWarpChunk = 32;
 template <class S>
 __device__ __forceinline__ void deposit(const CloudConsts& C, const AtmoConsts& A, const PtConsts& P, const S* apl,
                                         const S* apt, const PathState& ps, float4* acc, float4* acc_sq) {
+    if (P.points) {  // point source: the radiance of the path, no aerial perspective
+        float* o = P.point_out + 3 * (size_t)ps.px;
+        atomicAdd(o, ps.L.x);
+        atomicAdd(o + 1, ps.L.y);
+        atomicAdd(o + 2, ps.L.z);
+        return;
+    }
     float4 x = path_sample(C, A, P, apl, apt, ps);
     size_t pix = (size_t)ps.py * P.width + ps.px;
     atomicAdd(acc + pix, x);
@@ -540,7 +466,9 @@ __global__ void __launch_bounds__(128, 4) pathtrace_kernel(CloudConsts C, Materi
             if (!active && rank < take) {
                 int item = chunk_next + rank;
                 int f = item / P.n_items;
-                if (item_pixel(P, item - f * P.n_items, ps.px, ps.py)) {
+                if (P.points) {
+                    active = start_point_path(P, frame_begin + (unsigned)f, item - f * P.n_items, ps);
+                } else if (item_pixel(P, item - f * P.n_items, ps.px, ps.py)) {
                     active = start_path(C, P, frame_begin + (unsigned)f, ps);
                     if (!active) deposit(C, A, P, apl, apt, ps, acc, acc_sq);
                 }
@@ -678,17 +606,32 @@ int skyr_grid_majorants(skyr_ctx* ctx, const skyr_density_grid* gd, float* out) 
     return check_cuda(cudaGetLastError(), "grid majorant kernel");
 }
 
-int skyr_pathtrace(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
-                   const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
-                   const skyr_cloud_textures* textures, const skyr_density_grid* grid,
-                   const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
-                   const skyr_atmosphere_render_parameters* env_view, const skyr_lut_sizes* sizes,
-                   const void* transmittance, const void* sky_view_luminance, const void* sky_view_transmittance,
-                   const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
-                   unsigned frame_begin, int n_frames, const int* region_px, float* accumulation,
-                   float* accumulation_sq) {
-    if (!ctx || !atmosphere || !cloud || !pt || !view || !env_view || !sizes || !accumulation)
+}  // extern "C"
+
+namespace {
+
+// Work source of one launch: the view's region (tiles), a pixel list, or points.
+struct PtSource {
+    const int* region_px = nullptr;  // [x0, y0, x1, y1] or NULL (whole view)
+    const int* pixel_list = nullptr;
+    int n_pixels = 0;
+    const float* points = nullptr;
+    float* point_out = nullptr;
+    int n_points = 0;
+};
+
+int pathtrace_launch(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                     const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                     const skyr_cloud_textures* textures, const skyr_density_grid* grid,
+                     const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
+                     const skyr_atmosphere_render_parameters* env_view, const skyr_lut_sizes* sizes,
+                     const void* transmittance, const void* sky_view_luminance, const void* sky_view_transmittance,
+                     const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
+                     unsigned frame_begin, int n_frames, const PtSource& src, float* accumulation,
+                     float* accumulation_sq) {
+    if (!ctx || !atmosphere || !cloud || !pt || !view || !env_view || !sizes)
         return set_error(SKYR_EINVAL, "null argument");
+    if (!src.points && !accumulation) return set_error(SKYR_EINVAL, "null accumulation buffer");
     if (!transmittance || !sky_view_luminance || !sky_view_transmittance || !aerial_perspective_luminance ||
         !aerial_perspective_transmittance)
         return set_error(SKYR_EINVAL, "null LUT input");
@@ -778,6 +721,7 @@ int skyr_pathtrace(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
     P.sv_h = sizes->sky_view_height;
     P.width = view->width;
     P.height = view->height;
+    const int* region_px = src.region_px;
     if (region_px) {
         P.x0 = std::max(region_px[0], 0);
         P.y0 = std::max(region_px[1], 0);
@@ -788,15 +732,30 @@ int skyr_pathtrace(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
         P.x1 = view->width;
         P.y1 = view->height;
     }
-    if (P.x1 <= P.x0 || P.y1 <= P.y0 || n_frames == 0) return SKYR_OK;
+    long long items;
+    if (src.points) {
+        if (src.n_points < 0) return set_error(SKYR_EINVAL, "negative point count");
+        if (!src.point_out) return set_error(SKYR_EINVAL, "null point output");
+        if (!use_grid) return set_error(SKYR_ENOTSUP, "point sources need a density grid");
+        P.points = src.points;
+        P.point_out = src.point_out;
+        items = src.n_points;
+    } else if (src.pixel_list) {
+        if (src.n_pixels < 0) return set_error(SKYR_EINVAL, "negative pixel count");
+        P.pixel_list = src.pixel_list;
+        items = src.n_pixels;
+    } else {
+        if (P.x1 <= P.x0 || P.y1 <= P.y0) return SKYR_OK;
+        P.tiles_x = (P.x1 - P.x0 + 7) / 8;
+        items = (long long)P.tiles_x * ((P.y1 - P.y0 + 3) / 4) * 32;
+    }
+    if (items == 0 || n_frames == 0) return SKYR_OK;
     if (sizes->sky_view_width < 2 || sizes->sky_view_height < 2) return set_error(SKYR_EINVAL, "bad sky-view size");
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     if (int e = ensure_status(ctx)) return e;
     P.status = ctx->d_status;
-    P.tiles_x = (P.x1 - P.x0 + 7) / 8;
-    long long items = (long long)P.tiles_x * ((P.y1 - P.y0 + 3) / 4) * 32;
     if (items * n_frames > (1LL << 30))
-        return set_error(SKYR_EINVAL, "path tracer region x frames too large for one call (2^30 paths)");
+        return set_error(SKYR_EINVAL, "work items x frames too large for one call (2^30 paths)");
     P.n_items = (int)items;
     // the call's work counter
     if (int e = ensure_pt_scratch(ctx, sizeof(int))) return e;
@@ -824,6 +783,67 @@ int skyr_pathtrace(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
     };
     return sizes->format == SKYR_FORMAT_RGBA16F ? launch(__half2{}) : launch(float4{});
 }
+
+}  // namespace
+
+extern "C" {
+
+int skyr_pathtrace(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                   const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                   const skyr_cloud_textures* textures, const skyr_density_grid* grid,
+                   const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
+                   const skyr_atmosphere_render_parameters* env_view, const skyr_lut_sizes* sizes,
+                   const void* transmittance, const void* sky_view_luminance, const void* sky_view_transmittance,
+                   const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
+                   unsigned frame_begin, int n_frames, const int* region_px, float* accumulation,
+                   float* accumulation_sq) {
+    PtSource src;
+    src.region_px = region_px;
+    return pathtrace_launch(ctx, atmosphere, cloud, material, textures, grid, pt, view, env_view, sizes,
+                            transmittance, sky_view_luminance, sky_view_transmittance,
+                            aerial_perspective_luminance, aerial_perspective_transmittance, frame_begin, n_frames,
+                            src, accumulation, accumulation_sq);
+}
+
+int skyr_pathtrace_pixels(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                          const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                          const skyr_cloud_textures* textures, const skyr_density_grid* grid,
+                          const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
+                          const skyr_atmosphere_render_parameters* env_view, const skyr_lut_sizes* sizes,
+                          const void* transmittance, const void* sky_view_luminance,
+                          const void* sky_view_transmittance, const void* aerial_perspective_luminance,
+                          const void* aerial_perspective_transmittance, unsigned frame_begin, int n_frames,
+                          const int* pixels, int n_pixels, float* accumulation, float* accumulation_sq) {
+    if (n_pixels > 0 && !pixels) return set_error(SKYR_EINVAL, "null pixel list");
+    PtSource src;
+    src.pixel_list = pixels;
+    src.n_pixels = n_pixels;
+    return pathtrace_launch(ctx, atmosphere, cloud, material, textures, grid, pt, view, env_view, sizes,
+                            transmittance, sky_view_luminance, sky_view_transmittance,
+                            aerial_perspective_luminance, aerial_perspective_transmittance, frame_begin, n_frames,
+                            src, accumulation, accumulation_sq);
+}
+
+int skyr_pathtrace_points(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                          const skyr_cloud_parameters* cloud, const skyr_density_grid* grid,
+                          const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
+                          const skyr_atmosphere_render_parameters* env_view, const skyr_lut_sizes* sizes,
+                          const void* transmittance, const void* sky_view_luminance,
+                          const void* sky_view_transmittance, const void* aerial_perspective_luminance,
+                          const void* aerial_perspective_transmittance, unsigned frame_begin, int n_paths,
+                          const float* points, int n_points, float* out) {
+    if (n_points > 0 && (!points || !out)) return set_error(SKYR_EINVAL, "null points or output");
+    if (!grid || !grid->data) return set_error(SKYR_EINVAL, "point sources need a density grid");
+    PtSource src;
+    src.points = points;
+    src.point_out = out;
+    src.n_points = n_points;
+    return pathtrace_launch(ctx, atmosphere, cloud, nullptr, nullptr, grid, pt, view, env_view, sizes,
+                            transmittance, sky_view_luminance, sky_view_transmittance,
+                            aerial_perspective_luminance, aerial_perspective_transmittance, frame_begin, n_paths,
+                            src, nullptr, nullptr);
+}
+
 
 int skyr_pathtrace_resolve(skyr_ctx* ctx, const float* accumulation, int width, int height, unsigned frames,
                            const void* background_rgba16f, void* out_rgba16f) {

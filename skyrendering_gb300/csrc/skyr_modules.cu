@@ -2,6 +2,7 @@
 #include <algorithm>
 
 #include "../../include/skyr_mlp.h"
+#include "../../include/skyr_surrogate.h"
 #include "../../include/skyr_pathtrace.h"
 #include "skyr_ctx.cuh"
 
@@ -72,6 +73,8 @@ size_t skyr_struct_size_ext(int which) {
         case 9: return sizeof(skyr_grid_generator);
         case 10: return sizeof(skyr_pathtrace_parameters);
         case 11: return sizeof(skyr_mlp_hparams);
+        case 12: return sizeof(skyr_feature_volume);
+        case 13: return sizeof(skyr_surrogate_parameters);
         default: return 0;
     }
 }

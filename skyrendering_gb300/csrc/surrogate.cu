@@ -1,0 +1,566 @@
+// surrogate.cu — the surrogate-shaded voxel cloud (include/skyr_surrogate.h):
+// the feature lattice, training points and records, and the 128-step raymarch
+// with the network of mlp_device.cuh evaluated inside the march.
+//
+// The raymarch keeps a warp on an 8x4 pixel tile.  At each step the lanes whose
+// sample lies in the cloud write their feature record (interpolated from the
+// lattice) to the warp's shared-memory tile, and the warp evaluates the network
+// for its 32 samples on the tensor cores (mma.sync BF16, FP32 accumulation);
+// single scattering of the sun uses the lattice's optical depth to the sun.
+#include <cmath>
+#include <cstring>
+
+#include "../../include/skyr_surrogate.h"
+#include "mlp_device.cuh"
+#include "skyr_ctx.cuh"
+#include "voxel_device.cuh"
+
+namespace skyr {
+namespace {
+
+constexpr int kFeat = 42;  // position features per lattice node
+constexpr int kMaxSampleTries = 64;
+constexpr int kMaxTrackSteps = 1 << 16;
+
+struct Lattice {
+    const uint4* rec;  // [nodes][6] (48 bf16)
+    const float* tau;  // [nodes]
+    int nx, ny, nz;
+    float3 origin;
+    float inv_cell;
+    float3 sun;
+};
+
+__device__ __forceinline__ float u01(uint32_t& s) {
+    s = pcg_hash(s);
+    return (float)(s >> 8) * (1.f / 16777216.f);
+}
+
+__device__ __forceinline__ float3 uniform_dir(uint32_t& s) {
+    float c = 1.f - 2.f * u01(s), ph = 2.f * SKYR_PI * u01(s);
+    float r = sqrtf(fmaxf(0.f, 1.f - c * c)), sp, cp;
+    sincosf(ph, &sp, &cp);
+    return f3(r * cp, r * sp, c);
+}
+
+// slab intersection of the ray with [lo, hi]
+__device__ __forceinline__ void box_hit(float3 lo, float3 hi, float3 o, float3 d, float& t0, float& t1) {
+    float3 inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    float ax = (lo.x - o.x) * inv.x, bx = (hi.x - o.x) * inv.x;
+    float ay = (lo.y - o.y) * inv.y, by = (hi.y - o.y) * inv.y;
+    float az = (lo.z - o.z) * inv.z, bz = (hi.z - o.z) * inv.z;
+    t0 = fmaxf(0.f, fmaxf(fminf(ax, bx), fmaxf(fminf(ay, by), fminf(az, bz))));
+    t1 = fminf(fmaxf(ax, bx), fminf(fmaxf(ay, by), fmaxf(az, bz)));
+}
+
+struct GridBox {
+    float3 lo, hi;
+    float span;  // longest edge
+};
+
+// Trilinear interpolation of the lattice at x: the 42 features (when F) and
+// the optical depth to the sun.
+template <bool FEATURES>
+__device__ __forceinline__ float lattice_at(const Lattice& L, float3 x, float (&f)[kFeat]) {
+    float gx = (x.x - L.origin.x) * L.inv_cell, gy = (x.y - L.origin.y) * L.inv_cell,
+          gz = (x.z - L.origin.z) * L.inv_cell;
+    int ix = min(max((int)floorf(gx), 0), L.nx - 2), iy = min(max((int)floorf(gy), 0), L.ny - 2),
+        iz = min(max((int)floorf(gz), 0), L.nz - 2);
+    float fx = fminf(fmaxf(gx - ix, 0.f), 1.f), fy = fminf(fmaxf(gy - iy, 0.f), 1.f),
+          fz = fminf(fmaxf(gz - iz, 0.f), 1.f);
+    if (FEATURES) {
+#pragma unroll
+        for (int i = 0; i < kFeat; ++i) f[i] = 0.f;
+    }
+    float tau = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
+        float w = (dx ? fx : 1.f - fx) * (dy ? fy : 1.f - fy) * (dz ? fz : 1.f - fz);
+        size_t node = ((size_t)(iz + dz) * L.ny + (iy + dy)) * L.nx + (ix + dx);
+        tau = fmaf(w, __ldg(L.tau + node), tau);
+        if (FEATURES) {
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                uint4 v = __ldg(L.rec + node * 6 + q);
+                uint32_t u[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    int i = q * 8 + h * 2;
+                    if (i < kFeat) {
+                        __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&u[h]);
+                        f[i] = fmaf(w, __low2float(b), f[i]);
+                        if (i + 1 < kFeat) f[i + 1] = fmaf(w, __high2float(b), f[i + 1]);
+                    }
+                }
+            }
+        }
+    }
+    return tau;
+}
+
+// record of a sample (features + cos(view, sun)) as 6 x 16 bytes
+__device__ __forceinline__ void store_record(uint4* dst, const float (&f)[kFeat], float mu) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        uint32_t u[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            int i = q * 8 + h * 2;
+            float a = i < kFeat ? f[i] : (i == kFeat ? mu : 0.f);
+            float b = i + 1 < kFeat ? f[i + 1] : (i + 1 == kFeat ? mu : 0.f);
+            u[h] = mlp::pack_bf16(a, b);
+        }
+        dst[q] = make_uint4(u[0], u[1], u[2], u[3]);
+    }
+}
+
+struct LatticeBuild {
+    float dist[32];  // sun sample distances
+    float nbr;       // neighbour radius
+    float inv_sigma_ref;
+    float step;      // sun optical-depth march step
+};
+
+__global__ void __launch_bounds__(128) feature_lattice_kernel(PtConsts P, GridBox B, Lattice L, LatticeBuild Q,
+                                                              int stride, uint4* __restrict__ rec,
+                                                              float* __restrict__ tau) {
+    size_t n = (size_t)L.nx * L.ny * L.nz;
+    size_t node = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= n) return;
+    int ix = (int)(node % L.nx), iy = (int)((node / L.nx) % L.ny), iz = (int)(node / ((size_t)L.nx * L.ny));
+    float cell = 1.f / L.inv_cell;
+    float3 x = f3(L.origin.x + ix * cell, L.origin.y + iy * cell, L.origin.z + iz * cell);
+    float f[kFeat];
+    f[0] = grid_sigma(P, x) * Q.inv_sigma_ref;
+#pragma unroll 4
+    for (int k = 0; k < 32; ++k) f[1 + k] = grid_sigma(P, x + L.sun * Q.dist[k]) * Q.inv_sigma_ref;
+    const float r = Q.nbr * 0.57735026918962576f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        float3 o = f3((j & 1) ? r : -r, (j & 2) ? r : -r, (j & 4) ? r : -r);
+        f[33 + j] = grid_sigma(P, x + o) * Q.inv_sigma_ref;
+    }
+    f[41] = fminf(fmaxf((x.z - B.lo.z) / (B.hi.z - B.lo.z), 0.f), 1.f);
+    store_record(rec + node * 6, f, 0.f);
+    // optical depth to the sun: midpoint rule to the exit of the grid box
+    float t0, t1;
+    box_hit(B.lo, B.hi, x, L.sun, t0, t1);
+    float od = 0.f;
+    if (t1 > 0.f) {
+        int steps = min((int)ceilf(t1 / Q.step), kMaxTrackSteps);
+        float h = t1 / (float)max(steps, 1);
+        for (int s = 0; s < steps; ++s) od += grid_sigma(P, x + L.sun * ((s + 0.5f) * h));
+        od *= h;
+    }
+    tau[node] = od;
+}
+
+__global__ void __launch_bounds__(128) sample_points_kernel(PtConsts P, GridBox B, float sigma_max, float sigma_min,
+                                                            uint32_t seed_lo, uint32_t seed_hi, int n,
+                                                            float* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t s = pcg_hash(pcg_hash(seed_lo ^ pcg_hash((uint32_t)i)) + seed_hi);
+    float3 ext = B.hi - B.lo;
+    float3 x = B.lo + ext * 0.5f, d = f3(0.f, 0.f, 1.f);
+    bool found = false;
+    if ((i & 1) == 0 && sigma_max > 0.f) {
+        // first collision of a ray from outside the box aimed at a random point in it
+        for (int tr = 0; tr < kMaxSampleTries && !found; ++tr) {
+            float3 q = B.lo + f3(ext.x * u01(s), ext.y * u01(s), ext.z * u01(s));
+            float3 dir = uniform_dir(s);
+            float3 o = q - dir * (2.f * B.span);
+            float t0, t1;
+            box_hit(B.lo, B.hi, o, dir, t0, t1);
+            float t = t0;
+            for (int it = 0; it < kMaxTrackSteps; ++it) {
+                t += -__logf(1.f - u01(s)) / sigma_max;
+                if (!(t < t1)) break;
+                float3 p = o + dir * t;
+                if (u01(s) * sigma_max < grid_sigma(P, p)) {
+                    x = p;
+                    d = dir;
+                    found = true;
+                    break;
+                }
+            }
+        }
+    }
+    if (!found) {
+        for (int tr = 0; tr < 4 * kMaxSampleTries; ++tr) {
+            x = B.lo + f3(ext.x * u01(s), ext.y * u01(s), ext.z * u01(s));
+            if (grid_sigma(P, x) >= sigma_min) break;
+        }
+        d = uniform_dir(s);
+    }
+    float* o6 = out + 6 * (size_t)i;
+    o6[0] = x.x; o6[1] = x.y; o6[2] = x.z;
+    o6[3] = d.x; o6[4] = d.y; o6[5] = d.z;
+}
+
+__global__ void __launch_bounds__(128) records_kernel(Lattice L, const float* __restrict__ pts, int n,
+                                                      uint4* __restrict__ rec) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* q = pts + 6 * (size_t)i;
+    float3 x = f3(q[0], q[1], q[2]), d = f3(q[3], q[4], q[5]);
+    float f[kFeat];
+    lattice_at<true>(L, x, f);
+    store_record(rec + (size_t)i * 6, f, dot3(d, L.sun));
+}
+
+struct RenderConsts {
+    int steps, use_network;
+    float network_error, min_t;
+    float g_fwd, g_back, ratio;
+    const float* error_table;
+};
+
+constexpr int kBins = SKYR_SURROGATE_ERROR_BINS;
+
+// error-table bin of a sample: feature 0 and the mean of features 1..8
+__device__ __forceinline__ int error_bin(float f0, float near_sun) {
+    int a = min(max((int)(f0 * kBins), 0), kBins - 1), b = min(max((int)(near_sun * kBins), 0), kBins - 1);
+    return a * kBins + b;
+}
+
+__global__ void __launch_bounds__(256) error_bins_kernel(const __nv_bfloat16* __restrict__ rec, int n,
+                                                         int* __restrict__ bins) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const __nv_bfloat16* r = rec + (size_t)i * SKYR_MLP_RECORD;
+    float s = 0.f;
+    for (int k = 1; k <= 8; ++k) s += __bfloat162float(r[k]);
+    bins[i] = error_bin(__bfloat162float(r[0]), s * 0.125f);
+}
+
+constexpr int kRenderWarps = 4;
+constexpr int kSmTile = 32 * mlp::kXS * 2;    // records of one warp
+constexpr int kSmOut = 32 * 4 * 4;            // network outputs of one warp
+constexpr int kSmRender = mlp::kPackedBytes + kRenderWarps * (kSmTile + kSmOut);
+
+template <class S>
+__global__ void __launch_bounds__(128, 4) surrogate_render_kernel(CloudConsts C, AtmoConsts A, PtConsts P, Lattice L,
+                                                                  RenderConsts R, const float4* __restrict__ tlut,
+                                                                  int tw, int th, const S* __restrict__ apl,
+                                                                  const S* __restrict__ apt,
+                                                                  const unsigned char* __restrict__ packed,
+                                                                  float4* __restrict__ out,
+                                                                  float* __restrict__ out_err) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const unsigned full = 0xffffffffu;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (R.use_network) {
+        mlp::load_packed(sm, packed);
+        __syncthreads();
+    }
+    __nv_bfloat16* tile = reinterpret_cast<__nv_bfloat16*>(sm + mlp::kPackedBytes + warp * (kSmTile + kSmOut));
+    float* yout = reinterpret_cast<float*>(sm + mlp::kPackedBytes + warp * (kSmTile + kSmOut) + kSmTile);
+    const int tiles_x = (P.width + 7) / 8;
+    const int t_id = blockIdx.x * kRenderWarps + warp;
+    const int px = (t_id % tiles_x) * 8 + (lane & 7), py = (t_id / tiles_x) * 4 + (lane >> 3);
+    const bool in_view = px < P.width && py < P.height;
+    float u, v;
+    float3 dir = primary_dir(C, P, min(px, P.width - 1), min(py, P.height - 1), u, v);
+    float t0 = 0.f, t1 = 0.f;
+    region(P, C.cam, dir, t0, t1);
+    bool hit = in_view && t0 < t1;
+    const float dt = hit ? (t1 - t0) / (float)R.steps : 0.f;
+    uint32_t js = pcg_hash((uint32_t)(py * P.width + px) * 747796405u + 2891336453u);
+    const float jitter = (float)(js >> 8) * (1.f / 16777216.f);
+    const float mu = dot3(dir, C.sun);
+    const float ph = hg_pt(mu, R.g_back) * (1.f - R.ratio) + hg_pt(mu, R.g_fwd) * R.ratio;
+    float T = 1.f, err = 0.f, wsum = 0.f, wt = 0.f;
+    float3 Lum = f3(0.f);
+    uint4* row = reinterpret_cast<uint4*>(tile + lane * mlp::kXS);
+    for (int s = 0; s < R.steps; ++s) {
+        bool live = hit && T > R.min_t;
+        if (!__any_sync(full, live)) break;
+        float t = t0 + ((float)s + jitter) * dt;
+        float3 x = C.cam + dir * t;
+        float sigma = live ? grid_sigma(P, x) : 0.f;
+        bool need = live && sigma > 0.f;
+        if (!__any_sync(full, need)) continue;
+        float tau = 0.f, rel_err = R.network_error;
+        float3 ms = f3(0.f);
+        if (R.use_network) {
+            if (need) {
+                float f[kFeat];
+                tau = lattice_at<true>(L, x, f);
+                store_record(row, f, mu);
+                if (R.error_table) {
+                    float near_sun = 0.f;
+#pragma unroll
+                    for (int k = 1; k <= 8; ++k) near_sun += f[k];
+                    rel_err = __ldg(R.error_table + error_bin(f[0], near_sun * 0.125f));
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 6; ++q) row[q] = make_uint4(0, 0, 0, 0);
+            }
+            __syncwarp();
+            mlp::forward_warp(sm, tile, yout);
+            __syncwarp();
+            ms = f3(fmaxf(yout[lane * 4], 0.f), fmaxf(yout[lane * 4 + 1], 0.f), fmaxf(yout[lane * 4 + 2], 0.f));
+            __syncwarp();
+        } else if (need) {
+            float f[kFeat];
+            tau = lattice_at<false>(L, x, f);
+        }
+        if (need) {
+            float3 ss = sun_illuminance(C, A, tlut, tw, th, x) * (ph * __expf(-tau));
+            float dT = __expf(-sigma * dt);
+            float w = T * (1.f - dT);
+            Lum += (ss + ms) * w;
+            err += w * (ms.x + ms.y + ms.z) * (1.f / 3.f) * rel_err;
+            wsum += w;
+            wt += w * t;
+            T *= dT;
+        }
+    }
+    if (!in_view) return;
+    if (wsum > 0.f) {
+        // GetAerialPerspective (VolumetricCloudCommon.glsl:81-98) at the mean depth
+        float ta = wt / wsum;
+        if (C.atmo_in_space != 0.f) {
+            float r = C.R + C.cam.z, rm = r * dir.z;
+            float cc = (C.cam.z - A.thickness) * (r + A.top);
+            float disc = rm * rm - cc;
+            if (dir.z < 0.f && disc >= 0.f) ta -= fmaxf(cc / (-rm + sqrtf(disc)), 0.f);
+            else ta = 0.f;
+        }
+        float wz = sqrtf(fmaxf(ta, 0.f) * C.inv_ap_max_distance);
+        float ax = u * (float)(C.ap_w - 1), ay = v * (float)(C.ap_h - 1), az = wz * (float)(C.ap_d - 1);
+        float3 at = trilinear_clamp(apt, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
+        float3 al = trilinear_clamp(apl, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
+        Lum = Lum * at + al * (1.f - T);
+    }
+    size_t pix = (size_t)py * P.width + px;
+    out[pix] = make_float4(Lum.x, Lum.y, Lum.z, T);
+    if (out_err) out_err[pix] = err;
+}
+
+// Launch constants of a grid: the PtConsts grid fields and the grid box.
+int grid_setup(const skyr_density_grid* grid, PtConsts& P, GridBox& B) {
+    if (!grid || !grid->data) return set_error(SKYR_EINVAL, "null density grid");
+    if (grid->nx < 2 || grid->ny < 2 || grid->nz < 2 || !(grid->voxel_size > 0.f) ||
+        !std::isfinite(grid->density) || grid->density < 0.f || !std::isfinite(grid->origin[0]) ||
+        !std::isfinite(grid->origin[1]) || !std::isfinite(grid->origin[2]))
+        return set_error(SKYR_EINVAL, "bad density grid");
+    std::memset(&P, 0, sizeof(P));
+    P.grid = reinterpret_cast<const unsigned short*>(grid->data);
+    P.nx = grid->nx;
+    P.ny = grid->ny;
+    P.nz = grid->nz;
+    P.origin = make_float3(grid->origin[0], grid->origin[1], grid->origin[2]);
+    P.inv_voxel = 1.f / grid->voxel_size;
+    P.density = grid->density;
+    B.lo = P.origin;
+    B.hi = make_float3(grid->origin[0] + grid->nx * grid->voxel_size, grid->origin[1] + grid->ny * grid->voxel_size,
+                       grid->origin[2] + grid->nz * grid->voxel_size);
+    B.span = grid->voxel_size * (float)std::max(grid->nx, std::max(grid->ny, grid->nz));
+    return SKYR_OK;
+}
+
+int lattice_setup(const skyr_density_grid* grid, const skyr_feature_volume* fv, Lattice& L) {
+    if (!fv || !fv->data) return set_error(SKYR_EINVAL, "null feature lattice");
+    if (fv->stride < 1 || fv->nx < 2 || fv->ny < 2 || fv->nz < 2)
+        return set_error(SKYR_EINVAL, "feature lattice not sized (skyr_feature_volume_bytes)");
+    if (fv->nx != (grid->nx + fv->stride - 1) / fv->stride + 1 || fv->ny != (grid->ny + fv->stride - 1) / fv->stride + 1 ||
+        fv->nz != (grid->nz + fv->stride - 1) / fv->stride + 1)
+        return set_error(SKYR_EINVAL, "feature lattice does not match the grid");
+    if (reinterpret_cast<uintptr_t>(fv->data) & 15) return set_error(SKYR_EINVAL, "feature lattice must be 16-byte aligned");
+    size_t nodes = (size_t)fv->nx * fv->ny * fv->nz;
+    L.rec = reinterpret_cast<const uint4*>(fv->data);
+    L.tau = reinterpret_cast<const float*>(reinterpret_cast<const unsigned char*>(fv->data) + nodes * 96);
+    L.nx = fv->nx;
+    L.ny = fv->ny;
+    L.nz = fv->nz;
+    L.origin = make_float3(grid->origin[0], grid->origin[1], grid->origin[2]);
+    L.inv_cell = 1.f / (grid->voxel_size * (float)fv->stride);
+    L.sun = make_float3(fv->sun[0], fv->sun[1], fv->sun[2]);
+    return SKYR_OK;
+}
+
+int frame_consts(const skyr_atmosphere_parameters* atmosphere, const skyr_cloud_parameters* cloud,
+                 const skyr_cloud_view* view, const skyr_lut_sizes* sizes, CloudConsts& C, AtmoConsts& A) {
+    skyr_cloud_material mat;
+    skyr_cloud_material_default(SKYR_MATERIAL_MINIMAL, &mat);
+    skyr_cloud_textures tex{};
+    MaterialConsts M;
+    if (int st = derive_cloud_consts(*atmosphere, *cloud, mat, tex, *view, *sizes, C, M)) return st;
+    derive_atmo_consts(*atmosphere, A);
+    return SKYR_OK;
+}
+
+}  // namespace
+}  // namespace skyr
+
+using namespace skyr;
+
+extern "C" {
+
+int skyr_surrogate_parameters_default(skyr_surrogate_parameters* p) {
+    if (!p) return set_error(SKYR_EINVAL, "null parameters");
+    p->steps = 128;
+    p->use_network = 1;
+    p->network_error = 0.05f;
+    p->min_transmittance = 1e-4f;
+    p->error_table = nullptr;
+    return SKYR_OK;
+}
+
+size_t skyr_feature_volume_bytes(const skyr_density_grid* grid, int stride, skyr_feature_volume* fv) {
+    if (!grid || stride < 1 || grid->nx < 2 || grid->ny < 2 || grid->nz < 2) return 0;
+    int nx = (grid->nx + stride - 1) / stride + 1, ny = (grid->ny + stride - 1) / stride + 1,
+        nz = (grid->nz + stride - 1) / stride + 1;
+    if (fv) {
+        fv->stride = stride;
+        fv->nx = nx;
+        fv->ny = ny;
+        fv->nz = nz;
+    }
+    return (size_t)nx * ny * nz * (96 + 4);
+}
+
+int skyr_feature_volume_build(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                              const skyr_cloud_parameters* cloud, const skyr_density_grid* grid,
+                              const skyr_cloud_view* view, skyr_feature_volume* fv) {
+    if (!ctx || !atmosphere || !cloud || !grid || !view || !fv) return set_error(SKYR_EINVAL, "null argument");
+    if (!(fv->sigma_ref > 0.f) || !std::isfinite(fv->sigma_ref)) return set_error(SKYR_EINVAL, "bad sigma_ref");
+    PtConsts P;
+    GridBox B;
+    if (int e = grid_setup(grid, P, B)) return e;
+    if (skyr_feature_volume_bytes(grid, fv->stride, fv) == 0) return set_error(SKYR_EINVAL, "bad lattice stride");
+    skyr_lut_sizes sizes{};
+    sizes.transmittance_width = sizes.transmittance_height = 2;
+    sizes.aerial_perspective_width = sizes.aerial_perspective_height = sizes.aerial_perspective_depth = 2;
+    CloudConsts C;
+    AtmoConsts A;
+    if (int e = frame_consts(atmosphere, cloud, view, &sizes, C, A)) return e;
+    fv->sun[0] = C.sun.x;
+    fv->sun[1] = C.sun.y;
+    fv->sun[2] = C.sun.z;
+    Lattice L;
+    if (int e = lattice_setup(grid, fv, L)) return e;
+    LatticeBuild Q;
+    for (int k = 0; k < 32; ++k) Q.dist[k] = B.span * 0.01f * (float)std::pow(1000.0, k / 31.0);
+    Q.nbr = 0.1f * B.span;
+    Q.inv_sigma_ref = 1.f / fv->sigma_ref;
+    Q.step = 0.5f * grid->voxel_size;
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    size_t nodes = (size_t)L.nx * L.ny * L.nz;
+    feature_lattice_kernel<<<(unsigned)((nodes + 127) / 128), 128, 0, ctx->stream>>>(
+        P, B, L, Q, fv->stride, reinterpret_cast<uint4*>(fv->data), const_cast<float*>(L.tau));
+    return check_cuda(cudaGetLastError(), "feature lattice kernel");
+}
+
+int skyr_surrogate_sample_points(skyr_ctx* ctx, const skyr_density_grid* grid, float sigma_max, float sigma_min,
+                                 uint64_t seed, int n, float* points) {
+    if (!ctx || !grid || (n > 0 && !points)) return set_error(SKYR_EINVAL, "null argument");
+    if (n < 0) return set_error(SKYR_EINVAL, "negative point count");
+    if (!(sigma_max >= 0.f) || !std::isfinite(sigma_max) || !std::isfinite(sigma_min))
+        return set_error(SKYR_EINVAL, "bad extinction bounds");
+    PtConsts P;
+    GridBox B;
+    if (int e = grid_setup(grid, P, B)) return e;
+    if (n == 0) return SKYR_OK;
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    sample_points_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(P, B, sigma_max, sigma_min, (uint32_t)seed,
+                                                                  (uint32_t)(seed >> 32), n, points);
+    return check_cuda(cudaGetLastError(), "sample points kernel");
+}
+
+int skyr_surrogate_records(skyr_ctx* ctx, const skyr_density_grid* grid, const skyr_feature_volume* fv,
+                           const float* points, int n, uint16_t* records) {
+    if (!ctx || !grid || (n > 0 && (!points || !records))) return set_error(SKYR_EINVAL, "null argument");
+    if (n < 0) return set_error(SKYR_EINVAL, "negative point count");
+    if (reinterpret_cast<uintptr_t>(records) & 15) return set_error(SKYR_EINVAL, "records must be 16-byte aligned");
+    PtConsts P;
+    GridBox B;
+    if (int e = grid_setup(grid, P, B)) return e;
+    Lattice L;
+    if (int e = lattice_setup(grid, fv, L)) return e;
+    if (n == 0) return SKYR_OK;
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    records_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(L, points, n, reinterpret_cast<uint4*>(records));
+    return check_cuda(cudaGetLastError(), "records kernel");
+}
+
+int skyr_surrogate_error_bins(skyr_ctx* ctx, const uint16_t* records, int n, int* bins) {
+    if (!ctx || (n > 0 && (!records || !bins))) return set_error(SKYR_EINVAL, "null argument");
+    if (n < 0) return set_error(SKYR_EINVAL, "negative record count");
+    if (n == 0) return SKYR_OK;
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    error_bins_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(reinterpret_cast<const __nv_bfloat16*>(records), n,
+                                                                bins);
+    return check_cuda(cudaGetLastError(), "error bins kernel");
+}
+
+int skyr_surrogate_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                          const skyr_cloud_parameters* cloud, const skyr_density_grid* grid,
+                          const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
+                          const skyr_lut_sizes* sizes, const void* transmittance,
+                          const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
+                          const skyr_feature_volume* fv, const void* packed, const skyr_surrogate_parameters* sp,
+                          float* out_rgba, float* out_error) {
+    if (!ctx || !atmosphere || !cloud || !grid || !pt || !view || !sizes || !sp || !out_rgba)
+        return set_error(SKYR_EINVAL, "null argument");
+    if (!transmittance || !aerial_perspective_luminance || !aerial_perspective_transmittance)
+        return set_error(SKYR_EINVAL, "null LUT input");
+    if (sp->steps < 1 || sp->steps > 4096) return set_error(SKYR_EINVAL, "steps must be in [1, 4096]");
+    if (sp->use_network && !packed) return set_error(SKYR_EINVAL, "network requested but none given");
+    if (packed && (reinterpret_cast<uintptr_t>(packed) & 15))
+        return set_error(SKYR_EINVAL, "packed network must be 16-byte aligned");
+    if (!(std::fabs(pt->forward_phase_g) < 1.f) || !(std::fabs(pt->back_phase_g) < 1.f) ||
+        !(pt->forward_scattering_ratio >= 0.f && pt->forward_scattering_ratio <= 1.f))
+        return set_error(SKYR_EINVAL, "phase parameters out of range");
+    if (view->width < 1 || view->height < 1 || view->width > 16384 || view->height > 16384)
+        return set_error(SKYR_EINVAL, "render size must be in [1, 16384]");
+    if (sizes->aerial_perspective_width < 2 || sizes->aerial_perspective_height < 2 ||
+        sizes->aerial_perspective_depth < 2 || sizes->transmittance_width < 2 || sizes->transmittance_height < 2)
+        return set_error(SKYR_EINVAL, "LUT sizes must be >= 2");
+    PtConsts P;
+    GridBox B;
+    if (int e = grid_setup(grid, P, B)) return e;
+    Lattice L;
+    if (int e = lattice_setup(grid, fv, L)) return e;
+    CloudConsts C;
+    AtmoConsts A;
+    if (int e = frame_consts(atmosphere, cloud, view, sizes, C, A)) return e;
+    // the region box of the path tracer, clipped to the grid
+    float hw = pt->region_box_half_width;
+    P.box_min = make_float3(fmaxf(-hw, B.lo.x), fmaxf(-hw, B.lo.y), fmaxf(C.bottom, B.lo.z));
+    P.box_max = make_float3(fminf(hw, B.hi.x), fminf(hw, B.hi.y), fminf(C.top, B.hi.z));
+    P.width = view->width;
+    P.height = view->height;
+    RenderConsts R;
+    R.steps = sp->steps;
+    R.use_network = sp->use_network ? 1 : 0;
+    R.network_error = sp->network_error;
+    R.min_t = sp->min_transmittance;
+    R.g_fwd = pt->forward_phase_g;
+    R.g_back = pt->back_phase_g;
+    R.ratio = pt->forward_scattering_ratio;
+    R.error_table = sp->error_table;
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    auto launch = [&](auto tag) -> int {
+        using S = decltype(tag);
+        auto kernel = surrogate_render_kernel<S>;
+        const int use_smem = kSmRender;  // the network slot stays reserved when it is unused
+        if (int e = check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, use_smem),
+                               "surrogate smem attribute"))
+            return e;
+        int tiles = ((view->width + 7) / 8) * ((view->height + 3) / 4);
+        kernel<<<(tiles + kRenderWarps - 1) / kRenderWarps, 32 * kRenderWarps, use_smem, ctx->stream>>>(
+            C, A, P, L, R, reinterpret_cast<const float4*>(transmittance), sizes->transmittance_width,
+            sizes->transmittance_height, reinterpret_cast<const S*>(aerial_perspective_luminance),
+            reinterpret_cast<const S*>(aerial_perspective_transmittance),
+            reinterpret_cast<const unsigned char*>(packed), reinterpret_cast<float4*>(out_rgba), out_error);
+        return check_cuda(cudaGetLastError(), "surrogate render kernel");
+    };
+    return sizes->format == SKYR_FORMAT_RGBA16F ? launch(__half2{}) : launch(float4{});
+}
+
+}  // extern "C"

@@ -103,6 +103,9 @@ class Trainer:
         _check_records(rec)
         _abi.call("skyr_mlp_train_step", self._tr, _ptr(rec), _ptr(targets), rec.shape[0], _ptr(loss_accum))
 
+    def set_learning_rate(self, lr: float):
+        _abi.call("skyr_mlp_trainer_set_learning_rate", self._tr, C.c_float(lr))
+
     @property
     def steps(self) -> int:
         return int(_abi.lib().skyr_mlp_trainer_steps(self._tr))
