@@ -1,6 +1,6 @@
 """Benchmark of the atmosphere-LUT / volumetric-cloud hot path on one GB300.
 
-A step is one plain 1920x1080 frame:
+The timed step (value, e2e) is one plain 1920x1080 frame:
   * the whole LUT set (transmittance 256x64 / 40 samples, multi-scattering
     32x32 / 64 directions x 20 samples, sky-view 192x108 / 30 samples, aerial
     perspective 32^3 / 40 samples over 32 km), then
@@ -9,6 +9,13 @@ A step is one plain 1920x1080 frame:
 Noise textures (512^2 RG8 weather map, 128^3 RGBA8 base noise) are generated
 once before timing, as the reference regenerates them only when their
 parameters change.  Inputs are seeded synthetic (skyrendering_gb300/workloads.py).
+
+The third part of the metric, the surrogate against the path tracer on the
+512x640x352 voxel cloud, is measured after the timed frames and reported under
+"surrogate" (GPU times at 1024^2, errors at 256^2 against a path-traced
+reference, the path tracer's spp and time at the surrogate's error).  The
+batched workload (256 parameter sets, 64 views of uneven size, one CUDA graph
+with autotuned launch shapes) is reported under "batched".
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -44,6 +51,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="skyr", choices=["skyr", "reference"])
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="leave out the voxel-cloud leg (surrogate vs path tracer) of the metric")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="leave out the batched 256-set / 64-view graph measurement")
     return ap.parse_args()
 
 
@@ -159,6 +170,161 @@ class FrameState:
                        out_distance=self.dist)
 
 
+def surrogate_vs_pathtracer(ctx, small: int = 256, ref_spp: int = 4096, big: int = 1024):
+    """The voxel-cloud leg of the metric: GPU time of the surrogate-shaded image
+    against the plain path tracer at equal error.
+
+    * times (CUDA events, on the context's stream): the surrogate raymarch at
+      big x big, the feature lattice it needs, one path-traced frame at big x big
+      (a 16-frame call / 16);
+    * errors at small x small against a 2 x ref_spp path-traced reference:
+      surrogate, single scattering only (no network), and the path tracer at
+      64 / 256 / 1024 spp; the spp at which the path tracer reaches the
+      surrogate's error is interpolated in log-log between those points.
+    """
+    import math
+
+    import torch
+
+    from skyrendering_gb300 import surrogate as S
+    from skyrendering_gb300 import surrogate_train as T
+    from skyrendering_gb300.pathtrace import PathTracer
+
+    model = S.load_model(S.MODEL_PATH)
+    net = model.packed(ctx)
+    table = torch.from_numpy(model.error_table).cuda()
+    stream = ctx.stream
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps=5):
+        fn()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out = {"image": f"{big}x{big}", "grid": "512x640x352 FP16, max extinction 40/km, 16^3 brick majorants",
+           "network": "43-64-64-64-64-3 BF16, 128-step raymarch", "target_rel_l1": 0.02}
+    sc = T.Scene(ctx, size=big)
+    grid = sc.grid(0x5EED)
+    fv = sc.lattice(grid)
+    sp = S.parameters(error_table=table)
+    out["lattice_ms"] = timed(lambda: sc.lattice(grid), reps=3)
+    out["surrogate_ms"] = timed(lambda: S.render(ctx, sc.atmo, sc.cloud, grid, sc.pt, sc.view, sc.sizes, sc.luts,
+                                                 fv, net, sp))
+    tr = PathTracer(ctx, sc.pt, sc.cloud, sc.view, sc.env, sc.sizes, grid=grid)
+    out["pt_ms_per_spp"] = timed(lambda: tr.render(sc.atmo, sc.luts, 16), reps=2) / 16.0
+    del tr, fv
+    # errors at the small size
+    sm = T.Scene(ctx, size=small)
+    fvs = sm.lattice(grid)
+    sur, _ = S.render(ctx, sm.atmo, sm.cloud, grid, sm.pt, sm.view, sm.sizes, sm.luts, fvs, net, sp)
+    ss, _ = S.render(ctx, sm.atmo, sm.cloud, grid, sm.pt, sm.view, sm.sizes, sm.luts, fvs, None,
+                     S.parameters(use_network=0))
+
+    def pt_image(frames, begin):
+        t = PathTracer(ctx, sm.pt, sm.cloud, sm.view, sm.env, sm.sizes, grid=grid)
+        t.frames = begin
+        t.render(sm.atmo, sm.luts, frames)
+        return t.acc / frames
+
+    ref = (pt_image(ref_spp, 1000000) + pt_image(ref_spp, 2000000)) / 2
+    out["reference"] = f"{small}x{small}, 2 x {ref_spp} spp"
+    out["rel_l1_surrogate"] = e_s = S.relative_l1(sur, ref)
+    out["rel_l1_single_scattering_only"] = S.relative_l1(ss, ref)
+    pts = [(n, S.relative_l1(pt_image(n, 3000000 + n), ref)) for n in (64, 256, 1024)]
+    out["rel_l1_pt"] = {str(n): e for n, e in pts}
+    # log-log interpolation (or extrapolation from the last two points)
+    (n0, e0), (n1, e1) = (pts[-2], pts[-1]) if e_s < pts[1][1] else (pts[0], pts[1])
+    slope = math.log(e1 / e0) / math.log(n1 / n0)
+    spp = n0 * math.exp(math.log(e_s / e0) / slope) if slope < 0 else float("nan")
+    out["pt_spp_for_equal_error"] = spp
+    out["pt_ms_equal_error"] = spp * out["pt_ms_per_spp"]
+    surrogate_total = out["surrogate_ms"] + out["lattice_ms"]
+    out["speedup_equal_error"] = out["pt_ms_equal_error"] / surrogate_total
+    out["speedup_equal_error_static_lattice"] = out["pt_ms_equal_error"] / out["surrogate_ms"]
+    out["meets_target"] = bool(e_s <= 0.02 and out["speedup_equal_error"] >= 20.0)
+    ctx.check_status()
+    return out
+
+
+def batched_frames(ctx, reps: int = 5, n_sets: int = 256, n_views: int = 64):
+    """The batched workload (256 perturbed parameter sets, 64 views of uneven
+    size) as one CUDA graph: the prepared LUT batch (FP16 storage) followed by
+    the 64 raymarches fanned out over the context's streams.  Launch shapes are
+    picked by the autotuners first (LUT passes on the batch, raymarch on a
+    1920x1080 view of it)."""
+    import torch
+
+    from skyrendering_gb300 import batch as B
+    from skyrendering_gb300 import workloads as W
+    from skyrendering_gb300.atmosphere import LutSet
+    from skyrendering_gb300.cloud import NoiseTexture, blue_noise_tile, prepare_textures, textures_struct
+
+    stream = ctx.stream
+    params, renders, views, sov = W.batched_frame(n_sets, n_views)
+    sizes = W.plain_lut_sizes(1)
+    cloud, material = W.frame_cloud_parameters(), W.frame_material()
+    tex = {"cloud_map": NoiseTexture(W.cloud_map_desc()).generate(ctx),
+           "detail": NoiseTexture(W.base_noise_desc()).generate(ctx)}
+    prepare_textures(ctx, material.type, tex)
+    textures = textures_struct(**tex)
+    bn = blue_noise_tile().cuda()
+    luts = LutSet.allocate(sizes, n_sets)
+    lut_best, lut_times = B.autotune_luts(ctx, params, renders, n_sets, sizes, luts, reps=3)
+    k = next(i for i in range(n_views) if views[i].width == 1920) if any(
+        views[i].width == 1920 for i in range(n_views)) else 0
+    probe_rgba = torch.empty((views[k].height, views[k].width, 4), dtype=torch.float16, device="cuda")
+    probe_dist = torch.empty((views[k].height, views[k].width), dtype=torch.float32, device="cuda")
+    one = LutSet(luts.transmittance[sov[k]:sov[k] + 1], luts.multiscattering[sov[k]:sov[k] + 1],
+                 luts.sky_view_luminance[sov[k]:sov[k] + 1], luts.sky_view_transmittance[sov[k]:sov[k] + 1],
+                 luts.aerial_perspective_luminance[sov[k]:sov[k] + 1],
+                 luts.aerial_perspective_transmittance[sov[k]:sov[k] + 1])
+    cloud_best, cloud_times = B.autotune_cloud(ctx, params[sov[k]], cloud, material, textures, views[k], sizes, one,
+                                               bn, probe_rgba, probe_dist, reps=3)
+    del probe_rgba, probe_dist
+    lb = B.LutBatch(ctx, params, renders, n_sets, sizes)
+    out = B.ViewOutputs(views, n_views)
+    with B.capture(ctx) as lut_cap:
+        lb.launch(luts)
+    with B.capture(ctx) as cap:
+        lb.launch(luts)
+        B.render_views(ctx, params, n_sets, sov, cloud, material, textures, views, n_views, sizes, luts, bn, out)
+
+    def timed(g):
+        for _ in range(3):
+            g.launch()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            g.launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    lut_ms = timed(lut_cap.graph)
+    graph_ms = timed(cap.graph)
+    ctx.check_status()
+    px = out.pixels
+    res = {"sets": n_sets, "views": n_views, "view_pixels": px, "lut_storage": "RGBA16F",
+           "graph_ms": graph_ms, "lut_batch_ms": lut_ms, "lut_us_per_set": lut_ms * 1000.0 / n_sets,
+           "raymarch_ms": graph_ms - lut_ms, "raymarch_gpix_per_s": px / ((graph_ms - lut_ms) * 1e-3) / 1e9,
+           "graph_launches": 1, "kernels_per_graph": 3 + n_views,
+           "tuning": {"transmittance_lanes": lut_best.transmittance_lanes, "view_lanes": lut_best.view_lanes,
+                      "cloud_tile_width": cloud_best.cloud_tile_width,
+                      "cloud_block_warps_x": cloud_best.cloud_block_warps_x},
+           "autotune_lut_ms": {"transmittance_lanes_4_8_16": lut_times[:3], "view_lanes_4_8_16": lut_times[3:]},
+           "autotune_cloud_ms": {f"{w}x{32 // w}/{bx}": t for (w, bx), t in zip(B.TILE_CANDIDATES, cloud_times)}}
+    cap.graph.close()
+    lut_cap.graph.close()
+    lb.close()
+    return res
+
+
 def run_skyr(args):
     import ctypes as C
 
@@ -177,6 +343,12 @@ def run_skyr(args):
     torch.cuda.set_stream(stream)
     ctx = Context(stream)
     fs = FrameState(ctx)
+    # launch shapes from the autotuners, on this frame's own workload (setup, untimed)
+    from skyrendering_gb300 import batch as B
+
+    lut_tuned, _ = B.autotune_luts(ctx, fs.atmo, fs.render, 1, fs.sizes, fs.luts, reps=5)
+    cloud_tuned, _ = B.autotune_cloud(ctx, fs.atmo, fs.vc.params, fs.vc.material, fs.vc.textures, fs.view, fs.sizes,
+                                      fs.luts, fs.bn, fs.rgba, fs.dist, reps=5)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     kernels_per_step = 4  # transmittance, multi-scattering, sky-view + AP, cloud raymarch
 
@@ -276,7 +448,11 @@ def run_skyr(args):
                                "AP 32^3x40 over 32 km) + per-pixel cloud raymarch (layer 1.5-4.0 km, "
                                "Material1 50/km, 64 steps, 6 light steps)",
                    "l2": "flushed between timed steps (512 MB write outside the timed interval)",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "tuning": {"transmittance_lanes": lut_tuned.transmittance_lanes,
+                              "view_lanes": lut_tuned.view_lanes,
+                              "cloud_tile": f"{cloud_tuned.cloud_tile_width}x{32 // cloud_tuned.cloud_tile_width}",
+                              "cloud_block_warps_x": cloud_tuned.cloud_block_warps_x}},
         "components": {"lut_set_us": statistics.mean(lut_ms) * 1000.0, "cloud_frame_ms": cloud_mean,
                        "raymarch_samples": samples, "density_evaluations": evals,
                        "density_evaluations_per_s": evals / (cloud_mean * 1e-3)},
@@ -293,6 +469,10 @@ def run_skyr(args):
         "clocks": clocks,
         "wall_s": wall,
     }
+    if not args.no_surrogate:
+        result["surrogate"] = surrogate_vs_pathtracer(ctx)
+    if not args.no_batched:
+        result["batched"] = batched_frames(ctx)
     if rank == 0:
         if world == 1:
             result["cpu_baseline"] = cpu_baseline(args.cpu_sample_s)

@@ -380,3 +380,38 @@ _SIGNATURES.update({
                                         C.POINTER(LutSizes), P, P, P, C.POINTER(FeatureVolume), P,
                                         C.POINTER(SurrogateParameters), P, P]),
 })
+
+
+# ---------------------------------------------------------------------------
+# skyr_batch.h
+# ---------------------------------------------------------------------------
+SKYR_CLOUD_TILE_CANDIDATES = 12
+
+
+class Tuning(C.Structure):
+    _fields_ = [("transmittance_lanes", C.c_int), ("view_lanes", C.c_int), ("cloud_tile_width", C.c_int),
+                ("cloud_block_warps_x", C.c_int)]
+
+
+STRUCT_IDS.update({14: Tuning})
+_SIGNATURES.update({
+    "skyr_tuning_default": (C.c_int, [C.POINTER(Tuning)]),
+    "skyr_ctx_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "skyr_ctx_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "skyr_autotune_luts": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(AtmosphereRenderParameters),
+                                     C.c_int, C.POINTER(LutSizes), P, P, P, P, P, P, C.c_int, C.POINTER(Tuning), P]),
+    "skyr_autotune_cloud": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                      C.POINTER(CloudMaterial), C.POINTER(CloudTextures), C.POINTER(CloudView),
+                                      C.POINTER(LutSizes), P, P, P, P, P, P, C.c_int, C.POINTER(Tuning), P]),
+    "skyr_lut_batch_create": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(AtmosphereRenderParameters),
+                                        C.c_int, C.POINTER(LutSizes), C.POINTER(P)]),
+    "skyr_lut_batch_launch": (C.c_int, [P, P, P, P, P, P, P]),
+    "skyr_lut_batch_destroy": (C.c_int, [P]),
+    "skyr_cloud_render_views": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.c_int, P, C.POINTER(CloudParameters),
+                                          C.POINTER(CloudMaterial), C.POINTER(CloudTextures), C.POINTER(CloudView),
+                                          C.c_int, C.POINTER(LutSizes), P, P, P, P, P, P]),
+    "skyr_graph_begin": (C.c_int, [P]),
+    "skyr_graph_end": (C.c_int, [P, C.POINTER(P)]),
+    "skyr_graph_launch": (C.c_int, [P]),
+    "skyr_graph_destroy": (C.c_int, [P]),
+})

@@ -404,16 +404,23 @@ __global__ void __launch_bounds__(128) view_luts_kernel(JobSrc<TABLE> jobs, int 
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
-constexpr int kTLanes = 8;
-constexpr int kViewLanes = 8;
+// Lanes per texel / ray are a tuning choice (skyr_tuning): 4, 8 or 16.
+template <int LANES, bool TABLE>
+static void t_launch(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, float4* out, cudaStream_t st) {
+    long long threads = (long long)n_sets * s.transmittance_width * s.transmittance_height * LANES;
+    int blocks = (int)((threads + 127) / 128);
+    transmittance_kernel<LANES, TABLE>
+        <<<blocks, 128, 0, st>>>(jobs, n_sets, s.transmittance_width, s.transmittance_height, out);
+}
 
 template <bool TABLE>
 cudaError_t launch_transmittance(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, float4* out,
-                                 cudaStream_t st) {
-    long long threads = (long long)n_sets * s.transmittance_width * s.transmittance_height * kTLanes;
-    int blocks = (int)((threads + 127) / 128);
-    transmittance_kernel<kTLanes, TABLE>
-        <<<blocks, 128, 0, st>>>(jobs, n_sets, s.transmittance_width, s.transmittance_height, out);
+                                 cudaStream_t st, int lanes) {
+    switch (lanes) {
+        case 4: t_launch<4, TABLE>(jobs, n_sets, s, out, st); break;
+        case 16: t_launch<16, TABLE>(jobs, n_sets, s, out, st); break;
+        default: t_launch<8, TABLE>(jobs, n_sets, s, out, st); break;
+    }
     return cudaGetLastError();
 }
 
@@ -428,35 +435,45 @@ cudaError_t launch_multiscattering(JobSrc<TABLE> jobs, int n_sets, const skyr_lu
     return cudaGetLastError();
 }
 
-template <class S, bool TABLE>
-cudaError_t launch_view_luts(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, const float4* tlut,
-                             const S* ms, S* svl, S* svt, S* apl, S* apt, cudaStream_t st) {
+template <int LANES, class S, bool TABLE>
+static void v_launch(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, const float4* tlut, const S* ms,
+                     S* svl, S* svt, S* apl, S* apt, cudaStream_t st) {
     long long rays = (long long)n_sets * (s.sky_view_width * s.sky_view_height +
                                           s.aerial_perspective_width * s.aerial_perspective_height *
                                               s.aerial_perspective_depth);
-    int blocks = (int)((rays * kViewLanes + 127) / 128);
+    int blocks = (int)((rays * LANES + 127) / 128);
     LutView L{tlut, s.transmittance_width, s.transmittance_height};
-    view_luts_kernel<kViewLanes, S, TABLE><<<blocks, 128, 0, st>>>(
+    view_luts_kernel<LANES, S, TABLE><<<blocks, 128, 0, st>>>(
         jobs, n_sets, L, s.transmittance_width * s.transmittance_height, ms, s.multiscattering_width,
         s.multiscattering_height, s.multiscattering_width * s.multiscattering_height, s.sky_view_width,
         s.sky_view_height, s.aerial_perspective_width, s.aerial_perspective_height, s.aerial_perspective_depth, svl,
         svt, apl, apt);
+}
+
+template <class S, bool TABLE>
+cudaError_t launch_view_luts(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, const float4* tlut,
+                             const S* ms, S* svl, S* svt, S* apl, S* apt, cudaStream_t st, int lanes) {
+    switch (lanes) {
+        case 4: v_launch<4, S, TABLE>(jobs, n_sets, s, tlut, ms, svl, svt, apl, apt, st); break;
+        case 16: v_launch<16, S, TABLE>(jobs, n_sets, s, tlut, ms, svl, svt, apl, apt, st); break;
+        default: v_launch<8, S, TABLE>(jobs, n_sets, s, tlut, ms, svl, svt, apl, apt, st); break;
+    }
     return cudaGetLastError();
 }
 
 #define SKYR_INST(TABLE)                                                                                        \
     template cudaError_t launch_transmittance<TABLE>(JobSrc<TABLE>, int, const skyr_lut_sizes&, float4*,        \
-                                                     cudaStream_t);                                             \
+                                                     cudaStream_t, int);                                        \
     template cudaError_t launch_multiscattering<float4, TABLE>(JobSrc<TABLE>, int, const skyr_lut_sizes&,       \
                                                                const float4*, float4*, cudaStream_t);           \
     template cudaError_t launch_multiscattering<__half2, TABLE>(JobSrc<TABLE>, int, const skyr_lut_sizes&,      \
                                                                 const float4*, __half2*, cudaStream_t);         \
     template cudaError_t launch_view_luts<float4, TABLE>(JobSrc<TABLE>, int, const skyr_lut_sizes&,             \
                                                          const float4*, const float4*, float4*, float4*,        \
-                                                         float4*, float4*, cudaStream_t);                       \
+                                                         float4*, float4*, cudaStream_t, int);                  \
     template cudaError_t launch_view_luts<__half2, TABLE>(JobSrc<TABLE>, int, const skyr_lut_sizes&,            \
                                                           const float4*, const __half2*, __half2*, __half2*,    \
-                                                          __half2*, __half2*, cudaStream_t);
+                                                          __half2*, __half2*, cudaStream_t, int);
 SKYR_INST(false)
 SKYR_INST(true)
 #undef SKYR_INST

@@ -383,11 +383,14 @@ __global__ void __launch_bounds__(128, 4) cloud_render_kernel(CloudConsts C, Mat
                                                            const float* __restrict__ depth,
                                                            __half2* __restrict__ out_rgba,
                                                            float* __restrict__ out_dist,
-                                                           unsigned long long* __restrict__ counters) {
-    // 16x8 pixels per block, 8x4 per warp
+                                                           unsigned long long* __restrict__ counters,
+                                                           int tile_w, int warps_x) {
+    // a warp covers tile_w x (32 / tile_w) pixels; the block's 4 warps sit
+    // warps_x across and 4 / warps_x down (skyr_tuning)
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
-    int py = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+    int tile_h = 32 / tile_w, warps_y = 4 / warps_x;
+    int px = blockIdx.x * (tile_w * warps_x) + (warp % warps_x) * tile_w + (lane % tile_w);
+    int py = blockIdx.y * (tile_h * warps_y) + (warp / warps_x) * tile_h + (lane / tile_w);
     if (px >= C.width || py >= C.height) return;
     size_t pix = (size_t)py * C.width + px;
     float u = ((float)px + 0.5f) / (float)C.width, v = ((float)py + 0.5f) / (float)C.height;
@@ -480,14 +483,13 @@ extern "C" {
 
 }  // extern "C"
 
-namespace {
-int cloud_render_impl(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
-                      const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
-                      const skyr_cloud_textures* textures, const skyr_cloud_view* view,
-                      const skyr_lut_sizes* sizes, const void* transmittance,
-                      const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
-                      const float* blue_noise, const float* depth, void* out_rgba, float* out_distance,
-                      unsigned long long* counters) {
+namespace skyr {
+int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_parameters* atmosphere,
+                    const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                    const skyr_cloud_textures* textures, const skyr_cloud_view* view, const skyr_lut_sizes* sizes,
+                    const void* transmittance, const void* aerial_perspective_luminance,
+                    const void* aerial_perspective_transmittance, const float* blue_noise, const float* depth,
+                    void* out_rgba, float* out_distance, unsigned long long* counters) {
     if (!ctx) return set_error(SKYR_EINVAL, "null context");
     if (!atmosphere || !cloud || !material || !textures || !view || !sizes)
         return set_error(SKYR_EINVAL, "null parameter block");
@@ -511,24 +513,26 @@ int cloud_render_impl(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmospher
     AtmoConsts A;
     derive_atmo_consts(*atmosphere, A);
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
-    dim3 grid((view->width + 15) / 16, (view->height + 7) / 8);
+    const int tile_w = ctx->tuning.cloud_tile_width, warps_x = ctx->tuning.cloud_block_warps_x;
+    const int bw = tile_w * warps_x, bh = (32 / tile_w) * (4 / warps_x);
+    dim3 grid((view->width + bw - 1) / bw, (view->height + bh - 1) / bh);
     const float4* T = reinterpret_cast<const float4*>(transmittance);
     if (sizes->format == SKYR_FORMAT_RGBA16F) {
-        cloud_render_kernel<__half2><<<grid, 128, 0, ctx->stream>>>(
+        cloud_render_kernel<__half2><<<grid, 128, 0, stream>>>(
             C, M, A, T, sizes->transmittance_width, sizes->transmittance_height,
             reinterpret_cast<const __half2*>(aerial_perspective_luminance),
             reinterpret_cast<const __half2*>(aerial_perspective_transmittance), blue_noise, depth,
-            reinterpret_cast<__half2*>(out_rgba), out_distance, counters);
+            reinterpret_cast<__half2*>(out_rgba), out_distance, counters, tile_w, warps_x);
     } else {
-        cloud_render_kernel<float4><<<grid, 128, 0, ctx->stream>>>(
+        cloud_render_kernel<float4><<<grid, 128, 0, stream>>>(
             C, M, A, T, sizes->transmittance_width, sizes->transmittance_height,
             reinterpret_cast<const float4*>(aerial_perspective_luminance),
             reinterpret_cast<const float4*>(aerial_perspective_transmittance), blue_noise, depth,
-            reinterpret_cast<__half2*>(out_rgba), out_distance, counters);
+            reinterpret_cast<__half2*>(out_rgba), out_distance, counters, tile_w, warps_x);
     }
     return check_cuda(cudaGetLastError(), "cloud raymarch kernel");
 }
-}  // namespace
+}  // namespace skyr
 
 extern "C" {
 
@@ -538,9 +542,9 @@ int skyr_cloud_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmospher
                       const skyr_lut_sizes* sizes, const void* transmittance,
                       const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
                       const float* blue_noise, const float* depth, void* out_rgba, float* out_distance) {
-    return cloud_render_impl(ctx, atmosphere, cloud, material, textures, view, sizes, transmittance,
-                                    aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise,
-                                    depth, out_rgba, out_distance, nullptr);
+    return cloud_render_on(ctx, ctx ? ctx->stream : nullptr, atmosphere, cloud, material, textures, view, sizes,
+                           transmittance, aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise,
+                           depth, out_rgba, out_distance, nullptr);
 }
 
 int skyr_cloud_render_counted(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
@@ -552,9 +556,9 @@ int skyr_cloud_render_counted(skyr_ctx* ctx, const skyr_atmosphere_parameters* a
                               const float* depth, void* out_rgba, float* out_distance,
                               unsigned long long* counters) {
     if (!counters) return set_error(SKYR_EINVAL, "null counters");
-    return cloud_render_impl(ctx, atmosphere, cloud, material, textures, view, sizes, transmittance,
-                                   aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise,
-                                   depth, out_rgba, out_distance, counters);
+    return cloud_render_on(ctx, ctx ? ctx->stream : nullptr, atmosphere, cloud, material, textures, view, sizes,
+                           transmittance, aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise,
+                           depth, out_rgba, out_distance, counters);
 }
 
 

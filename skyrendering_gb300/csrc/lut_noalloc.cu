@@ -55,12 +55,14 @@ int launch_all(skyr_ctx* ctx, const LutSetJob* jobs, int n, const skyr_lut_sizes
     cudaStream_t st = ctx->stream;
     float4* t = reinterpret_cast<float4*>(T);
     S* ms = reinterpret_cast<S*>(MS);
-    if (int e = skyr::check_cuda(skyr::launch_transmittance<true>(src, n, s, t, st), "transmittance kernel")) return e;
+    if (int e = skyr::check_cuda(skyr::launch_transmittance<true>(src, n, s, t, st, ctx->tuning.transmittance_lanes),
+                                 "transmittance kernel"))
+        return e;
     if (int e = skyr::check_cuda(skyr::launch_multiscattering<S, true>(src, n, s, t, ms, st), "multiscattering kernel"))
         return e;
     return skyr::check_cuda(skyr::launch_view_luts<S, true>(src, n, s, t, ms, reinterpret_cast<S*>(svl),
                                                             reinterpret_cast<S*>(svt), reinterpret_cast<S*>(apl),
-                                                            reinterpret_cast<S*>(apt), st),
+                                                            reinterpret_cast<S*>(apt), st, ctx->tuning.view_lanes),
                             "view LUT kernel");
 }
 

@@ -253,18 +253,7 @@ constexpr int kMaxSets = 1 << 16;
 int build_jobs(skyr_ctx* ctx, const skyr_atmosphere_parameters* params, const skyr_atmosphere_render_parameters* rp,
                int n, std::vector<LutSetJob>& jobs) {
     jobs.resize(n);
-    for (int i = 0; i < n; ++i) {
-        int st = validate_atmosphere(&params[i], i);
-        if (st) return st;
-        derive_atmo_consts(params[i], jobs[i].a);
-        if (rp) {
-            st = validate_render(&rp[i], &params[i], i);
-            if (st) return st;
-            derive_view_consts(params[i], rp[i], jobs[i].v);
-        } else {
-            std::memset(&jobs[i].v, 0, sizeof(ViewConsts));
-        }
-    }
+    if (int st = skyr::derive_jobs(params, rp, n, jobs.data())) return st;
     if (n > 1) {
         int st = ensure_job_table(ctx, sizeof(LutSetJob) * n);
         if (st) return st;
@@ -281,7 +270,8 @@ int run(skyr_ctx* ctx, JobSrc<TABLE> src, int n, const skyr_lut_sizes& s, bool d
         S* MS, S* svl, S* svt, S* apl, S* apt) {
     cudaStream_t st = ctx->stream;
     if (do_base) {
-        int e = check_cuda(launch_transmittance<TABLE>(src, n, s, T, st), "transmittance kernel");
+        int e = check_cuda(launch_transmittance<TABLE>(src, n, s, T, st, ctx->tuning.transmittance_lanes),
+                           "transmittance kernel");
         if (e) return e;
         e = check_cuda(launch_multiscattering<S, TABLE>(src, n, s, T, MS, st), "multiscattering kernel");
         if (e) return e;
@@ -290,7 +280,8 @@ int run(skyr_ctx* ctx, JobSrc<TABLE> src, int n, const skyr_lut_sizes& s, bool d
         skyr_lut_sizes v = s;
         if (!svl) v.sky_view_width = v.sky_view_height = 0;
         if (!apl) v.aerial_perspective_width = v.aerial_perspective_height = v.aerial_perspective_depth = 0;
-        return check_cuda(launch_view_luts<S, TABLE>(src, n, v, T, MS, svl, svt, apl, apt, st), "view LUT kernel");
+        return check_cuda(launch_view_luts<S, TABLE>(src, n, v, T, MS, svl, svt, apl, apt, st, ctx->tuning.view_lanes),
+                          "view LUT kernel");
     }
     return SKYR_OK;
 }
@@ -334,6 +325,41 @@ int lut_entry(skyr_ctx* ctx, const skyr_atmosphere_parameters* params, const sky
 }
 
 }  // namespace
+
+namespace skyr {
+
+int derive_jobs(const skyr_atmosphere_parameters* params, const skyr_atmosphere_render_parameters* rp, int n,
+                LutSetJob* jobs) {
+    for (int i = 0; i < n; ++i) {
+        int st = validate_atmosphere(&params[i], i);
+        if (st) return st;
+        derive_atmo_consts(params[i], jobs[i].a);
+        if (rp) {
+            st = validate_render(&rp[i], &params[i], i);
+            if (st) return st;
+            derive_view_consts(params[i], rp[i], jobs[i].v);
+        } else {
+            std::memset(&jobs[i].v, 0, sizeof(ViewConsts));
+        }
+    }
+    return SKYR_OK;
+}
+
+int launch_lut_passes(skyr_ctx* ctx, const LutSetJob* table, int n, const skyr_lut_sizes& s, bool do_view, void* T,
+                      void* MS, void* svl, void* svt, void* apl, void* apt) {
+    JobSrc<true> src{table};
+    if (s.format == SKYR_FORMAT_RGBA16F)
+        return run<__half2, true>(ctx, src, n, s, true, do_view, reinterpret_cast<float4*>(T),
+                                  reinterpret_cast<__half2*>(MS), reinterpret_cast<__half2*>(svl),
+                                  reinterpret_cast<__half2*>(svt), reinterpret_cast<__half2*>(apl),
+                                  reinterpret_cast<__half2*>(apt));
+    return run<float4, true>(ctx, src, n, s, true, do_view, reinterpret_cast<float4*>(T),
+                             reinterpret_cast<float4*>(MS), reinterpret_cast<float4*>(svl),
+                             reinterpret_cast<float4*>(svt), reinterpret_cast<float4*>(apl),
+                             reinterpret_cast<float4*>(apt));
+}
+
+}  // namespace skyr
 
 extern "C" {
 

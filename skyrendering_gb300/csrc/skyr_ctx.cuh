@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/skyr.h"
+#include "../../include/skyr_batch.h"
 
 struct skyr_ctx {
     cudaStream_t stream = nullptr;
@@ -18,7 +19,17 @@ struct skyr_ctx {
     void* pt_scratch = nullptr;
     size_t pt_scratch_bytes = 0;
     int* d_status = nullptr;  // device-side error flags of bounded waits
+    // launch shapes (skyr_batch.h)
+    skyr_tuning tuning{8, 8, 8, 2};
+    // internal streams and events that fan a call's independent launches out
+    // from the context's stream and join them back (created on first use)
+    static constexpr int kAux = 4;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t fork_event = nullptr;
+    cudaEvent_t join_event[kAux] = {};
 };
+
+struct LutSetJob;  // per-set kernel constants (skyr_internal.cuh)
 
 namespace skyr {
 int set_error(int code, const char* fmt, ...);
@@ -33,4 +44,21 @@ int ensure_pt_scratch(skyr_ctx* ctx, size_t bytes);
 int validate_atmosphere(const skyr_atmosphere_parameters* p, int i);
 int validate_render(const skyr_atmosphere_render_parameters* r, const skyr_atmosphere_parameters* p, int i);
 int validate_sizes(const skyr_lut_sizes* s, bool views);
+// Validate and derive the per-set kernel constants of n LUT sets (no upload).
+int derive_jobs(const skyr_atmosphere_parameters* params, const skyr_atmosphere_render_parameters* rp, int n,
+                LutSetJob* jobs);
+// Enqueue the LUT passes for n sets whose constants are in a device table
+// (the context's tuning picks the lanes); the outputs as skyr_update_lut_set.
+int launch_lut_passes(skyr_ctx* ctx, const LutSetJob* table, int n, const skyr_lut_sizes& s, bool do_view, void* T,
+                      void* MS, void* svl, void* svt, void* apl, void* apt);
+// Cloud raymarch of one view on `stream` (cloud.cu); the launch shape from the
+// context's tuning.
+int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_parameters* atmosphere,
+                    const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                    const skyr_cloud_textures* textures, const skyr_cloud_view* view, const skyr_lut_sizes* sizes,
+                    const void* transmittance, const void* aerial_perspective_luminance,
+                    const void* aerial_perspective_transmittance, const float* blue_noise, const float* depth,
+                    void* out_rgba, float* out_distance, unsigned long long* counters);
+// Create the internal streams / events of a context if needed.
+int ensure_aux_streams(skyr_ctx* ctx);
 }  // namespace skyr

@@ -15,6 +15,14 @@ void ctx_release_resources(skyr_ctx* ctx) {
     ctx->cloud_scratch = ctx->pt_scratch = nullptr;
     ctx->d_status = nullptr;
     ctx->cloud_scratch_bytes = ctx->pt_scratch_bytes = 0;
+    for (int k = 0; k < skyr_ctx::kAux; ++k) {
+        if (ctx->aux[k]) cudaStreamDestroy(ctx->aux[k]);
+        if (ctx->join_event[k]) cudaEventDestroy(ctx->join_event[k]);
+        ctx->aux[k] = nullptr;
+        ctx->join_event[k] = nullptr;
+    }
+    if (ctx->fork_event) cudaEventDestroy(ctx->fork_event);
+    ctx->fork_event = nullptr;
 }
 
 // Grow-only per-context scratch of the path tracer (its per-frame work counters).
@@ -75,6 +83,7 @@ size_t skyr_struct_size_ext(int which) {
         case 11: return sizeof(skyr_mlp_hparams);
         case 12: return sizeof(skyr_feature_volume);
         case 13: return sizeof(skyr_surrogate_parameters);
+        case 14: return sizeof(skyr_tuning);
         default: return 0;
     }
 }

@@ -144,19 +144,16 @@ def frame_camera() -> Camera:
     return Camera()
 
 
-def batched_lut_sets(n: int = 256, seed: int = SEED):
-    """n parameter sets: Rayleigh, Mie and ozone coefficients each scaled by a
-    log-uniform factor in [0.5, 1.5] of the Earth-like set, Mie g ~ U[0.6, 0.9];
-    each set paired with a view at altitude U[0, 10] km, sun zenith U[0, 95] deg,
-    sun azimuth U[0, 360) deg."""
+def _batched_sets(n: int, seed: int):
+    """(params, cameras, sun zeniths, sun azimuths) of the batched workload."""
     rng = np.random.default_rng(seed)
     base = earth_like_atmosphere()
     params = (_abi.AtmosphereParameters * n)()
-    renders = (_abi.AtmosphereRenderParameters * n)()
+    cams, zen, azi = [], [], []
     lo, hi = math.log(0.5), math.log(1.5)
+    import ctypes
     for i in range(n):
         p = params[i]
-        import ctypes
         ctypes.memmove(ctypes.byref(p), ctypes.byref(base), ctypes.sizeof(base))
         kr, km, ko = np.exp(rng.uniform(lo, hi, size=3))
         p.rayleigh_scattering_scale = base.rayleigh_scattering_scale * kr
@@ -164,10 +161,45 @@ def batched_lut_sets(n: int = 256, seed: int = SEED):
         p.mie_absorption_scale = base.mie_absorption_scale * km
         p.ozone_absorption_scale = base.ozone_absorption_scale * ko
         p.mie_phase_g = rng.uniform(0.6, 0.9)
-        cam = Camera(position=(0.0, float(rng.uniform(0.0, 10.0)), 0.0), yaw=float(rng.uniform(0, 360)),
-                     pitch=float(rng.uniform(-5.0, 30.0)))
-        renders[i] = render_parameters(cam, float(rng.uniform(0.0, 95.0)), float(rng.uniform(0.0, 360.0)))
+        cams.append(Camera(position=(0.0, float(rng.uniform(0.0, 10.0)), 0.0), yaw=float(rng.uniform(0, 360)),
+                           pitch=float(rng.uniform(-5.0, 30.0))))
+        zen.append(float(rng.uniform(0.0, 95.0)))
+        azi.append(float(rng.uniform(0.0, 360.0)))
+    return params, cams, zen, azi
+
+
+def batched_lut_sets(n: int = 256, seed: int = SEED):
+    """n parameter sets: Rayleigh, Mie and ozone coefficients each scaled by a
+    log-uniform factor in [0.5, 1.5] of the Earth-like set, Mie g ~ U[0.6, 0.9];
+    each set paired with a view at altitude U[0, 10] km, sun zenith U[0, 95] deg,
+    sun azimuth U[0, 360) deg."""
+    params, cams, zen, azi = _batched_sets(n, seed)
+    renders = (_abi.AtmosphereRenderParameters * n)()
+    for i in range(n):
+        renders[i] = render_parameters(cams[i], zen[i], azi[i])
     return params, renders
+
+
+VIEW_SIZES = ((640, 360), (1280, 720), (1920, 1080), (3840, 2160))
+
+
+def batched_frame(n_sets: int = 256, n_views: int = 64, seed: int = SEED):
+    """The batched workload: n_sets parameter sets (as batched_lut_sets) and
+    n_views views of sizes drawn uniformly from VIEW_SIZES; view i looks
+    through the camera and sun of set i (its aspect ratio set to the view's).
+    Returns (params, renders, views, set_of_view)."""
+    params, cams, zen, azi = _batched_sets(n_sets, seed)
+    rng = np.random.default_rng(seed + 1)
+    views = (_abi.CloudView * n_views)()
+    for i in range(n_views):
+        w, h = VIEW_SIZES[int(rng.integers(len(VIEW_SIZES)))]
+        c = cams[i]
+        cams[i] = Camera(position=c.position, yaw=c.yaw, pitch=c.pitch, fovy=60.0, width=w, height=h)
+        views[i] = frame_view(cams[i], zen[i], azi[i])
+    renders = (_abi.AtmosphereRenderParameters * n_sets)()
+    for i in range(n_sets):
+        renders[i] = render_parameters(cams[i], zen[i], azi[i])
+    return params, renders, views, list(range(n_views))
 
 
 # ---------------------------------------------------------------------------
