@@ -4,6 +4,9 @@ times on one stream, synchronise and exit 0.
     python -m skyrendering_gb300.profile_cases luts  --iters 3
     python -m skyrendering_gb300.profile_cases cloud --iters 3
     python -m skyrendering_gb300.profile_cases pt    --iters 2 [--global-majorant] [--size 1024] [--frames 4]
+    python -m skyrendering_gb300.profile_cases surrogate --iters 3 [--size 1024]
+    python -m skyrendering_gb300.profile_cases lattice --iters 2
+    python -m skyrendering_gb300.profile_cases mlp --iters 3
 
 Cases (seeded synthetic inputs from workloads.py):
   luts   the plain LUT set (T 256x64, MS 32x32, SV 192x108, AP 32^3) of the
@@ -13,6 +16,11 @@ Cases (seeded synthetic inputs from workloads.py):
          brick majorants and the LUT set once, then `frames` path-traced
          frames of the size x size view per iteration, in one launch (128
          bounces, HG 0.857).
+  surrogate  the committed network's 128-step surrogate raymarch of that grid
+         (size x size, feature lattice built once);
+  lattice the feature lattice of that grid for the scene's sun;
+  mlp    one Adam training step of the network on a 16384-sample batch of
+         seeded random records.
 The per-iteration CUDA-event time is printed for orientation; it is not a
 benchmark figure (bench.py is).
 """
@@ -66,9 +74,40 @@ def pt_case(ctx, size: int, global_majorant: bool, frames: int):
     return lambda: tracer.render(atmo, luts, frames)
 
 
+def surrogate_case(ctx, size: int, what: str):
+    from . import surrogate as S
+    from . import surrogate_train as T
+
+    sc = T.Scene(ctx, size=size)
+    grid = sc.grid(W.SEED)
+    if what == "lattice":
+        return lambda: sc.lattice(grid)
+    fv = sc.lattice(grid)
+    model = S.load_model(S.MODEL_PATH)
+    net = model.packed(ctx)
+    table = torch.from_numpy(model.error_table).cuda()
+    sp = S.parameters(error_table=table)
+    out = torch.empty((size, size, 4), dtype=torch.float32, device="cuda")
+    err = torch.empty((size, size), dtype=torch.float32, device="cuda")
+    keep = (table, fv)
+    return lambda: (S.render(ctx, sc.atmo, sc.cloud, grid, sc.pt, sc.view, sc.sizes, sc.luts, fv, net, sp, out, err),
+                    keep)
+
+
+def mlp_case(ctx):
+    from . import mlp
+
+    g = torch.Generator(device="cuda").manual_seed(5)
+    x = torch.rand((16384, mlp.INPUTS), device="cuda", generator=g)
+    rec = mlp.to_records(x)
+    t = torch.rand((16384, 3), device="cuda", generator=g) + 0.5
+    tr = mlp.Trainer(ctx, mlp.init_params(1), mlp.hparams())
+    return lambda: (tr.step(rec, t), tr)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["luts", "cloud", "pt"])
+    ap.add_argument("case", choices=["luts", "cloud", "pt", "surrogate", "lattice", "mlp"])
     ap.add_argument("--iters", type=int, default=3)
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--global-majorant", action="store_true")
@@ -81,8 +120,12 @@ def main(argv=None):
         step = lut_case(ctx, W.frame_camera())[-1]
     elif a.case == "cloud":
         step = cloud_case(ctx)
-    else:
+    elif a.case == "pt":
         step = pt_case(ctx, a.size, a.global_majorant, a.frames)
+    elif a.case in ("surrogate", "lattice"):
+        step = surrogate_case(ctx, a.size, a.case)
+    else:
+        step = mlp_case(ctx)
     torch.cuda.synchronize()
     for i in range(a.iters):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
