@@ -11,13 +11,18 @@
  * Network inputs (one feature record, SKYR_MLP_RECORD bf16):
  *   0       extinction at the point / sigma_ref
  *   1..32   extinction at the point + d_k * sun, d_k = span * 0.01 * 1000^(k/31)
- *   33..40  extinction at the point + 0.1 * span * (+-1, +-1, +-1) / sqrt(3)
+ *   33..40  extinction at the 8 corners of a cube around the point whose
+ *           corners lie 0.1 * span away, with axes (v, u, w): v the view
+ *           direction, u the sun's component perpendicular to v, w = v x u;
+ *           corner j is +-1/sqrt(3) along v, u, w by bits 0, 1, 2 of j
  *   41      height of the point within the grid box, 0 (bottom) .. 1 (top)
  *   42      cos(view direction, sun direction)
  *   43..47  zero
- * span = the grid's longest edge.  Features 0..41 are taken at the nodes of a
- * coarse lattice (every `stride` voxels) and interpolated trilinearly, the same
- * way for training points and for the raymarch.
+ * span = the grid's longest edge; extinctions are divided by sigma_ref.
+ * Features 0..32 and 41 depend on the position only: they are taken at the
+ * nodes of a coarse lattice (every `stride` voxels, where 33..40 are zero) and
+ * interpolated trilinearly; 33..40 are looked up in the grid per sample.  Both
+ * are done the same way for training points and for the raymarch.
  */
 #ifndef SKYR_SURROGATE_H_
 #define SKYR_SURROGATE_H_

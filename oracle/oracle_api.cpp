@@ -588,6 +588,24 @@ int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_c
             for (int k = 0; k < 42; ++k) f[k] += w * orc::bf16_to_float(lattice_rec[node * 48 + k]);
         }
     };
+    // features 33..40: the view-oriented cube corners (skyr_surrogate.h)
+    const double span = (double)gd->voxel_size * std::max(gd->nx, std::max(gd->ny, gd->nz));
+    const double nbr = 0.1 * span / std::sqrt(3.0), inv_ref = 1.0 / fv->sigma_ref;
+    auto view_neighbours = [&](orc::V3<double> x, orc::V3<double> v, double f[42]) {
+        orc::V3<double> u = sun - v * orc::dot(v, sun);
+        double l2 = orc::dot(u, u);
+        if (l2 < 1e-8) {
+            orc::V3<double> b1;
+            orc::PathTracerOracle<double>::basis(v, u, b1);
+        } else {
+            u = u / std::sqrt(l2);
+        }
+        orc::V3<double> w = orc::cross(v, u);
+        for (int j = 0; j < 8; ++j) {
+            orc::V3<double> o = v * ((j & 1) ? nbr : -nbr) + u * ((j & 2) ? nbr : -nbr) + w * ((j & 4) ? nbr : -nbr);
+            f[33 + j] = PT.grid_sigma(x + o) * inv_ref;
+        }
+    };
     const double gb = pt->back_phase_g, gf = pt->forward_phase_g, ratio = pt->forward_scattering_ratio;
     auto hg = [](double c, double g) { return (0.25 / orc::kPi) * (1 - g * g) / std::pow(1 + g * g - 2 * g * c, 1.5); };
     parallel_for(n, threads, [&](int i) {
@@ -613,6 +631,7 @@ int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_c
                 if (!(sigma > 0)) continue;
                 double f[42], tau;
                 lattice(x, f, tau);
+                view_neighbours(x, dir, f);
                 orc::V3<double> ms(0.0);
                 if (use_network) {
                     double rec[43], y[3];

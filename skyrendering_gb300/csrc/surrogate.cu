@@ -115,6 +115,30 @@ __device__ __forceinline__ void store_record(uint4* dst, const float (&f)[kFeat]
     }
 }
 
+// Features 33..40: extinction / sigma_ref at the 8 corners of a cube whose
+// corners lie `dist` from x, with axes (v, u, w): v the view direction, u the
+// sun's component perpendicular to v (any perpendicular when the two are
+// parallel), w = v x u.  Corner j takes +dist/sqrt(3) along v, u, w where bit
+// 0, 1, 2 of j is set, -dist/sqrt(3) where it is not.
+__device__ __forceinline__ void view_neighbours(const PtConsts& P, float3 x, float3 v, float3 sun, float dist,
+                                                float inv_ref, float (&f)[kFeat]) {
+    float3 u = sun - v * dot3(v, sun);
+    float l2 = dot3(u, u);
+    if (l2 < 1e-8f) {
+        float3 b1;
+        onb(v, u, b1);
+    } else {
+        u = u * rsqrtf(l2);
+    }
+    float3 w = f3(v.y * u.z - v.z * u.y, v.z * u.x - v.x * u.z, v.x * u.y - v.y * u.x);
+    const float r = dist * 0.57735026918962576f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        float3 o = v * ((j & 1) ? r : -r) + u * ((j & 2) ? r : -r) + w * ((j & 4) ? r : -r);
+        f[33 + j] = grid_sigma(P, x + o) * inv_ref;
+    }
+}
+
 struct LatticeBuild {
     float dist[32];  // sun sample distances
     float nbr;       // neighbour radius
@@ -135,12 +159,9 @@ __global__ void __launch_bounds__(128) feature_lattice_kernel(PtConsts P, GridBo
     f[0] = grid_sigma(P, x) * Q.inv_sigma_ref;
 #pragma unroll 4
     for (int k = 0; k < 32; ++k) f[1 + k] = grid_sigma(P, x + L.sun * Q.dist[k]) * Q.inv_sigma_ref;
-    const float r = Q.nbr * 0.57735026918962576f;
+    // features 33..40 depend on the view direction: filled per sample (view_neighbours)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        float3 o = f3((j & 1) ? r : -r, (j & 2) ? r : -r, (j & 4) ? r : -r);
-        f[33 + j] = grid_sigma(P, x + o) * Q.inv_sigma_ref;
-    }
+    for (int j = 0; j < 8; ++j) f[33 + j] = 0.f;
     f[41] = fminf(fmaxf((x.z - B.lo.z) / (B.hi.z - B.lo.z), 0.f), 1.f);
     store_record(rec + node * 6, f, 0.f);
     // optical depth to the sun: midpoint rule to the exit of the grid box
@@ -199,14 +220,15 @@ __global__ void __launch_bounds__(128) sample_points_kernel(PtConsts P, GridBox 
     o6[3] = d.x; o6[4] = d.y; o6[5] = d.z;
 }
 
-__global__ void __launch_bounds__(128) records_kernel(Lattice L, const float* __restrict__ pts, int n,
-                                                      uint4* __restrict__ rec) {
+__global__ void __launch_bounds__(128) records_kernel(Lattice L, PtConsts P, float nbr, float inv_ref,
+                                                      const float* __restrict__ pts, int n, uint4* __restrict__ rec) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* q = pts + 6 * (size_t)i;
     float3 x = f3(q[0], q[1], q[2]), d = f3(q[3], q[4], q[5]);
     float f[kFeat];
     lattice_at<true>(L, x, f);
+    view_neighbours(P, x, d, L.sun, nbr, inv_ref, f);
     store_record(rec + (size_t)i * 6, f, dot3(d, L.sun));
 }
 
@@ -215,6 +237,7 @@ struct RenderConsts {
     float network_error, min_t;
     float g_fwd, g_back, ratio;
     const float* error_table;
+    float nbr, inv_ref;  // view-neighbour distance and 1 / sigma_ref
 };
 
 constexpr int kBins = SKYR_SURROGATE_ERROR_BINS;
@@ -288,6 +311,7 @@ __global__ void __launch_bounds__(128, 4) surrogate_render_kernel(CloudConsts C,
             if (need) {
                 float f[kFeat];
                 tau = lattice_at<true>(L, x, f);
+                view_neighbours(P, x, dir, C.sun, R.nbr, R.inv_ref, f);
                 store_record(row, f, mu);
                 if (R.error_table) {
                     float near_sun = 0.f;
@@ -484,7 +508,8 @@ int skyr_surrogate_records(skyr_ctx* ctx, const skyr_density_grid* grid, const s
     if (int e = lattice_setup(grid, fv, L)) return e;
     if (n == 0) return SKYR_OK;
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
-    records_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(L, points, n, reinterpret_cast<uint4*>(records));
+    records_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(L, P, 0.1f * B.span, 1.f / fv->sigma_ref, points, n,
+                                                           reinterpret_cast<uint4*>(records));
     return check_cuda(cudaGetLastError(), "records kernel");
 }
 
@@ -544,6 +569,8 @@ int skyr_surrogate_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmos
     R.g_back = pt->back_phase_g;
     R.ratio = pt->forward_scattering_ratio;
     R.error_table = sp->error_table;
+    R.nbr = 0.1f * B.span;
+    R.inv_ref = 1.f / fv->sigma_ref;
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     auto launch = [&](auto tag) -> int {
         using S = decltype(tag);

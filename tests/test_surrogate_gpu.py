@@ -11,7 +11,7 @@
   the committed network (BF16 rounding points mirrored): mean relative error
   of the luminance <= 1e-3, transmittance 1e-5;
 * accuracy: on the 512x640x352 evaluation cloud at 128^2 the network image is
-  within 12 % relative L1 of a 8192-spp path-traced reference while single
+  within 8 % relative L1 of a 8192-spp path-traced reference while single
   scattering alone is >= 80 % off (what the trained network gains).
 """
 import ctypes as C
@@ -60,6 +60,19 @@ def _box_exit(lo, hi, x, d):
     return t1
 
 
+def _view_neighbours(grid, x, v, sun, sigma_ref):
+    """Features 33..40 (skyr_surrogate.h): extinction at the view-oriented cube corners."""
+    g = grid.struct
+    span = g.voxel_size * max(g.nx, g.ny, g.nz)
+    r = 0.1 * span / math.sqrt(3.0)
+    u = sun[None, :] - v * (v @ sun)[:, None]
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    w = np.cross(v, u)
+    pts = [x + v * (r if j & 1 else -r) + u * (r if j & 2 else -r) + w * (r if j & 4 else -r) for j in range(8)]
+    sig = orc.grid_sigma(g, grid.data.cpu().numpy(), np.concatenate(pts)).reshape(8, -1).T
+    return sig / sigma_ref
+
+
 def test_lattice_matches_oracle(small):
     sc, grid, fv = small
     g = grid.struct
@@ -80,14 +93,11 @@ def test_lattice_matches_oracle(small):
     pts = [x]
     for k in range(32):
         pts.append(x + sun * (span * 0.01 * 1000.0 ** (k / 31.0)))
-    r = 0.1 * span / math.sqrt(3.0)
-    for j in range(8):
-        o = np.array([r if j & 1 else -r, r if j & 2 else -r, r if j & 4 else -r])
-        pts.append(x + o)
-    sig = orc.grid_sigma(g, data, np.concatenate(pts)).reshape(41, -1).T / st.sigma_ref
+    sig = orc.grid_sigma(g, data, np.concatenate(pts)).reshape(33, -1).T / st.sigma_ref
     hi = org + np.array(SMALL) * g.voxel_size
     alt = np.clip((x[:, 2] - org[2]) / (hi[2] - org[2]), 0, 1)
-    feat = np.concatenate([sig, alt[:, None]], 1)
+    # 33..40 depend on the view direction: zero in the lattice
+    feat = np.concatenate([sig, np.zeros((len(x), 8)), alt[:, None]], 1)
     got = rec[idx, :42].astype(np.uint32) << 16
     got = got.view(np.float32)
     np.testing.assert_allclose(got, _bf16(feat), rtol=1e-2, atol=1e-3)
@@ -121,7 +131,9 @@ def test_records_interpolate_lattice(ctx, small):
         w = np.prod(np.where(d, fr, 1 - fr), 1)
         node = ((i0[:, 2] + d[2]) * st.ny + (i0[:, 1] + d[1])) * st.nx + (i0[:, 0] + d[0])
         f += w[:, None] * lat[node]
-    f[:, 42] = p[:, 3:] @ np.array(st.sun[:])
+    sun = np.array(st.sun[:], dtype=np.float64)
+    f[:, 42] = p[:, 3:] @ sun
+    f[:, 33:41] = _view_neighbours(grid, p[:, :3], p[:, 3:], sun, st.sigma_ref)
     got = rec.float().cpu().numpy()
     np.testing.assert_allclose(got, _bf16(f), rtol=1e-2, atol=2e-3)
 
@@ -206,9 +218,9 @@ def test_surrogate_accuracy_and_network_gain(ctx):
     ctx.check_status()
     e_net, e_ss = S.relative_l1(with_net, ref), S.relative_l1(ss_only, ref)
     print(f"relative L1 vs 8192 spp: network {e_net:.4f}, single scattering only {e_ss:.4f}")
-    assert e_net <= 0.12
+    assert e_net <= 0.08
     assert e_ss >= 0.8
-    assert e_ss >= 5 * e_net
+    assert e_ss >= 10 * e_net
     # the view transmittance is the same with or without the network and matches the path tracer's alpha
     torch.testing.assert_close(with_net[..., 3], ss_only[..., 3])
     assert float((with_net[..., 3] - ref[..., 3]).abs().mean()) < 2e-3
