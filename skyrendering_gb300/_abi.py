@@ -386,11 +386,12 @@ _SIGNATURES.update({
 # skyr_batch.h
 # ---------------------------------------------------------------------------
 SKYR_CLOUD_TILE_CANDIDATES = 12
+SKYR_CLOUD_TUNE_CANDIDATES = 24
 
 
 class Tuning(C.Structure):
     _fields_ = [("transmittance_lanes", C.c_int), ("view_lanes", C.c_int), ("cloud_tile_width", C.c_int),
-                ("cloud_block_warps_x", C.c_int)]
+                ("cloud_block_warps_x", C.c_int), ("cloud_blocks_per_sm", C.c_int)]
 
 
 STRUCT_IDS.update({14: Tuning})

@@ -17,6 +17,9 @@ from .atmosphere import Context, LutSet, _ptr
 
 TILE_CANDIDATES = ((4, 1), (4, 2), (4, 4), (8, 1), (8, 2), (8, 4), (16, 1), (16, 2), (16, 4), (32, 1), (32, 2),
                    (32, 4))
+OCCUPANCY_CANDIDATES = (5, 6)
+# (tile width, block warps x, blocks per SM) in the order of skyr_autotune_cloud's times
+CLOUD_CANDIDATES = tuple((w, bx, occ) for occ in OCCUPANCY_CANDIDATES for w, bx in TILE_CANDIDATES)
 
 
 def tuning(ctx: Context) -> _abi.Tuning:
@@ -50,9 +53,9 @@ def autotune_luts(ctx: Context, params, renders, n: int, sizes, luts: LutSet, re
 
 def autotune_cloud(ctx: Context, atmosphere, cloud, material, textures, view, sizes, luts: LutSet, blue_noise,
                    out_rgba, out_dist, reps: int = 3):
-    """(chosen tuning, times ms per TILE_CANDIDATES entry)."""
+    """(chosen tuning, times ms per CLOUD_CANDIDATES entry)."""
     best = _abi.Tuning()
-    times = (C.c_float * _abi.SKYR_CLOUD_TILE_CANDIDATES)()
+    times = (C.c_float * _abi.SKYR_CLOUD_TUNE_CANDIDATES)()
     _abi.call("skyr_autotune_cloud", ctx.handle, C.byref(atmosphere), C.byref(cloud), C.byref(material),
               C.byref(textures), C.byref(view), C.byref(sizes), _ptr(luts.transmittance),
               _ptr(luts.aerial_perspective_luminance), _ptr(luts.aerial_perspective_transmittance), _ptr(blue_noise),

@@ -48,6 +48,8 @@ constexpr int kTileCandidates[SKYR_CLOUD_TILE_CANDIDATES][2] = {
     {4, 1}, {4, 2}, {4, 4}, {8, 1}, {8, 2}, {8, 4}, {16, 1}, {16, 2}, {16, 4}, {32, 1}, {32, 2}, {32, 4}};
 constexpr int kLaneCandidates[3] = {4, 8, 16};
 
+constexpr int kOccupancyCandidates[2] = {5, 6};
+
 bool valid_lanes(int l) { return l == 4 || l == 8 || l == 16; }
 bool valid_tile(int w, int bx) { return (w == 4 || w == 8 || w == 16 || w == 32) && (bx == 1 || bx == 2 || bx == 4); }
 
@@ -77,7 +79,7 @@ extern "C" {
 
 int skyr_tuning_default(skyr_tuning* t) {
     if (!t) return set_error(SKYR_EINVAL, "null tuning");
-    *t = skyr_tuning{8, 8, 8, 2};
+    *t = skyr_tuning{8, 8, 8, 2, 5};
     return SKYR_OK;
 }
 
@@ -87,6 +89,8 @@ int skyr_ctx_set_tuning(skyr_ctx* ctx, const skyr_tuning* t) {
         return set_error(SKYR_EINVAL, "lanes must be 4, 8 or 16");
     if (!valid_tile(t->cloud_tile_width, t->cloud_block_warps_x))
         return set_error(SKYR_EINVAL, "cloud tile width must be 4, 8, 16 or 32 and block warps 1, 2 or 4");
+    if (t->cloud_blocks_per_sm != 5 && t->cloud_blocks_per_sm != 6)
+        return set_error(SKYR_EINVAL, "cloud blocks per SM must be 5 or 6");
     ctx->tuning = *t;
     return SKYR_OK;
 }
@@ -242,11 +246,13 @@ int skyr_autotune_cloud(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosph
     if (!ctx || !best) return set_error(SKYR_EINVAL, "null argument");
     if (reps < 1 || reps > 1000) return set_error(SKYR_EINVAL, "reps must be in [1, 1000]");
     const skyr_tuning start = ctx->tuning;
-    float tt[SKYR_CLOUD_TILE_CANDIDATES] = {};
+    float tt[SKYR_CLOUD_TUNE_CANDIDATES] = {};
     int best_i = -1, st = SKYR_OK;
-    for (int i = 0; i < SKYR_CLOUD_TILE_CANDIDATES && !st; ++i) {
-        ctx->tuning.cloud_tile_width = kTileCandidates[i][0];
-        ctx->tuning.cloud_block_warps_x = kTileCandidates[i][1];
+    for (int i = 0; i < SKYR_CLOUD_TUNE_CANDIDATES && !st; ++i) {
+        const int* tile = kTileCandidates[i % SKYR_CLOUD_TILE_CANDIDATES];
+        ctx->tuning.cloud_tile_width = tile[0];
+        ctx->tuning.cloud_block_warps_x = tile[1];
+        ctx->tuning.cloud_blocks_per_sm = kOccupancyCandidates[i / SKYR_CLOUD_TILE_CANDIDATES];
         st = time_launches(ctx, reps, [&]() {
             return cloud_render_on(ctx, ctx->stream, atmosphere, cloud, material, textures, view, sizes, transmittance,
                                    aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise, nullptr,
@@ -256,8 +262,9 @@ int skyr_autotune_cloud(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosph
     }
     ctx->tuning = start;
     if (st) return st;
-    ctx->tuning.cloud_tile_width = kTileCandidates[best_i][0];
-    ctx->tuning.cloud_block_warps_x = kTileCandidates[best_i][1];
+    ctx->tuning.cloud_tile_width = kTileCandidates[best_i % SKYR_CLOUD_TILE_CANDIDATES][0];
+    ctx->tuning.cloud_block_warps_x = kTileCandidates[best_i % SKYR_CLOUD_TILE_CANDIDATES][1];
+    ctx->tuning.cloud_blocks_per_sm = kOccupancyCandidates[best_i / SKYR_CLOUD_TILE_CANDIDATES];
     if (times_ms) std::memcpy(times_ms, tt, sizeof(tt));
     *best = ctx->tuning;
     return SKYR_OK;

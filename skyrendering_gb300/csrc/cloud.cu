@@ -8,6 +8,7 @@
 // cancellation-free FP32 forms; all frame derivations are done on the host in
 // double.
 #include <cmath>
+#include <type_traits>
 #include <cstring>
 
 #include "atmosphere_kernels.cuh"
@@ -373,9 +374,11 @@ __device__ __forceinline__ void shell_intersect(const CloudConsts& C, float mu, 
     }
 }
 
-// counters (optional): the frame's raymarch samples and density evaluations
-template <class S>
-__global__ void __launch_bounds__(128, 4) cloud_render_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
+// counters (optional): the frame's raymarch samples and density evaluations.
+// MINB: resident blocks per SM the register budget is cut for (a tuning
+// choice, skyr_tuning::cloud_blocks_per_sm).
+template <class S, int MINB>
+__global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
                                                            const float4* __restrict__ tlut, int tw, int th,
                                                            const S* __restrict__ ap_lum,
                                                            const S* __restrict__ ap_trans,
@@ -517,18 +520,21 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
     const int bw = tile_w * warps_x, bh = (32 / tile_w) * (4 / warps_x);
     dim3 grid((view->width + bw - 1) / bw, (view->height + bh - 1) / bh);
     const float4* T = reinterpret_cast<const float4*>(transmittance);
-    if (sizes->format == SKYR_FORMAT_RGBA16F) {
-        cloud_render_kernel<__half2><<<grid, 128, 0, stream>>>(
+    auto launch = [&](auto tag, auto minb) {
+        using S = decltype(tag);
+        cloud_render_kernel<S, decltype(minb)::value><<<grid, 128, 0, stream>>>(
             C, M, A, T, sizes->transmittance_width, sizes->transmittance_height,
-            reinterpret_cast<const __half2*>(aerial_perspective_luminance),
-            reinterpret_cast<const __half2*>(aerial_perspective_transmittance), blue_noise, depth,
+            reinterpret_cast<const S*>(aerial_perspective_luminance),
+            reinterpret_cast<const S*>(aerial_perspective_transmittance), blue_noise, depth,
             reinterpret_cast<__half2*>(out_rgba), out_distance, counters, tile_w, warps_x);
+    };
+    const bool half = sizes->format == SKYR_FORMAT_RGBA16F;
+    if (ctx->tuning.cloud_blocks_per_sm == 6) {
+        if (half) launch(__half2{}, std::integral_constant<int, 6>{});
+        else launch(float4{}, std::integral_constant<int, 6>{});
     } else {
-        cloud_render_kernel<float4><<<grid, 128, 0, stream>>>(
-            C, M, A, T, sizes->transmittance_width, sizes->transmittance_height,
-            reinterpret_cast<const float4*>(aerial_perspective_luminance),
-            reinterpret_cast<const float4*>(aerial_perspective_transmittance), blue_noise, depth,
-            reinterpret_cast<__half2*>(out_rgba), out_distance, counters, tile_w, warps_x);
+        if (half) launch(__half2{}, std::integral_constant<int, 5>{});
+        else launch(float4{}, std::integral_constant<int, 5>{});
     }
     return check_cuda(cudaGetLastError(), "cloud raymarch kernel");
 }

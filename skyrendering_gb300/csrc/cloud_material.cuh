@@ -50,48 +50,56 @@ __device__ __forceinline__ float sample_sigma_t(const MaterialConsts& M, float3 
     }
 }
 
-// Material0 and Voxel need the camera position for the LOD of a displaced /
-// arbitrary point; they are evaluated here.
+// Material0 (VolumetricCloudDefaultMaterial0.glsl:9-32) and Voxel need the
+// camera position for the LOD of a displaced / arbitrary point.  Both are kept
+// out of line: they hold many texture filters (Material0: eight) that would
+// otherwise be inlined at every density call site of the raymarch, whose hot
+// loop the usual Material1 / Minimal configurations run.
+static __device__ __noinline__ float sigma_t_material0(const CloudConsts& C, const MaterialConsts& M, float3 p,
+                                                      float h01, float dist_to_cam) {
+    float lg = __log2f(dist_to_cam);
+    float u = fmaf(p.x, M.cloud_map.frequency, M.cloud_map.bias_x);
+    float v = fmaf(p.y, M.cloud_map.frequency, M.cloud_map.bias_y);
+    float lod = __log2f(M.cloud_map.k_lod) + lg + M.lod_bias;
+    float cr = dtex_sample(M.cloud_map_tex, 0, u, v, 0.f, lod, M.min2d);
+    float cg = dtex_sample(M.cloud_map_tex, 1, u, v, 0.f, lod, M.min2d);
+    float xu = fmaf(p.x, M.displacement.frequency, M.displacement.bias_x);
+    float xv = fmaf(p.y, M.displacement.frequency, M.displacement.bias_y);
+    float xw = p.z * M.displacement.frequency;
+    float xl = __log2f(M.displacement.k_lod) + lg + M.lod_bias;
+    float3 disp;
+    disp.x = dtex_sample(M.displacement_tex, 0, xu, xv, 0.f, xl, M.mindisp) +
+             dtex_sample(M.displacement_tex, 2, xu, xw, 0.f, xl, M.mindisp);
+    disp.y = dtex_sample(M.displacement_tex, 1, xu, xv, 0.f, xl, M.mindisp);
+    disp.z = dtex_sample(M.displacement_tex, 3, xu, xw, 0.f, xl, M.mindisp);
+    float3 q = p + disp * M.m0_disp_scale;
+    float3 dq = q - C.cam;
+    float dl = __log2f(sqrtf(dot3(dq, dq)));
+    float du = fmaf(q.x, M.detail.frequency, M.detail.bias_x);
+    float dv = fmaf(q.y, M.detail.frequency, M.detail.bias_y);
+    float dw = q.z * M.detail.frequency;
+    float dt = dtex_sample(M.detail_tex, 0, du, dv, dw, __log2f(M.detail.k_lod) + dl + M.lod_bias, M.min3d);
+    dt = fmaf(dt, M.m0_detail_x, M.m0_detail_y);
+    // CalHeightMask (VolumetricCloudDefaultMaterial0.glsl:9-12)
+    float hit = clamp01(h01 / cg);
+    float mask = clamp01(hit * (hit - 1.f) * -4.f);
+    return clamp01((cr * mask - dt) / (1.f - dt)) * h01 * M.density;
+}
+
+static __device__ __noinline__ float sigma_t_voxel(const MaterialConsts& M, float3 p, float h01, float dist_to_cam) {
+    // VolumetricCloudMaterialVoxel.glsl:12-16
+    float u = fmaf(p.x, M.vx_freq_x, M.vx_bias_x);
+    float v = fmaf(p.y, M.vx_freq_y, M.vx_bias_y);
+    float lod = __log2f(M.vx_k_lod * dist_to_cam) + M.lod_bias;
+    return dtex_sample(M.voxel_tex, 0, u, v, h01, lod, SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST) * M.density;
+}
+
 __device__ __forceinline__ float sigma_t(const CloudConsts& C, const MaterialConsts& M, float3 p, float h01,
                                          float dist_to_cam) {
     if (M.type == SKYR_MATERIAL_DEFAULT1 || M.type == SKYR_MATERIAL_MINIMAL)
         return sample_sigma_t(M, p, h01, dist_to_cam);
-    if (M.type == SKYR_MATERIAL_DEFAULT0) {
-        float lg = __log2f(dist_to_cam);
-        float u = fmaf(p.x, M.cloud_map.frequency, M.cloud_map.bias_x);
-        float v = fmaf(p.y, M.cloud_map.frequency, M.cloud_map.bias_y);
-        float lod = __log2f(M.cloud_map.k_lod) + lg + M.lod_bias;
-        float cr = dtex_sample(M.cloud_map_tex, 0, u, v, 0.f, lod, M.min2d);
-        float cg = dtex_sample(M.cloud_map_tex, 1, u, v, 0.f, lod, M.min2d);
-        float xu = fmaf(p.x, M.displacement.frequency, M.displacement.bias_x);
-        float xv = fmaf(p.y, M.displacement.frequency, M.displacement.bias_y);
-        float xw = p.z * M.displacement.frequency;
-        float xl = __log2f(M.displacement.k_lod) + lg + M.lod_bias;
-        float3 disp;
-        disp.x = dtex_sample(M.displacement_tex, 0, xu, xv, 0.f, xl, M.mindisp) +
-                 dtex_sample(M.displacement_tex, 2, xu, xw, 0.f, xl, M.mindisp);
-        disp.y = dtex_sample(M.displacement_tex, 1, xu, xv, 0.f, xl, M.mindisp);
-        disp.z = dtex_sample(M.displacement_tex, 3, xu, xw, 0.f, xl, M.mindisp);
-        float3 q = p + disp * M.m0_disp_scale;
-        float3 dq = q - C.cam;
-        float dl = __log2f(sqrtf(dot3(dq, dq)));
-        float du = fmaf(q.x, M.detail.frequency, M.detail.bias_x);
-        float dv = fmaf(q.y, M.detail.frequency, M.detail.bias_y);
-        float dw = q.z * M.detail.frequency;
-        float dt = dtex_sample(M.detail_tex, 0, du, dv, dw, __log2f(M.detail.k_lod) + dl + M.lod_bias, M.min3d);
-        dt = fmaf(dt, M.m0_detail_x, M.m0_detail_y);
-        // CalHeightMask (VolumetricCloudDefaultMaterial0.glsl:9-12)
-        float hit = clamp01(h01 / cg);
-        float mask = clamp01(hit * (hit - 1.f) * -4.f);
-        return clamp01((cr * mask - dt) / (1.f - dt)) * h01 * M.density;
-    }
-    if (M.type == SKYR_MATERIAL_VOXEL) {
-        // VolumetricCloudMaterialVoxel.glsl:12-16
-        float u = fmaf(p.x, M.vx_freq_x, M.vx_bias_x);
-        float v = fmaf(p.y, M.vx_freq_y, M.vx_bias_y);
-        float lod = __log2f(M.vx_k_lod * dist_to_cam) + M.lod_bias;
-        return dtex_sample(M.voxel_tex, 0, u, v, h01, lod, SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST) * M.density;
-    }
+    if (M.type == SKYR_MATERIAL_DEFAULT0) return sigma_t_material0(C, M, p, h01, dist_to_cam);
+    if (M.type == SKYR_MATERIAL_VOXEL) return sigma_t_voxel(M, p, h01, dist_to_cam);
     return 0.f;
 }
 

@@ -5,8 +5,9 @@ launch-shape tuning, the autotuners, multi-view raymarches and CUDA graphs.
   constants: bit-identical LUTs;
 * lanes per texel change only the order of the per-ray sums: LUTs within 2e-6
   relative (FP32) / one FP16 step (FP16) of the default;
-* the raymarch's warp-tile shape changes only which lane computes a pixel: the
-  12 shapes give bit-identical frames;
+* the raymarch's warp-tile shape and register budget change only which lane
+  computes a pixel and how it is scheduled: the 24 shapes give bit-identical
+  frames;
 * views rendered together (forked streams) or replayed from a CUDA graph are
   bit-identical to one skyr_cloud_render per view;
 * a seeded subset of the batched workload (perturbed atmospheres, altitudes up
@@ -99,12 +100,12 @@ def test_cloud_tile_shapes_are_identical(sctx):
     view = W.frame_view(cam, 45.0, width=320, height=180)
     ref_rgba, ref_dist = cl.vc.render(atmo, view, sizes, luts, cl.bn)
     ref_rgba, ref_dist = ref_rgba.clone(), ref_dist.clone()
-    for w, bx in B.TILE_CANDIDATES:
-        B.set_tuning(sctx, cloud_tile_width=w, cloud_block_warps_x=bx)
+    for w, bx, occ in B.CLOUD_CANDIDATES:
+        B.set_tuning(sctx, cloud_tile_width=w, cloud_block_warps_x=bx, cloud_blocks_per_sm=occ)
         rgba, dist = cl.vc.render(atmo, view, sizes, luts, cl.bn)
         sctx.synchronize()
-        assert torch.equal(rgba, ref_rgba), (w, bx)
-        assert torch.equal(dist, ref_dist), (w, bx)
+        assert torch.equal(rgba, ref_rgba), (w, bx, occ)
+        assert torch.equal(dist, ref_dist), (w, bx, occ)
 
 
 def _batched(ctx, n_sets=6, n_views=5, fmt=1):
@@ -169,9 +170,9 @@ def test_autotuners(sctx):
     dist = torch.empty((360, 640), dtype=torch.float32, device="cuda")
     best, times = B.autotune_cloud(sctx, atmo, cl.cloud, cl.material, cl.textures, view, sizes, l1, cl.bn, rgba,
                                    dist, reps=2)
-    assert (best.cloud_tile_width, best.cloud_block_warps_x) in B.TILE_CANDIDATES
-    assert min(times) == pytest.approx(times[B.TILE_CANDIDATES.index((best.cloud_tile_width,
-                                                                       best.cloud_block_warps_x))])
+    key = (best.cloud_tile_width, best.cloud_block_warps_x, best.cloud_blocks_per_sm)
+    assert key in B.CLOUD_CANDIDATES
+    assert min(times) == pytest.approx(times[B.CLOUD_CANDIDATES.index(key)])
 
 
 def _mean_rel(got, want):
