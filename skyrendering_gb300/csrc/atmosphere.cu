@@ -10,8 +10,12 @@
 //    integrating a contiguous chunk, and the chunks are composed with the
 //    associative rule (L_a, T_a) o (L_b, T_b) = (L_a + T_a L_b, T_a T_b)
 //    through warp shuffles;
-//  * the multi-scattering texel is one warp (64 sphere directions, two per
-//    lane) reduced with shuffles instead of a shared-memory tree.
+//  * the multi-scattering texel is one 256-thread block (64 sphere directions
+//    x 4 chunks), reduced with shuffles and one shared-memory pass;
+//  * the passes after the first are programmatic dependent launches, so each
+//    one's blocks are scheduled while the previous one drains.
+#include <utility>
+
 #include "skyr_internal.cuh"
 #include "atmosphere_kernels.cuh"
 #include "lut_access.cuh"
@@ -42,6 +46,15 @@ __device__ __forceinline__ void medium(const AtmoConsts& A, float h, float3& ray
     mie_s = A.mie_scattering * em;
     ext = ray_s + A.mie_extinction * em + A.ozone_absorption * oz;
 }
+
+// Programmatic dependent launch: the multi-scattering and view passes are
+// launched with programmatic stream serialisation, so their blocks can be
+// scheduled while the previous pass drains.  A dependent pass waits here,
+// before its first LUT read, until the previous pass has completed and its
+// writes are visible (a no-op for a launch without the attribute); a pass lets
+// its dependents be scheduled once its own main work is under way.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
 
 // Number of samples of `for (float i = start; i < steps; ++i)`.
 __device__ __forceinline__ int sample_count(float start, float steps) {
@@ -128,6 +141,7 @@ __device__ __forceinline__ void integrate(const AtmoConsts& A, const LutView& L,
 template <int LANES, bool TABLE>
 __global__ void __launch_bounds__(128) transmittance_kernel(JobSrc<TABLE> jobs, int n_sets, int w, int h,
                                                             float4* __restrict__ out) {
+    pdl_launch_dependents();  // the pass is a single wave: every block is already resident
     int gid = blockIdx.x * blockDim.x + threadIdx.x;
     int lane = gid % LANES;
     int texel = gid / LANES;
@@ -232,7 +246,9 @@ __global__ void __launch_bounds__(kMsThreads) multiscattering_kernel(JobSrc<TABL
     RayStart s0{r, alt, rho2, mu, mu_s, view.z * sun_z + view.y * mu_s};
     int k0 = (n * chunk) / kMsChunks, k1 = (n * (chunk + 1)) / kMsChunks;
     float3 lum, tr, lf;
+    pdl_wait();  // the transmittance LUT
     integrate<true, float4>(A, Ls, nullptr, 0, 0, s0, dist / steps, 0.5f, k0, k1, iso, iso, lum, tr, lf);
+    pdl_launch_dependents();
     compose_lanes<kMsChunks>(lum, tr, &lf);
     if (chunk == 0 && ground) {
         // ComputeGroundLuminance (Atmosphere.glsl:297-306) at r = R
@@ -376,6 +392,7 @@ __global__ void __launch_bounds__(128) view_luts_kernel(JobSrc<TABLE> jobs, int 
     float nu = s0.nu;
     float3 lum = f3(0.f), tr = f3(1.f), lf;
     bool active = marching > 0.f;
+    pdl_wait();  // the transmittance and multi-scattering LUTs
     if (active) {
         // RayleighPhaseFunction / MiePhaseFunction (Atmosphere.glsl:138-154)
         float ph_r = 3.f / (16.f * SKYR_PI) * (1.f + nu * nu);
@@ -424,14 +441,33 @@ cudaError_t launch_transmittance(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_
     return cudaGetLastError();
 }
 
+// A launch whose blocks may start before the previous kernel on the stream has
+// finished (programmatic stream serialisation); the kernel orders its reads with
+// pdl_wait.
+template <class... P, class... A>
+static cudaError_t launch_dependent(void (*kernel)(P...), dim3 grid, dim3 block, cudaStream_t st, A&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
+
 template <class S, bool TABLE>
 cudaError_t launch_multiscattering(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, const float4* tlut,
                                    S* out, cudaStream_t st) {
     int blocks = n_sets * s.multiscattering_width * s.multiscattering_height;
     LutView L{tlut, s.transmittance_width, s.transmittance_height};
-    multiscattering_kernel<S, TABLE><<<blocks, kMsThreads, 0, st>>>(jobs, n_sets, L,
-                                                             s.transmittance_width * s.transmittance_height,
-                                                             s.multiscattering_width, s.multiscattering_height, out);
+    if (cudaError_t e = launch_dependent(multiscattering_kernel<S, TABLE>, dim3(blocks), dim3(kMsThreads), st, jobs,
+                                         n_sets, L, s.transmittance_width * s.transmittance_height,
+                                         s.multiscattering_width, s.multiscattering_height, out))
+        return e;
     return cudaGetLastError();
 }
 
@@ -443,11 +479,11 @@ static void v_launch(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, co
                                               s.aerial_perspective_depth);
     int blocks = (int)((rays * LANES + 127) / 128);
     LutView L{tlut, s.transmittance_width, s.transmittance_height};
-    view_luts_kernel<LANES, S, TABLE><<<blocks, 128, 0, st>>>(
-        jobs, n_sets, L, s.transmittance_width * s.transmittance_height, ms, s.multiscattering_width,
-        s.multiscattering_height, s.multiscattering_width * s.multiscattering_height, s.sky_view_width,
-        s.sky_view_height, s.aerial_perspective_width, s.aerial_perspective_height, s.aerial_perspective_depth, svl,
-        svt, apl, apt);
+    launch_dependent(view_luts_kernel<LANES, S, TABLE>, dim3(blocks), dim3(128), st, jobs, n_sets, L,
+                     s.transmittance_width * s.transmittance_height, ms, s.multiscattering_width,
+                     s.multiscattering_height, s.multiscattering_width * s.multiscattering_height, s.sky_view_width,
+                     s.sky_view_height, s.aerial_perspective_width, s.aerial_perspective_height,
+                     s.aerial_perspective_depth, svl, svt, apl, apt);
 }
 
 template <class S, bool TABLE>
