@@ -16,7 +16,9 @@ The third part of the metric, the surrogate against the path tracer on the
 "surrogate" (GPU times at 1024^2, errors at 256^2 against a path-traced
 reference, the path tracer's spp and time at the surrogate's error).  The
 batched workload (256 parameter sets, 64 views of uneven size, one CUDA graph
-with autotuned launch shapes) is reported under "batched".
+with autotuned launch shapes) is reported under "batched", and the cloud
+shadow passes (shadow map, blur, shadow froxel) with the shadowed frame under
+"shadow".
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -28,6 +30,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -52,6 +55,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="skyr", choices=["skyr", "reference"])
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)
+    ap.add_argument("--no-shadow", action="store_true", help="skip the cloud shadow-pass leg")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="leave out the voxel-cloud leg (surrogate vs path tracer) of the metric")
     ap.add_argument("--no-batched", action="store_true",
@@ -328,6 +332,132 @@ def batched_frames(ctx, reps: int = 5, n_sets: int = 256, n_views: int = 64):
     return res
 
 
+def shadow_passes(ctx, fs, lut_graph, reps: int = 20, cpu: bool = True):
+    """The cloud shadow passes of a 1920x1080 frame (VolumetricCloud::RenderShadow:
+    512^2 (depth, T) map blended into the previous frame's, 9-tap separable
+    blur, 160x90x128 R16 shadow froxel) on the frame workload: each pass timed
+    alone (CUDA events, back-to-back launches), the three as one CUDA graph,
+    and the shadowed frame -- LUT set + shadow passes + the raymarch reading
+    the froxel -- with L2 flushed between frames.  The FP64 oracle's time for
+    the same passes on the host cores (sampled map texels, scaled) is beside it."""
+    import ctypes as C
+
+    import torch
+
+    from skyrendering_gb300 import _abi
+    from skyrendering_gb300 import batch as B
+    from skyrendering_gb300 import cloud as CL
+    from skyrendering_gb300.atmosphere import _ptr
+
+    stream = ctx.stream
+    sizes = CL.shadow_sizes(1920, 1080)
+    sh = CL.CloudShadow(ctx, sizes)
+    sh.render(fs.vc, fs.atmo, fs.view, fs.bn)  # the first frame: nothing to blend into
+    view = _abi.CloudView.from_buffer_copy(fs.view)
+    view.frame_id = 1.0
+    wind = (0.01, 0.0)
+    frame = CL.light_frame(fs.atmo, fs.vc.params, view, sizes, previous=sh.frame, wind_delta=wind)
+    prev, cur = sh.raw[sh.current], sh.raw[1 - sh.current]
+    base = (ctx.handle, C.byref(fs.atmo), C.byref(fs.vc.params), C.byref(fs.vc.material), C.byref(fs.vc.textures),
+            C.byref(view), C.byref(sizes), C.byref(frame), _ptr(fs.bn), _ptr(prev), _ptr(cur))
+
+    def launch(stage):  # 1: the map, 2: + blur, 3: + froxel
+        _abi.call("skyr_cloud_shadow_render", *base, _ptr(sh.map) if stage >= 2 else None,
+                  _ptr(sh.froxel) if stage >= 3 else None)
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_map = timed(lambda: launch(1))
+    t_map_blur = timed(lambda: launch(2))
+    t_all = timed(lambda: launch(3))
+    with B.capture(ctx) as cap:
+        launch(3)
+    shadow_graph = cap.graph
+    t_graph = timed(shadow_graph.launch)
+    fview = sh.attach(_abi.CloudView.from_buffer_copy(fs.view))
+    with B.capture(ctx) as ccap:
+        fs.vc.render(fs.atmo, fview, fs.sizes, fs.luts, fs.bn, out_rgba=fs.rgba, out_distance=fs.dist)
+    cloud_graph = ccap.graph
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(reps)]
+    for _ in range(3):
+        lut_graph.launch()
+        shadow_graph.launch()
+        cloud_graph.launch()
+    torch.cuda.synchronize()
+    for i in range(reps):
+        flush.fill_(float(i))
+        ev[i][0].record(stream)
+        lut_graph.launch()
+        ev[i][1].record(stream)
+        shadow_graph.launch()
+        ev[i][2].record(stream)
+        cloud_graph.launch()
+        ev[i][3].record(stream)
+    torch.cuda.synchronize()
+    ctx.check_status()
+    frame_ms = statistics.mean(a.elapsed_time(d) for a, _, _, d in ev)
+    shadow_in_frame = statistics.mean(b.elapsed_time(c) for _, b, c, _ in ev)
+    cloud_in_frame = statistics.mean(c.elapsed_time(d) for _, _, c, d in ev)
+    mw, mh = sizes.map_width, sizes.map_height
+    fw, fh, fd = sizes.froxel_width, sizes.froxel_height, sizes.froxel_depth
+    sun_z = math.cos(math.radians(SUN_ZENITH))
+    steps = int(12.0 - 6.0 * sun_z)  # light-ray samples per map texel (the sun's local z ~ cos(zenith))
+    blur_ms = t_map_blur - t_map
+    froxel_ms = t_all - t_map_blur
+    res = {"map": f"{mw}x{mh} float2, temporal blend", "froxel": f"{fw}x{fh}x{fd} unorm16",
+           "map_ms": t_map, "blur_ms": blur_ms, "froxel_ms": froxel_ms, "passes_ms": t_all,
+           "passes_graph_ms": t_graph,
+           "map_density_evaluations": mw * mh * steps,
+           "map_density_evaluations_per_s": mw * mh * steps / (t_map * 1e-3),
+           "blur_bytes": 2 * mw * mh * 8, "blur_gb_per_s": 2 * mw * mh * 8 / max(blur_ms * 1e-3, 1e-9) / 1e9,
+           "froxel_bytes": mw * mh * 8 + fw * fh * fd * 2,
+           "froxel_gb_per_s": (mw * mh * 8 + fw * fh * fd * 2) / max(froxel_ms * 1e-3, 1e-9) / 1e9,
+           "shadowed_frame_ms": frame_ms, "shadow_in_frame_ms": shadow_in_frame,
+           "raymarch_with_froxel_ms": cloud_in_frame,
+           "note": "per-pass times are differences of back-to-back launches (map; map+blur; all three); "
+                   "the shadowed frame replays three graphs with L2 flushed between frames"}
+    if cpu:
+        import numpy as np
+
+        from oracle import oracle as orc
+
+        host = {k: (t.desc, t.data.cpu().numpy()) for k, t in fs.tex.items()}
+        fa = orc.frame_array(frame)
+        threads = os.cpu_count() or 1
+        texels = np.arange(0, mw * mh, 64, dtype=np.int32)
+        t0 = time.perf_counter()
+        orc.shadow_map(fs.atmo, fs.vc.params, fs.vc.material, host, view, mw, mh, fa, True, fs.bn.cpu().numpy(),
+                       previous_map=prev.cpu().numpy(), texels=texels, nthreads=threads)
+        t_map_cpu = (time.perf_counter() - t0) * (mw * mh) / len(texels)
+        smap = sh.map.cpu().numpy()
+        t0 = time.perf_counter()
+        orc.shadow_blur(cur.cpu().numpy())
+        t_blur_cpu = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        orc.shadow_froxel(fs.atmo, fs.vc.params, fs.vc.material, host, view, fa, smap, (fw, fh, fd),
+                          nthreads=threads)
+        t_fx_cpu = time.perf_counter() - t0
+        res["cpu_oracle"] = {"passes_ms": (t_map_cpu + t_blur_cpu + t_fx_cpu) * 1e3, "map_ms": t_map_cpu * 1e3,
+                             "blur_ms": t_blur_cpu * 1e3, "froxel_ms": t_fx_cpu * 1e3, "cores": threads,
+                             "kind": "port", "precision": "f64",
+                             "sample": f"{len(texels)} of {mw * mh} map texels scaled; full blur and froxel"}
+    shadow_graph.close()
+    cloud_graph.close()
+    return res
+
+
 def run_skyr(args):
     import ctypes as C
 
@@ -486,6 +616,8 @@ def run_skyr(args):
         "clocks": clocks,
         "wall_s": wall,
     }
+    if not args.no_shadow:
+        result["shadow"] = shadow_passes(ctx, fs, lut_graph, cpu=(rank == 0 and world == 1))
     if not args.no_surrogate:
         result["surrogate"] = surrogate_vs_pathtracer(ctx)
     if not args.no_batched:

@@ -153,6 +153,7 @@ typedef struct skyr_cloud_parameters {
     float phase_g_forward;
     float phase_g_back;
     float phase_back_scale;
+    float shadow_map_max_distance; /* km, frustum depth the shadow map covers (VolumetricCloud.h:30) */
 } skyr_cloud_parameters;
 
 int skyr_cloud_parameters_default(skyr_cloud_parameters* c);
@@ -168,12 +169,20 @@ typedef struct skyr_cloud_view {
     float sun_direction_theta, sun_direction_phi; /* degrees */
     float frame_id;
     float aerial_perspective_lut_max_distance;
+    /* Shadow froxel of skyr_cloud_shadow_render for this view, or NULL for a
+     * visibility of 1: unorm16 texels [depth][height][width], read with GL
+     * LINEAR + CLAMP_TO_EDGE at the pixel's (u, v) and w = distance /
+     * shadow_froxel_max_distance, and faded to 1 by clamp(1 / w, 0, 1)
+     * (SampleRayScatterVisibility, VolumetricCloudShadowInterface.glsl:10-13);
+     * it scales the aerial-perspective luminance of the composite. */
+    const uint16_t* shadow_froxel;
+    int shadow_froxel_width, shadow_froxel_height, shadow_froxel_depth;
 } skyr_cloud_view;
 
 /* The raymarch pass of VolumetricCloud::Render at full resolution
  * (shaders/SkyRendering/VolumetricCloudRender.comp:139-210), with an empty
  * depth buffer where `depth` is NULL (else one float per pixel, GL window
- * depth) and a shadow froxel of 1.  Inputs: the transmittance LUT and the
+ * depth) and the view's shadow froxel (1 where it has none).  Inputs: the transmittance LUT and the
  * aerial-perspective LUTs of `sizes` (RGBA32F or RGBA16F per sizes->format),
  * a 64x64 float blue-noise tile.  Outputs (device): `out_rgba` half4 per pixel
  * (rgb luminance, a transmittance; reference RGBA16F), `out_distance` float per

@@ -78,6 +78,25 @@ def _ref(x):
     return C.cast(C.byref(x), P) if x is not None else None
 
 
+def _host_view(view, froxel, keep):
+    """Copy of a skyr_cloud_view whose shadow froxel is the host array `froxel`
+    (uint16 [depth][height][width]) or none, so that a device pointer never
+    reaches the oracle."""
+    if view is None:
+        return None
+    v = type(view).from_buffer_copy(view)
+    if froxel is None:
+        v.shadow_froxel = None
+        v.shadow_froxel_width = v.shadow_froxel_height = v.shadow_froxel_depth = 0
+    else:
+        a = np.ascontiguousarray(froxel, dtype=np.uint16)
+        assert a.ndim == 3
+        keep.append(a)
+        v.shadow_froxel = a.ctypes.data
+        v.shadow_froxel_depth, v.shadow_froxel_height, v.shadow_froxel_width = a.shape
+    return v
+
+
 def lut_set(params, render, sizes, precision: int = 64, views: bool = True, nthreads: int | None = None):
     """Whole LUT set of one parameter set (dict of float64 arrays, RGBA, x fastest)."""
     t = np.zeros((sizes.transmittance_height, sizes.transmittance_width, 4))
@@ -188,15 +207,17 @@ def pcg_hash(x: int) -> int:
 
 
 def cloud_render(atmo, cloud, material, textures_host: dict, view, sizes, transmittance, ap_lum, ap_trans,
-                 blue_noise, depth=None, pixels=None, precision: int = 64, nthreads: int | None = None):
+                 blue_noise, depth=None, pixels=None, precision: int = 64, nthreads: int | None = None,
+                 froxel: np.ndarray | None = None):
     """Raymarch pixels (flat indices, or all) of `view` with host textures.
 
     textures_host maps 'cloud_map' / 'detail' / 'displacement' / 'voxel' to
-    (desc, uint8 array)."""
+    (desc, uint8 array); `froxel` is the view's shadow froxel on the host."""
     import skyrendering_gb300._abi as A  # struct layout only
 
     t = A.CloudTextures()
     keep = []
+    view = _host_view(view, froxel, keep)
     for name in ("cloud_map", "detail", "displacement", "voxel"):
         if name in textures_host:
             desc, arr = textures_host[name]
@@ -259,11 +280,13 @@ def grid_majorants(grid_struct, data_half: np.ndarray) -> np.ndarray:
 
 def pathtrace(atmo, cloud, material, textures_host: dict | None, grid_struct, grid_half: np.ndarray | None,
               majorant: np.ndarray | None, pt, view, env_view, sizes, luts: dict, frame_begin: int, n_frames: int,
-              pixels, precision: int = 64, nthreads: int | None = None):
+              pixels, precision: int = 64, nthreads: int | None = None, froxel: np.ndarray | None = None):
     """Per-pixel (sum, sum of squares) of n_frames path-traced frames."""
     import skyrendering_gb300._abi as A
 
     keep = []
+    view = _host_view(view, froxel, keep)
+    env_view = _host_view(env_view, None, keep)
     t = A.CloudTextures()
     for name, (desc, arr) in (textures_host or {}).items():
         arr = np.ascontiguousarray(arr, dtype=np.uint8)
@@ -394,6 +417,8 @@ def point_radiance(atmo, cloud, grid_struct, data_half, pt, view, env_view, size
                    n_paths: int, points: np.ndarray, nthreads: int | None = None):
     """Per point (sum, sum of squares) of n_paths point-source path radiances."""
     keep = []
+    view = _host_view(view, None, keep)
+    env_view = _host_view(env_view, None, keep)
     g = _grid_copy(grid_struct, data_half, keep)
     arrs = _lut_arrays(luts, ("transmittance", "sky_view_luminance", "sky_view_transmittance",
                               "aerial_perspective_luminance", "aerial_perspective_transmittance"))
@@ -408,10 +433,11 @@ def point_radiance(atmo, cloud, grid_struct, data_half, pt, view, env_view, size
 
 def surrogate_render(atmo, cloud, grid_struct, data_half, pt, view, sizes, luts: dict, lattice: np.ndarray, fv,
                      params: np.ndarray, out_scale: float, steps: int, use_network: bool, min_t: float,
-                     rel_err: float, pixels, nthreads: int | None = None):
+                     rel_err: float, pixels, nthreads: int | None = None, froxel: np.ndarray | None = None):
     """FP64 surrogate raymarch of listed pixels over the GPU-built lattice bytes:
     (out[n][4] = rgb, transmittance; err[n])."""
     keep = []
+    view = _host_view(view, froxel, keep)
     g = _grid_copy(grid_struct, data_half, keep)
     arrs = _lut_arrays(luts, ("transmittance", "aerial_perspective_luminance", "aerial_perspective_transmittance"))
     nodes = fv.nx * fv.ny * fv.nz
@@ -428,3 +454,103 @@ def surrogate_render(atmo, cloud, grid_struct, data_half, pt, view, sizes, luts:
                                        _dp(err))
     assert rc == 0
     return out, err
+
+
+# ---------------------------------------------------------------------------
+# cloud shadow passes
+# ---------------------------------------------------------------------------
+def _declare_shadow(lb):
+    lb.oracle_cloud_light_frame.restype = C.c_int
+    lb.oracle_cloud_light_frame.argtypes = [P, P, P, C.c_int, C.c_int, D, FP, D]
+    lb.oracle_cloud_shadow_map.restype = C.c_int
+    lb.oracle_cloud_shadow_map.argtypes = [P, P, P, P, P, C.c_int, C.c_int, D, C.c_int, F32, D, I32, C.c_int,
+                                           C.c_int, D]
+    lb.oracle_cloud_shadow_blur.restype = C.c_int
+    lb.oracle_cloud_shadow_blur.argtypes = [C.c_int, C.c_int, D, D]
+    lb.oracle_cloud_shadow_froxel.restype = C.c_int
+    lb.oracle_cloud_shadow_froxel.argtypes = [P, P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, D, D,
+                                              C.c_int, U16, D]
+
+
+_EXT.append(_declare_shadow)
+
+
+def _textures_struct(textures_host: dict | None, keep):
+    import skyrendering_gb300._abi as A  # struct layout only
+
+    t = A.CloudTextures()
+    for name, (desc, arr) in (textures_host or {}).items():
+        arr = np.ascontiguousarray(arr, dtype=np.uint8)
+        keep.append(arr)
+        setattr(t, name, arr.ctypes.data)
+        setattr(t, name + "_desc", desc)
+    return t
+
+
+def frame_array(frame) -> np.ndarray:
+    """A skyr_cloud_light_frame as the oracle's 4 x 16 doubles (light VP,
+    inverse, model, reprojection), column-major."""
+    return np.concatenate([np.array(frame.light_view_projection[:]), np.array(frame.inverse_light_view_projection[:]),
+                           np.array(frame.model[:]), np.array(frame.shadow_map_reproject[:])]).astype(np.float64)
+
+
+def light_frame(atmo, cloud, view, map_w: int, map_h: int, previous: np.ndarray | None = None,
+                wind=None) -> tuple[np.ndarray, bool]:
+    """FP64 light transform of a view: (4 x 16 doubles, has_previous)."""
+    keep = []
+    v = _host_view(view, None, keep)
+    out = np.zeros(64)
+    prev = None if previous is None else np.ascontiguousarray(previous, dtype=np.float64)
+    w = None if wind is None else np.ascontiguousarray(wind, dtype=np.float32)
+    has = lib().oracle_cloud_light_frame(_ref(atmo), _ref(cloud), _ref(v), map_w, map_h, _dp(prev),
+                                         None if w is None else w.ctypes.data_as(FP), _dp(out))
+    return out, bool(has)
+
+
+def shadow_map(atmo, cloud, material, textures_host, view, map_w: int, map_h: int, frame: np.ndarray,
+               has_previous: bool, blue_noise, previous_map=None, texels=None, nthreads: int | None = None):
+    """Shadow-map texels (flat indices y * map_w + x, or all): [n][2] (depth, T)."""
+    keep = []
+    t = _textures_struct(textures_host, keep)
+    v = _host_view(view, None, keep)
+    fr = np.ascontiguousarray(frame, dtype=np.float64)
+    bn = np.ascontiguousarray(blue_noise, dtype=np.float32)
+    pm = None if previous_map is None else np.ascontiguousarray(previous_map, dtype=np.float64).reshape(-1)
+    n = map_w * map_h if texels is None else len(texels)
+    tx = None if texels is None else np.ascontiguousarray(texels, dtype=np.int32)
+    out = np.zeros((n, 2))
+    rc = lib().oracle_cloud_shadow_map(_ref(atmo), _ref(cloud), _ref(material), _ref(t), _ref(v), map_w, map_h,
+                                       _dp(fr), int(has_previous), bn.ctypes.data_as(F32), _dp(pm),
+                                       None if tx is None else tx.ctypes.data_as(I32), n, nthreads or threads(),
+                                       _dp(out))
+    assert rc == 0
+    return out
+
+
+def shadow_blur(raw: np.ndarray) -> np.ndarray:
+    """Both blur passes of an [h][w][2] map."""
+    r = np.ascontiguousarray(raw, dtype=np.float64)
+    h, w = r.shape[:2]
+    out = np.zeros_like(r)
+    assert lib().oracle_cloud_shadow_blur(w, h, _dp(r.reshape(-1)), _dp(out.reshape(-1))) == 0
+    return out
+
+
+def shadow_froxel(atmo, cloud, material, textures_host, view, frame: np.ndarray, shadow_map_hw2: np.ndarray,
+                  froxel_size, nthreads: int | None = None):
+    """The R16 shadow froxel [d][h][w] (uint16) and its running means before the
+    store (float64) from a blurred [h][w][2] map."""
+    keep = []
+    t = _textures_struct(textures_host, keep)
+    v = _host_view(view, None, keep)
+    fr = np.ascontiguousarray(frame, dtype=np.float64)
+    m = np.ascontiguousarray(shadow_map_hw2, dtype=np.float64)
+    mh, mw = m.shape[:2]
+    fw, fh, fd = froxel_size
+    out = np.zeros((fd, fh, fw), dtype=np.uint16)
+    exact = np.zeros((fd, fh, fw))
+    rc = lib().oracle_cloud_shadow_froxel(_ref(atmo), _ref(cloud), _ref(material), _ref(t), _ref(v), mw, mh, fw,
+                                          fh, fd, _dp(fr), _dp(m.reshape(-1)), nthreads or threads(),
+                                          out.ctypes.data_as(U16), _dp(exact.reshape(-1)))
+    assert rc == 0
+    return out, exact

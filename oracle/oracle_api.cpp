@@ -11,6 +11,8 @@
 #include "oracle_cloud.hpp"
 #include "oracle_noise.hpp"
 #include "oracle_pathtrace.hpp"
+#include "oracle_shadow.hpp"
+#include "../include/skyr_cloud_shadow.h"
 #include "../include/skyr_surrogate.h"
 
 namespace {
@@ -663,11 +665,118 @@ int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_c
                    ww = 0.5 / al.d + wz * (1 - 1.0 / al.d);
             orc::V3<double> at = orc::sample_linear_clamp3(*W->C.ap_trans, uu, vq, ww);
             orc::V3<double> alum = orc::sample_linear_clamp3(al, uu, vq, ww);
+            alum = alum * W->C.RayScatterVisibility(u, vv, wt / wsum);
             L = L * at + alum * (1 - T);
         }
         for (int c = 0; c < 3; ++c) out[4 * (size_t)i + c] = L[c];
         out[4 * (size_t)i + 3] = T;
         err[i] = errs;
+    });
+    return 0;
+}
+
+}  // extern "C"
+
+// ---- cloud shadow passes ----------------------------------------------------
+namespace {
+
+// A light frame as 4 x 16 doubles: light_vp, inv_light_vp, model, reproject.
+orc::LightFrameD frame_from(const double* f, int has_previous) {
+    orc::LightFrameD L;
+    for (int i = 0; i < 16; ++i) {
+        L.light_vp.m[i] = f[i];
+        L.inv_light_vp.m[i] = f[16 + i];
+        L.model.m[i] = f[32 + i];
+        L.reproject.m[i] = f[48 + i];
+    }
+    L.has_previous = has_previous != 0;
+    return L;
+}
+
+void frame_to(const orc::LightFrameD& L, double* f) {
+    for (int i = 0; i < 16; ++i) {
+        f[i] = L.light_vp.m[i];
+        f[16 + i] = L.inv_light_vp.m[i];
+        f[32 + i] = L.model.m[i];
+        f[48 + i] = L.reproject.m[i];
+    }
+}
+
+// The cloud oracle of a view with its material textures bound (no LUTs).
+std::unique_ptr<orc::CloudOracle<double>> cloud_oracle(const orc::AtmosphereOracle<double>& O,
+                                                       const skyr_atmosphere_parameters* atmo,
+                                                       const skyr_cloud_parameters* cp,
+                                                       const skyr_cloud_material* m, const skyr_cloud_textures* tx,
+                                                       const skyr_cloud_view* v) {
+    auto C = std::unique_ptr<orc::CloudOracle<double>>(new orc::CloudOracle<double>{
+        O, orc::derive_cloud_frame<double>(*atmo, *cp, *m, *tx, *v), {}, {}, {}, {}, nullptr, nullptr, nullptr,
+        nullptr});
+    auto set = [](orc::Tex8& t, const void* p, const skyr_noise_texture_desc& d, bool border) {
+        t.data = (const uint8_t*)p;
+        t.w = d.width; t.h = d.height; t.d = d.depth; t.channels = d.channels;
+        t.border = border;
+        t.init();
+    };
+    set(C->cloud_map, tx->cloud_map, tx->cloud_map_desc, false);
+    set(C->detail, tx->detail, tx->detail_desc, false);
+    set(C->displacement, tx->displacement, tx->displacement_desc, false);
+    set(C->voxel, tx->voxel, tx->voxel_desc, true);
+    return C;
+}
+
+}  // namespace
+
+extern "C" {
+
+// VolumetricCloud::Update's light transform; previous may be NULL.
+int oracle_cloud_light_frame(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                             const skyr_cloud_view* v, int map_w, int map_h, const double* previous,
+                             const float* wind, double* out) {
+    orc::LightFrameD prev;
+    if (previous) prev = frame_from(previous, 0);
+    orc::LightFrameD L = orc::derive_light_frame(*atmo, *cp, *v, map_w, map_h, previous ? &prev : nullptr, wind);
+    frame_to(L, out);
+    return L.has_previous ? 1 : 0;
+}
+
+// Shadow-map texels (texels[i] = y * map_w + x, or all when texels == NULL);
+// out[2 i + {0, 1}] = (depth, transmittance).
+int oracle_cloud_shadow_map(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                            const skyr_cloud_material* m, const skyr_cloud_textures* tx, const skyr_cloud_view* v,
+                            int map_w, int map_h, const double* frame, int has_previous, const float* blue_noise,
+                            const double* previous_map, const int* texels, int n, int threads, double* out) {
+    orc::AtmosphereOracle<double> O{orc::derive_atmosphere<double>(*atmo)};
+    auto C = cloud_oracle(O, atmo, cp, m, tx, v);
+    orc::ShadowMapOracle S{*C, frame_from(frame, has_previous), map_w, map_h, blue_noise, previous_map};
+    parallel_for(n, threads, [&](int i) {
+        int p = texels ? texels[i] : i;
+        S.Texel(p % map_w, p / map_w, out + 2 * (size_t)i);
+    });
+    return 0;
+}
+
+int oracle_cloud_shadow_blur(int w, int h, const double* in, double* out) {
+    orc::shadow_blur(w, h, in, out);
+    return 0;
+}
+
+// The shadow froxel of a view from a blurred map: out (R16) and, when not
+// NULL, exact (the running means before the store); [depth][height][width].
+int oracle_cloud_shadow_froxel(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                               const skyr_cloud_material* m, const skyr_cloud_textures* tx, const skyr_cloud_view* v,
+                               int map_w, int map_h, int fw, int fh, int fd, const double* frame, const double* map,
+                               int threads, uint16_t* out, double* exact) {
+    orc::CloudFrame<double> F = orc::derive_cloud_frame<double>(*atmo, *cp, *m, *tx, *v);
+    orc::LightFrameD L = frame_from(frame, 0);
+    const size_t slice = (size_t)fw * fh;
+    parallel_for(fw * fh, threads, [&](int i) {
+        std::vector<double> col(fd);
+        orc::froxel_column(F, L, map, map_w, map_h, fw, fh, fd, cp->shadow_froxel_max_distance, i % fw, i / fw,
+                           col.data());
+        for (int z = 0; z < fd; ++z) {
+            out[z * slice + i] = orc::unorm16(col[z]);
+            if (exact) exact[z * slice + i] = col[z];
+        }
     });
     return 0;
 }

@@ -134,6 +134,10 @@ struct CloudFrame {
     T m1_threshold, m1_height_hardness, m1_edge_hardness, m1_detail_base, m1_detail_scale, m1_height_cut, m1_edge_cut;
     T m0_detail_x, m0_detail_y, m0_disp_scale;
     T vx_freq_x, vx_freq_y, vx_bias_x, vx_bias_y, vx_k_lod;
+    // shadow froxel of the view (skyr_cloud_view.shadow_froxel), null: visibility 1
+    const uint16_t* froxel = nullptr;
+    int fx_w = 0, fx_h = 0, fx_d = 0;
+    T inv_froxel_max = T(0);
 };
 
 template <class T>
@@ -234,6 +238,13 @@ CloudFrame<T> derive_cloud_frame(const skyr_atmosphere_parameters& atmo, const s
         T maxw = T(std::max(d.width, std::max(d.height, d.depth)));
         f.vx_k_lod = maxw * tan_half / (T(std::min(m.voxel_width[0], m.voxel_width[1])) * vmin);
     }
+    if (v.shadow_froxel) {
+        f.froxel = v.shadow_froxel;
+        f.fx_w = v.shadow_froxel_width;
+        f.fx_h = v.shadow_froxel_height;
+        f.fx_d = v.shadow_froxel_depth;
+        f.inv_froxel_max = T(1) / T(cp.shadow_froxel_max_distance);  // GetShadowFroxel (VolumetricCloud.h:72)
+    }
     return f;
 }
 
@@ -306,6 +317,33 @@ struct CloudOracle {
             }
         }
         return T(0);
+    }
+
+    // SampleRayScatterVisibility (VolumetricCloudShadowInterface.glsl:10-13): the
+    // R16 froxel through a LINEAR + CLAMP_TO_EDGE sampler
+    // (Samplers::GetLinearNoMipmapClampToEdge, VolumetricCloud.h:72)
+    T RayScatterVisibility(T u, T v, T dist) const {
+        if (!F.froxel) return T(1);
+        T w = dist * F.inv_froxel_max;
+        T c[3] = {u * T(F.fx_w) - T(0.5), v * T(F.fx_h) - T(0.5), w * T(F.fx_d) - T(0.5)};
+        const int n[3] = {F.fx_w, F.fx_h, F.fx_d};
+        int i0[3], i1[3];
+        T f[3];
+        for (int k = 0; k < 3; ++k) {
+            T fl = std::floor(c[k]);
+            f[k] = c[k] - fl;
+            i0[k] = std::min(std::max(int(fl), 0), n[k] - 1);
+            i1[k] = std::min(std::max(int(fl) + 1, 0), n[k] - 1);
+        }
+        T s = T(0);
+        for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx) {
+                    int x = dx ? i1[0] : i0[0], y = dy ? i1[1] : i0[1], z = dz ? i1[2] : i0[2];
+                    T wgt = (dx ? f[0] : T(1) - f[0]) * (dy ? f[1] : T(1) - f[1]) * (dz ? f[2] : T(1) - f[2]);
+                    s += wgt * T(F.froxel[(size_t(z) * F.fx_h + y) * F.fx_w + x]) / T(65535);
+                }
+        return mixg(T(1), s, clampg(T(1) / w, T(0), T(1)));
     }
 
     // RayShellIntersect (VolumetricCloudRender.comp:39-71)
@@ -397,7 +435,7 @@ struct CloudOracle {
     }
 
     // main (VolumetricCloudRender.comp:139-210) at full resolution: pixel
-    // (px, py) of a w x h image with window depth `depth` and shadow froxel 1.
+    // (px, py) of a w x h image with window depth `depth`.
     void Pixel(int px, int py, int w, int h, float depth, T out_rgba[4], T& out_dist) const {
         T u = (T(px) + T(0.5)) / T(w), v = (T(py) + T(0.5)) / T(h);
         V3<T> frag = projective_mul(F.inv_mvp, V3<T>(u * T(2) - T(1), v * T(2) - T(1), T(depth) * T(2) - T(1)));
@@ -459,7 +497,7 @@ struct CloudOracle {
         T ww = T(0.5) / T(ap_lum->d) + wz * (T(1) - T(1) / T(ap_lum->d));
         V3<T> at = sample_linear_clamp3(*ap_trans, uu, vv, ww);
         V3<T> al = sample_linear_clamp3(*ap_lum, uu, vv, ww);
-        // SampleRayScatterVisibility with a froxel of 1 is 1
+        al = al * RayScatterVisibility(u, v, avg_t);  // VolumetricCloudRender.comp:198
         lum = lum * at + al * (T(1) - c.trans);
         lum = lum / std::max(T(1e-5), T(1) - c.trans);
         T fade = smoothstepg(F.max_visible_distance * T(0.75), F.max_visible_distance, it[0][0]);

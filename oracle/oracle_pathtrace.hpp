@@ -432,6 +432,7 @@ struct PathTracerOracle {
             T ww = T(0.5) / T(al.d) + wz * (T(1) - T(1) / T(al.d));
             V3<T> at = sample_linear_clamp3(*Cl.ap_trans, uu, vv, ww);
             V3<T> alum = sample_linear_clamp3(al, uu, vv, ww);
+            alum = alum * Cl.RayScatterVisibility(u, v, st);  // PathTracing.comp:277
             L = L * at + alum;
         }
         out[0] = L.x;

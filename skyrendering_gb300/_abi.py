@@ -230,6 +230,7 @@ class CloudParameters(C.Structure):
         ("sun_multiscattering_sigma_scale", C.c_float), ("env_multiscattering_sigma_scale", C.c_float),
         ("env_bottom_visibility", C.c_float), ("env_sun_height_curve_exp", C.c_float),
         ("phase_g_forward", C.c_float), ("phase_g_back", C.c_float), ("phase_back_scale", C.c_float),
+        ("shadow_map_max_distance", C.c_float),
     ]
 
 
@@ -237,7 +238,9 @@ class CloudView(C.Structure):
     _fields_ = [("camera_position", f3), ("view_projection", f16), ("fovy", C.c_float),
                 ("viewport_width", C.c_int), ("viewport_height", C.c_int), ("width", C.c_int),
                 ("height", C.c_int), ("sun_direction_theta", C.c_float), ("sun_direction_phi", C.c_float),
-                ("frame_id", C.c_float), ("aerial_perspective_lut_max_distance", C.c_float)]
+                ("frame_id", C.c_float), ("aerial_perspective_lut_max_distance", C.c_float),
+                ("shadow_froxel", C.c_void_p), ("shadow_froxel_width", C.c_int), ("shadow_froxel_height", C.c_int),
+                ("shadow_froxel_depth", C.c_int)]
 
 
 STRUCT_IDS.update({3: NoiseTextureDesc, 4: CloudMaterial, 5: CloudTextures, 6: CloudParameters, 7: CloudView})
@@ -257,6 +260,32 @@ _SIGNATURES.update({
 _SIGNATURES["skyr_cloud_render_counted"] = (
     C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters), C.POINTER(CloudMaterial),
               C.POINTER(CloudTextures), C.POINTER(CloudView), C.POINTER(LutSizes), P, P, P, P, P, P, P, P])
+
+# ---------------------------------------------------------------------------
+# skyr_cloud_shadow.h
+# ---------------------------------------------------------------------------
+class CloudShadowSizes(C.Structure):
+    _fields_ = [("map_width", C.c_int), ("map_height", C.c_int), ("froxel_width", C.c_int),
+                ("froxel_height", C.c_int), ("froxel_depth", C.c_int)]
+
+
+class CloudLightFrame(C.Structure):
+    _fields_ = [("light_view_projection", f16), ("inverse_light_view_projection", f16), ("model", f16),
+                ("shadow_map_reproject", f16), ("has_previous", C.c_int)]
+
+
+STRUCT_IDS.update({15: CloudShadowSizes, 16: CloudLightFrame})
+_SIGNATURES.update({
+    "skyr_cloud_shadow_sizes_default": (C.c_int, [C.c_int, C.c_int, C.POINTER(CloudShadowSizes)]),
+    "skyr_cloud_light_frame_derive": (C.c_int, [C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                                C.POINTER(CloudView), C.POINTER(CloudShadowSizes),
+                                                C.POINTER(CloudLightFrame), C.POINTER(C.c_float),
+                                                C.POINTER(CloudLightFrame)]),
+    "skyr_cloud_shadow_render": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                           C.POINTER(CloudMaterial), C.POINTER(CloudTextures), C.POINTER(CloudView),
+                                           C.POINTER(CloudShadowSizes), C.POINTER(CloudLightFrame), P, P, P, P, P]),
+})
+
 
 # allocation-free LUT set (static device scratch, SKYR_NOALLOC_MAX_SETS sets)
 SKYR_NOALLOC_MAX_SETS = 256

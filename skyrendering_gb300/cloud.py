@@ -5,6 +5,9 @@
   parameters change (GenerateIfParameterChanged).
 * ``VolumetricCloud.render`` ~ the raymarch pass of VolumetricCloud::Render
   (src/SkyRendering/VolumetricCloud.cpp:361-385) at full resolution.
+* ``CloudShadow`` ~ VolumetricCloud::RenderShadow (VolumetricCloud.cpp:282-325)
+  with its state: the raw shadow maps used in turn, the blurred map, the
+  shadow froxel and the previous frame's light transform.
 """
 from __future__ import annotations
 
@@ -117,6 +120,76 @@ class VolumetricCloud:
                   _ptr(luts.aerial_perspective_transmittance), _ptr(blue_noise), _ptr(depth), _ptr(out_rgba),
                   _ptr(out_distance))
         return out_rgba, out_distance
+
+
+def shadow_sizes(viewport_width: int, viewport_height: int) -> _abi.CloudShadowSizes:
+    """512 x 512 map, (w / 12) x (h / 12) x 128 froxel (VolumetricCloud.cpp:52,134-135)."""
+    s = _abi.CloudShadowSizes()
+    _abi.call("skyr_cloud_shadow_sizes_default", viewport_width, viewport_height, C.byref(s))
+    return s
+
+
+def light_frame(atmosphere: _abi.AtmosphereParameters, params: _abi.CloudParameters, view: _abi.CloudView,
+                sizes: _abi.CloudShadowSizes, previous: _abi.CloudLightFrame | None = None,
+                wind_delta=None) -> _abi.CloudLightFrame:
+    """The light transform of VolumetricCloud::Update for a view (host only)."""
+    out = _abi.CloudLightFrame()
+    wind = None if wind_delta is None else (C.c_float * 2)(*wind_delta)
+    _abi.call("skyr_cloud_light_frame_derive", C.byref(atmosphere), C.byref(params), C.byref(view), C.byref(sizes),
+              None if previous is None else C.byref(previous), wind, C.byref(out))
+    return out
+
+
+class CloudShadow:
+    """Shadow-pass state of one viewport (VolumetricCloud.h:106-115,
+    VolumetricCloud.cpp:102-113,134-135): two raw (depth, transmittance) maps
+    used in turn, so that each frame blends into the previous one, the
+    blurred map and the R16 shadow froxel ([depth][height][width], stored as
+    int16 words, read as uint16)."""
+
+    def __init__(self, ctx: Context, sizes: _abi.CloudShadowSizes):
+        self.ctx, self.sizes = ctx, sizes
+        h, w = sizes.map_height, sizes.map_width
+        self.raw = [torch.zeros((h, w, 2), dtype=torch.float32, device="cuda") for _ in range(2)]
+        self.map = torch.zeros((h, w, 2), dtype=torch.float32, device="cuda")
+        self.froxel = torch.zeros((sizes.froxel_depth, sizes.froxel_height, sizes.froxel_width), dtype=torch.int16,
+                                  device="cuda")
+        self.frame: _abi.CloudLightFrame | None = None  # the last frame's light transform
+        self.current = 0  # index of the raw map written last
+
+    def render(self, cloud: "VolumetricCloud", atmosphere: _abi.AtmosphereParameters, view: _abi.CloudView,
+               blue_noise: torch.Tensor, wind_delta=None, blend: bool = True) -> _abi.CloudLightFrame:
+        """RenderShadow for `view`: derive this frame's light transform, write
+        the other raw map (blended with the last one unless `blend` is False or
+        this is the first frame), blur it and rebuild the froxel."""
+        frame = light_frame(atmosphere, cloud.params, view, self.sizes, self.frame if blend else None, wind_delta)
+        k = 1 - self.current
+        previous = self.raw[self.current] if (blend and self.frame is not None) else None
+        _abi.call("skyr_cloud_shadow_render", self.ctx.handle, C.byref(atmosphere), C.byref(cloud.params),
+                  C.byref(cloud.material), C.byref(cloud.textures), C.byref(view), C.byref(self.sizes),
+                  C.byref(frame), _ptr(blue_noise), _ptr(previous), _ptr(self.raw[k]), _ptr(self.map),
+                  _ptr(self.froxel))
+        self.frame, self.current = frame, k
+        return frame
+
+    @property
+    def raw_map(self) -> torch.Tensor:
+        return self.raw[self.current]
+
+    def attach(self, view: _abi.CloudView) -> _abi.CloudView:
+        """Point `view` at this froxel (the raymarch, path tracer and surrogate
+        then scale their aerial-perspective luminance by its visibility)."""
+        view.shadow_froxel = self.froxel.data_ptr()
+        view.shadow_froxel_width = self.sizes.froxel_width
+        view.shadow_froxel_height = self.sizes.froxel_height
+        view.shadow_froxel_depth = self.sizes.froxel_depth
+        return view
+
+
+def detach_froxel(view: _abi.CloudView) -> _abi.CloudView:
+    view.shadow_froxel = None
+    view.shadow_froxel_width = view.shadow_froxel_height = view.shadow_froxel_depth = 0
+    return view
 
 
 def blue_noise_tile(seed: int = 0x5EED) -> torch.Tensor:

@@ -33,8 +33,9 @@ double dotd(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 D3 crossd(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
 D3 normd(D3 a) { return mul(a, 1.0 / std::sqrt(dotd(a, a))); }
 float3 tof(D3 a) { return make_float3((float)a.x, (float)a.y, (float)a.z); }
+}  // namespace
 
-bool inv4(const double* m, double* out) {
+bool invert4d(const double* m, double* out) {
     double w[4][8];
     for (int r = 0; r < 4; ++r)
         for (int c = 0; c < 4; ++c) {
@@ -61,7 +62,7 @@ bool inv4(const double* m, double* out) {
     return true;
 }
 
-void matmul4(const double* a, const double* b, double* c) {  // column-major c = a b
+void matmul4d(const double* a, const double* b, double* c) {  // column-major c = a b
     for (int r = 0; r < 4; ++r)
         for (int col = 0; col < 4; ++col) {
             double s = 0;
@@ -69,6 +70,8 @@ void matmul4(const double* a, const double* b, double* c) {  // column-major c =
             c[col * 4 + r] = s;
         }
 }
+
+namespace {
 
 int fill_tex(DTex& t, const void* p, const skyr_noise_texture_desc& d, bool border, bool required,
              const char* what, const void* ex, int ex_channels) {
@@ -119,8 +122,8 @@ int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud
                         up.x,    up.y,    up.z,    0, origin.x, origin.y, origin.z, 1};
     double vp[16], mvp[16], imvp[16];
     for (int i = 0; i < 16; ++i) vp[i] = v.view_projection[i];
-    matmul4(vp, model, mvp);
-    if (!inv4(mvp, imvp)) return set_error(SKYR_EINVAL, "view_projection is singular");
+    matmul4d(vp, model, mvp);
+    if (!invert4d(mvp, imvp)) return set_error(SKYR_EINVAL, "view_projection is singular");
     // local camera: the model is a rotation + translation, inverse = transpose
     D3 rel = sub(cam, origin);
     D3 cam_l{dotd(front, rel), dotd(right, rel), dotd(up, rel)};
@@ -138,6 +141,8 @@ int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud
     c.w1 = (float)colw(1);
     c.w2 = (float)colw(2);
     c.wf = (float)(colw(2) + colw(3));
+    c.a3 = tof(sub(col(3), mul(cam_l, colw(3))));
+    c.w3 = (float)colw(3);
     c.cam = tof(cam_l);
     c.sun = tof(sun_l);
     c.R = (float)R;
@@ -177,6 +182,17 @@ int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud
     c.ap_w = sizes.aerial_perspective_width;
     c.ap_h = sizes.aerial_perspective_height;
     c.ap_d = sizes.aerial_perspective_depth;
+    if (v.shadow_froxel) {
+        if (v.shadow_froxel_width < 1 || v.shadow_froxel_height < 1 || v.shadow_froxel_depth < 1 ||
+            v.shadow_froxel_width > 16384 || v.shadow_froxel_height > 16384 || v.shadow_froxel_depth > 4096)
+            return set_error(SKYR_EINVAL, "shadow froxel size out of range");
+        if (!(cp.shadow_froxel_max_distance > 0.f)) return set_error(SKYR_EINVAL, "bad shadow froxel max distance");
+        c.froxel = v.shadow_froxel;
+        c.fx_w = v.shadow_froxel_width;
+        c.fx_h = v.shadow_froxel_height;
+        c.fx_d = v.shadow_froxel_depth;
+        c.inv_froxel_max_distance = (float)(1.0 / cp.shadow_froxel_max_distance);
+    }
 
     mc.type = m.type;
     mc.min2d = m.minfilter2d;
@@ -452,6 +468,7 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, 
                                 wz * (float)(C.ap_d - 1));
     float3 al = trilinear_clamp(ap_lum, C.ap_w, C.ap_h, C.ap_d, u * (float)(C.ap_w - 1), v * (float)(C.ap_h - 1),
                                 wz * (float)(C.ap_d - 1));
+    al = al * froxel_visibility(C, u, v, avg_t);  // VolumetricCloudRender.comp:198
     lum = lum * at + al * (1.f - mk.trans);
     lum = lum * (1.f / fmaxf(1e-5f, 1.f - mk.trans));
     float fade = smoothstepf(C.max_visible_distance * 0.75f, C.max_visible_distance, it[0]);
@@ -591,6 +608,7 @@ int skyr_cloud_parameters_default(skyr_cloud_parameters* c) {
     c->phase_g_forward = 0.85f;
     c->phase_g_back = -0.15f;
     c->phase_back_scale = 2.16f;
+    c->shadow_map_max_distance = 20.f;
     return SKYR_OK;
 }
 

@@ -154,6 +154,8 @@ struct CloudConsts {
     // so that far-plane points (depth near 1) do not cancel in FP32
     float3 a0, a1, a2, af;
     float w0, w1, w2, wf;
+    float3 a3;  // NDC z = 0 rays: (frag - cam) = (a0 x + a1 y + a3) / (w0 x + w1 y + w3)
+    float w3;
     float3 cam;  // local z-up
     float3 sun;  // local
     float R, bottom, top;       // Earth radius, cloud layer altitudes
@@ -170,7 +172,42 @@ struct CloudConsts {
     float atmo_in_space;  // camera beyond the atmosphere top
     int width, height;
     int ap_w, ap_h, ap_d;
+    const uint16_t* froxel;  // shadow froxel, or null for a visibility of 1
+    int fx_w, fx_h, fx_d;
+    float inv_froxel_max_distance;
 };
+
+// SampleRayScatterVisibility (VolumetricCloudShadowInterface.glsl:10-13): the
+// shadow froxel read with GL LINEAR + CLAMP_TO_EDGE at (u, v, dist / max) and
+// faded to 1 by clamp(1 / w, 0, 1) beyond its last slice; 1 without a froxel.
+__device__ __forceinline__ float froxel_visibility(const CloudConsts& C, float u, float v, float dist) {
+    if (!C.froxel) return 1.f;
+    float w = dist * C.inv_froxel_max_distance;
+    // clamping the texel coordinate first is CLAMP_TO_EDGE's rule for LINEAR
+    float x = fminf(fmaxf(u * (float)C.fx_w - 0.5f, 0.f), (float)(C.fx_w - 1));
+    float y = fminf(fmaxf(v * (float)C.fx_h - 0.5f, 0.f), (float)(C.fx_h - 1));
+    float z = fminf(fmaxf(w * (float)C.fx_d - 0.5f, 0.f), (float)(C.fx_d - 1));
+    int x0 = (int)x, y0 = (int)y, z0 = (int)z;
+    int x1 = min(x0 + 1, C.fx_w - 1), y1 = min(y0 + 1, C.fx_h - 1), z1 = min(z0 + 1, C.fx_d - 1);
+    float a = x - (float)x0, b = y - (float)y0, g = z - (float)z0;
+    const size_t slice = (size_t)C.fx_w * C.fx_h;
+    float r[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const uint16_t* s = C.froxel + (size_t)(k ? z1 : z0) * slice;
+        float t00 = (float)__ldg(s + (size_t)y0 * C.fx_w + x0), t10 = (float)__ldg(s + (size_t)y0 * C.fx_w + x1);
+        float t01 = (float)__ldg(s + (size_t)y1 * C.fx_w + x0), t11 = (float)__ldg(s + (size_t)y1 * C.fx_w + x1);
+        float top = t00 + (t10 - t00) * a, bot = t01 + (t11 - t01) * a;
+        r[k] = top + (bot - top) * b;
+    }
+    float f = (r[0] + (r[1] - r[0]) * g) * (1.f / 65535.f);
+    float k = fminf(fmaxf(__frcp_rn(w), 0.f), 1.f);  // w = 0 gives +inf, clamped to 1
+    return 1.f + (f - 1.f) * k;
+}
+
+// Column-major 4x4 helpers of the host derivations (double).
+bool invert4d(const double* m, double* out);
+void matmul4d(const double* a, const double* b, double* c);
 
 int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud_parameters& cp,
                         const skyr_cloud_material& m, const skyr_cloud_textures& tex, const skyr_cloud_view& v,

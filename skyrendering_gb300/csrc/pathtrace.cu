@@ -269,6 +269,7 @@ __device__ __forceinline__ float4 path_sample(const CloudConsts& C, const AtmoCo
         float ax = u * (float)(C.ap_w - 1), ay = v * (float)(C.ap_h - 1), az = wz * (float)(C.ap_d - 1);
         float3 at = trilinear_clamp(apt, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
         float3 al = trilinear_clamp(apl, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
+        al = al * froxel_visibility(C, u, v, ps.scattered_t);  // PathTracing.comp:277
         L = L * at + al;
     }
     return make_float4(L.x, L.y, L.z, ps.scattered ? 0.f : 1.f);

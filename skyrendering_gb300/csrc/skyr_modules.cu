@@ -4,6 +4,7 @@
 #include "../../include/skyr_mlp.h"
 #include "../../include/skyr_surrogate.h"
 #include "../../include/skyr_pathtrace.h"
+#include "../../include/skyr_cloud_shadow.h"
 #include "skyr_ctx.cuh"
 
 namespace skyr {
@@ -84,6 +85,8 @@ size_t skyr_struct_size_ext(int which) {
         case 12: return sizeof(skyr_feature_volume);
         case 13: return sizeof(skyr_surrogate_parameters);
         case 14: return sizeof(skyr_tuning);
+        case 15: return sizeof(skyr_cloud_shadow_sizes);
+        case 16: return sizeof(skyr_cloud_light_frame);
         default: return 0;
     }
 }

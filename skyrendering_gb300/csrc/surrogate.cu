@@ -358,6 +358,7 @@ __global__ void __launch_bounds__(128, 4) surrogate_render_kernel(CloudConsts C,
         float ax = u * (float)(C.ap_w - 1), ay = v * (float)(C.ap_h - 1), az = wz * (float)(C.ap_d - 1);
         float3 at = trilinear_clamp(apt, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
         float3 al = trilinear_clamp(apl, C.ap_w, C.ap_h, C.ap_d, ax, ay, az);
+        al = al * froxel_visibility(C, u, v, wt / wsum);
         Lum = Lum * at + al * (1.f - T);
     }
     size_t pix = (size_t)py * P.width + px;

@@ -7,6 +7,7 @@ times on one stream, synchronise and exit 0.
     python -m skyrendering_gb300.profile_cases surrogate --iters 3 [--size 1024]
     python -m skyrendering_gb300.profile_cases lattice --iters 2
     python -m skyrendering_gb300.profile_cases mlp --iters 3
+    python -m skyrendering_gb300.profile_cases shadow --iters 3
 
 Cases (seeded synthetic inputs from workloads.py):
   luts   the plain LUT set (T 256x64, MS 32x32, SV 192x108, AP 32^3) of the
@@ -21,6 +22,8 @@ Cases (seeded synthetic inputs from workloads.py):
   lattice the feature lattice of that grid for the scene's sun;
   mlp    one Adam training step of the network on a 16384-sample batch of
          seeded random records.
+  shadow the cloud shadow passes of the 1920x1080 frame (512^2 map blended
+         into the previous frame's, blur, 160x90x128 froxel).
 The per-iteration CUDA-event time is printed for orientation; it is not a
 benchmark figure (bench.py is).
 """
@@ -105,9 +108,26 @@ def mlp_case(ctx):
     return lambda: (tr.step(rec, t), tr)
 
 
+def shadow_case(ctx):
+    from .cloud import CloudShadow, shadow_sizes
+
+    cam = W.frame_camera()
+    tex = {"cloud_map": NoiseTexture(W.cloud_map_desc()).generate(ctx),
+           "detail": NoiseTexture(W.base_noise_desc()).generate(ctx)}
+    material = W.frame_material()
+    prepare_textures(ctx, material.type, tex)
+    bn = blue_noise_tile().cuda()
+    view = W.frame_view(cam, SUN_ZENITH)
+    vc = VolumetricCloud(ctx, W.frame_cloud_parameters(), material, textures_struct(**tex))
+    sh = CloudShadow(ctx, shadow_sizes(1920, 1080))
+    sh.render(vc, W.earth_like_atmosphere(), view, bn)
+    atmo = W.earth_like_atmosphere()
+    return lambda: sh.render(vc, atmo, view, bn, wind_delta=(0.01, 0.0))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["luts", "cloud", "pt", "surrogate", "lattice", "mlp"])
+    ap.add_argument("case", choices=["luts", "cloud", "pt", "surrogate", "lattice", "mlp", "shadow"])
     ap.add_argument("--iters", type=int, default=3)
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--global-majorant", action="store_true")
@@ -124,6 +144,8 @@ def main(argv=None):
         step = pt_case(ctx, a.size, a.global_majorant, a.frames)
     elif a.case in ("surrogate", "lattice"):
         step = surrogate_case(ctx, a.size, a.case)
+    elif a.case == "shadow":
+        step = shadow_case(ctx)
     else:
         step = mlp_case(ctx)
     torch.cuda.synchronize()

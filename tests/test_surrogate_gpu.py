@@ -171,19 +171,27 @@ def test_pixel_list_matches_region(ctx, small):
     torch.testing.assert_close(acc, tr.acc, rtol=1e-5, atol=1e-7)
 
 
-@pytest.mark.parametrize("use_network", [0, 1])
-def test_render_matches_oracle(ctx, small, use_network):
+@pytest.mark.parametrize("use_network,froxel", [(0, False), (1, False), (1, True)])
+def test_render_matches_oracle(ctx, small, use_network, froxel):
     sc, grid, fv = small
     model = S.load_model(S.MODEL_PATH)
     net = model.packed(ctx)
     sp = S.parameters(use_network=use_network, network_error=0.1)
-    img, err = S.render(ctx, sc.atmo, sc.cloud, grid, sc.pt, sc.view, sc.sizes, sc.luts, fv, net, sp)
+    view, syn = sc.view, None
+    if froxel:  # a shadow froxel scaling the aerial-perspective luminance
+        from .test_cloud_shadow_gpu import attach, device_froxel, synthetic_froxel
+
+        syn = synthetic_froxel(seed=13)
+        dev = device_froxel(syn)
+        view = attach(_abi.CloudView.from_buffer_copy(sc.view), dev)
+    img, err = S.render(ctx, sc.atmo, sc.cloud, grid, sc.pt, view, sc.sizes, sc.luts, fv, net, sp)
     ctx.synchronize()
     w, h = sc.view.width, sc.view.height
     pix = np.arange(w * h, dtype=np.int32)
-    out, oerr = orc.surrogate_render(sc.atmo, sc.cloud, grid.struct, grid.data.cpu().numpy(), sc.pt, sc.view,
+    out, oerr = orc.surrogate_render(sc.atmo, sc.cloud, grid.struct, grid.data.cpu().numpy(), sc.pt, view,
                                      sc.sizes, _luts_host(sc), fv.buf.cpu().numpy(), fv.struct, model.params,
-                                     model.label_scale, sp.steps, bool(use_network), sp.min_transmittance, 0.1, pix)
+                                     model.label_scale, sp.steps, bool(use_network), sp.min_transmittance, 0.1, pix,
+                                     froxel=syn)
     g = img.reshape(-1, 4).double().cpu().numpy()
     lum_g = g[:, :3] @ [0.2126, 0.7152, 0.0722]
     lum_o = out[:, :3] @ [0.2126, 0.7152, 0.0722]
