@@ -18,7 +18,9 @@ reference, the path tracer's spp and time at the surrogate's error).  The
 batched workload (256 parameter sets, 64 views of uneven size, one CUDA graph
 with autotuned launch shapes) is reported under "batched", and the cloud
 shadow passes (shadow map, blur, shadow froxel) with the shadowed frame under
-"shadow".
+"shadow".  The reference's production cloud pass (quarter-resolution raymarch,
+temporal reconstruction, upscale) and the production frame built on it (LUT
+set + shadow passes + quarter pass) are under "quarter".
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -56,6 +58,7 @@ def parse():
     ap.add_argument("--impl", default="skyr", choices=["skyr", "reference"])
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)
     ap.add_argument("--no-shadow", action="store_true", help="skip the cloud shadow-pass leg")
+    ap.add_argument("--no-quarter", action="store_true", help="skip the quarter-resolution cloud-pass leg")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="leave out the voxel-cloud leg (surrogate vs path tracer) of the metric")
     ap.add_argument("--no-batched", action="store_true",
@@ -458,6 +461,110 @@ def shadow_passes(ctx, fs, lut_graph, reps: int = 20, cpu: bool = True):
     return res
 
 
+def quarter_pass(ctx, fs, lut_graph, reps: int = 20):
+    """The reference's production cloud pass at 1920x1080 (VolumetricCloud::Render):
+    checkerboard depth, index, the raymarch of 480x270 checkerboard texels,
+    the temporal reconstruction at 960x540 and the upscale composited into an
+    RGBA16F HDR target, on an empty depth buffer in steady state (the previous
+    frame's reconstruction as history).  Timed as one CUDA graph with and
+    without the upscale, and inside the production frame: LUT set + shadow
+    passes + quarter pass reading the shadow froxel, L2 flushed between frames."""
+    import ctypes as C
+
+    import torch
+
+    from skyrendering_gb300 import _abi
+    from skyrendering_gb300 import batch as B
+    from skyrendering_gb300 import cloud as CL
+    from skyrendering_gb300.atmosphere import _ptr
+
+    stream = ctx.stream
+    W_, H_ = fs.view.width, fs.view.height
+    zn, zf = fs.cam.z_near, fs.cam.z_far
+    vp = CL.CloudViewport(ctx, W_, H_)
+    hdr = torch.zeros((H_, W_, 4), dtype=torch.float16, device="cuda")
+    vp.render(fs.vc, fs.atmo, fs.view, fs.sizes, fs.luts, fs.bn, hdr=hdr, z_near=zn, z_far=zf)
+    sh = CL.CloudShadow(ctx, CL.shadow_sizes(W_, H_))
+    sh.render(fs.vc, fs.atmo, fs.view, fs.bn)
+    view = _abi.CloudView.from_buffer_copy(fs.view)
+    view.frame_id = 1.0
+    frame = CL.temporal_frame(fs.atmo, view, vp.previous_view, None, zn, zf, 1)
+    b = vp.buffers(history=True)
+    L = fs.luts
+
+    def call(v, out_hdr):
+        _abi.call("skyr_cloud_render_quarter", ctx.handle, C.byref(fs.atmo), C.byref(fs.vc.params),
+                  C.byref(fs.vc.material), C.byref(fs.vc.textures), C.byref(v), C.byref(fs.sizes),
+                  _ptr(L.transmittance), _ptr(L.aerial_perspective_luminance),
+                  _ptr(L.aerial_perspective_transmittance), _ptr(fs.bn), None, C.byref(frame), C.byref(b),
+                  _ptr(out_hdr))
+
+    with B.capture(ctx) as cap:
+        call(view, hdr)
+    full = cap.graph
+    with B.capture(ctx) as cap:
+        call(view, None)
+    no_upscale = cap.graph
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(g):
+        for _ in range(3):
+            g.launch()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            g.launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_full, t_no_up = timed(full), timed(no_upscale)
+    # the production frame: LUT set, shadow passes, quarter pass reading the froxel
+    shadow_frame = CL.light_frame(fs.atmo, fs.vc.params, view, sh.sizes, previous=sh.frame)
+    prev, cur = sh.raw[sh.current], sh.raw[1 - sh.current]
+    with B.capture(ctx) as cap:
+        _abi.call("skyr_cloud_shadow_render", ctx.handle, C.byref(fs.atmo), C.byref(fs.vc.params),
+                  C.byref(fs.vc.material), C.byref(fs.vc.textures), C.byref(view), C.byref(sh.sizes),
+                  C.byref(shadow_frame), _ptr(fs.bn), _ptr(prev), _ptr(cur), _ptr(sh.map), _ptr(sh.froxel))
+    shadow_graph = cap.graph
+    fview = sh.attach(_abi.CloudView.from_buffer_copy(view))
+    with B.capture(ctx) as cap:
+        call(fview, hdr)
+    quarter_graph = cap.graph
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(reps)]
+    for _ in range(3):
+        lut_graph.launch()
+        shadow_graph.launch()
+        quarter_graph.launch()
+    torch.cuda.synchronize()
+    for i in range(reps):
+        flush.fill_(float(i))
+        ev[i][0].record(stream)
+        lut_graph.launch()
+        ev[i][1].record(stream)
+        shadow_graph.launch()
+        ev[i][2].record(stream)
+        quarter_graph.launch()
+        ev[i][3].record(stream)
+    torch.cuda.synchronize()
+    ctx.check_status()
+    res = {"viewport": f"{W_}x{H_}", "raymarch": f"{W_ // 4}x{H_ // 4} checkerboard texels",
+           "reconstruct": f"{W_ // 2}x{H_ // 2}", "depth": "empty (1)", "history": "previous reconstruction",
+           "pass_ms": t_full, "pass_without_upscale_ms": t_no_up, "upscale_ms": t_full - t_no_up,
+           "production_frame_ms": statistics.mean(a.elapsed_time(d) for a, _, _, d in ev),
+           "production_frame_parts_ms": {
+               "lut_set": statistics.mean(a.elapsed_time(b_) for a, b_, _, _ in ev),
+               "shadow_passes": statistics.mean(b_.elapsed_time(c) for _, b_, c, _ in ev),
+               "quarter_pass": statistics.mean(c.elapsed_time(d) for _, _, c, d in ev)},
+           "kernels_per_pass": 5,
+           "note": "production frame = LUT set + shadow passes + quarter-resolution cloud pass with the froxel, "
+                   "three CUDA graphs, L2 flushed between frames; the composite is the upscale's"}
+    for g in (full, no_upscale, shadow_graph, quarter_graph):
+        g.close()
+    return res
+
+
 def run_skyr(args):
     import ctypes as C
 
@@ -618,6 +725,8 @@ def run_skyr(args):
     }
     if not args.no_shadow:
         result["shadow"] = shadow_passes(ctx, fs, lut_graph, cpu=(rank == 0 and world == 1))
+    if not args.no_quarter:
+        result["quarter"] = quarter_pass(ctx, fs, lut_graph)
     if not args.no_surrogate:
         result["surrogate"] = surrogate_vs_pathtracer(ctx)
     if not args.no_batched:

@@ -554,3 +554,103 @@ def shadow_froxel(atmo, cloud, material, textures_host, view, frame: np.ndarray,
                                           out.ctypes.data_as(U16), _dp(exact.reshape(-1)))
     assert rc == 0
     return out, exact
+
+
+# ---------------------------------------------------------------------------
+# quarter-resolution cloud pass
+# ---------------------------------------------------------------------------
+def _declare_quarter(lb):
+    lb.oracle_cloud_checkerboard.restype = C.c_int
+    lb.oracle_cloud_checkerboard.argtypes = [F32, C.c_int, C.c_int, D]
+    lb.oracle_cloud_index.restype = C.c_int
+    lb.oracle_cloud_index.argtypes = [D, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, D]
+    lb.oracle_cloud_render_quarter.restype = C.c_int
+    lb.oracle_cloud_render_quarter.argtypes = [P, P, P, P, P, P, D, D, D, F32, D, D, I32, C.c_int, C.c_int, D, D]
+    lb.oracle_cloud_reconstruct.restype = C.c_int
+    lb.oracle_cloud_reconstruct.argtypes = [P, P, P, P, P, FP, C.c_float, C.c_float, C.c_int, D, D, D, D, D, C.c_int,
+                                            D]
+    lb.oracle_cloud_upscale.restype = C.c_int
+    lb.oracle_cloud_upscale.argtypes = [C.c_int, C.c_int, F32, C.c_float, C.c_float, D, D, D, C.c_int, D]
+
+
+_EXT.append(_declare_quarter)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _f32p(a, keep):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    keep.append(a)
+    return a.ctypes.data_as(F32)
+
+
+def checkerboard(depth, w: int, h: int) -> np.ndarray:
+    """Checkerboard depth [h/2][w/2] of a window depth [h][w] (None: 1)."""
+    keep = []
+    out = np.zeros((h // 2, w // 2))
+    assert lib().oracle_cloud_checkerboard(_f32p(depth, keep), w, h, _dp(out)) == 0
+    return out
+
+
+def index_gen(cb, w: int, h: int, z_near: float, z_far: float, base: int) -> np.ndarray:
+    """[qh][qw][2] (index, linear depth) from a checkerboard depth [h/2][w/2]."""
+    c = _f64(cb)
+    out = np.zeros(((h // 2) // 2, (w // 2) // 2, 2))
+    assert lib().oracle_cloud_index(_dp(c), w, h, z_near, z_far, base, _dp(out)) == 0
+    return out
+
+
+def render_quarter(atmo, cloud, material, textures_host, view, sizes, transmittance, ap_lum, ap_trans, blue_noise,
+                   index, cb, pixels=None, froxel=None, nthreads: int | None = None):
+    """Raymarch quarter texels (flat y * qw + x, or all) at their checkerboard texels."""
+    keep = []
+    t = _textures_struct(textures_host, keep)
+    v = _host_view(view, froxel, keep)
+    qw, qh = (view.width // 2) // 2, (view.height // 2) // 2
+    n = qw * qh if pixels is None else len(pixels)
+    px = None if pixels is None else np.ascontiguousarray(pixels, dtype=np.int32)
+    rgba, dist = np.zeros((n, 4)), np.zeros(n)
+    bn = np.ascontiguousarray(blue_noise, dtype=np.float32)
+    ix, c = _f64(index).reshape(-1), _f64(cb).reshape(-1)
+    arrs = [_f64(transmittance), _f64(ap_lum), _f64(ap_trans)]
+    rc = lib().oracle_cloud_render_quarter(_ref(atmo), _ref(cloud), _ref(material), _ref(t), _ref(v), _ref(sizes),
+                                           *[_dp(a) for a in arrs], bn.ctypes.data_as(F32), _dp(ix), _dp(c),
+                                           None if px is None else px.ctypes.data_as(I32), n, nthreads or threads(),
+                                           _dp(rgba), _dp(dist))
+    assert rc == 0
+    return rgba, dist
+
+
+def reconstruct(atmo, cloud, material, textures_host, view, frame, cb, index, render, rdist, previous,
+                nthreads: int | None = None) -> np.ndarray:
+    """[h/2][w/2][4] reconstruction; `frame` a skyr_cloud_temporal_frame; previous None: no history."""
+    keep = []
+    t = _textures_struct(textures_host, keep)
+    v = _host_view(view, None, keep)
+    hw, hh = view.width // 2, view.height // 2
+    out = np.zeros((hh, hw, 4))
+    rp = np.ascontiguousarray(frame.reproject[:], dtype=np.float32)
+    prev = None if previous is None else _f64(previous).reshape(-1)
+    args = [_f64(a).reshape(-1) for a in (cb, index, render, rdist)]
+    rc = lib().oracle_cloud_reconstruct(_ref(atmo), _ref(cloud), _ref(material), _ref(t), _ref(v),
+                                        rp.ctypes.data_as(FP), frame.z_near, frame.z_far,
+                                        int(bool(frame.has_previous)), *[_dp(a) for a in args], _dp(prev),
+                                        nthreads or threads(), _dp(out.reshape(-1)))
+    assert rc == 0
+    return out
+
+
+def upscale(w: int, h: int, depth, z_near: float, z_far: float, cb, rec, hdr_in,
+            nthreads: int | None = None) -> np.ndarray:
+    """[h][w][4]: the upscaled reconstruction composited over hdr_in."""
+    keep = []
+    out = np.zeros((h, w, 4))
+    args = [_f64(a).reshape(-1) for a in (cb, rec, hdr_in)]
+    rc = lib().oracle_cloud_upscale(w, h, _f32p(depth, keep), z_near, z_far, *[_dp(a) for a in args],
+                                    nthreads or threads(), _dp(out.reshape(-1)))
+    assert rc == 0
+    return out

@@ -12,6 +12,7 @@
 #include "oracle_noise.hpp"
 #include "oracle_pathtrace.hpp"
 #include "oracle_shadow.hpp"
+#include "oracle_quarter.hpp"
 #include "../include/skyr_cloud_shadow.h"
 #include "../include/skyr_surrogate.h"
 
@@ -777,6 +778,83 @@ int oracle_cloud_shadow_froxel(const skyr_atmosphere_parameters* atmo, const sky
             out[z * slice + i] = orc::unorm16(col[z]);
             if (exact) exact[z * slice + i] = col[z];
         }
+    });
+    return 0;
+}
+
+}  // extern "C"
+
+// ---- quarter-resolution cloud pass ------------------------------------------
+extern "C" {
+
+// CheckerboardGen.comp: out (w/2) x (h/2); depth NULL = 1
+int oracle_cloud_checkerboard(const float* depth, int w, int h, double* out) {
+    orc::checkerboard(depth, orc::quarter_dims(w, h), out);
+    return 0;
+}
+
+// VolumetricCloudIndexGen.comp from a checkerboard depth: out[2] per quarter texel
+int oracle_cloud_index(const double* cb, int w, int h, float z_near, float z_far, int base, double* out) {
+    orc::index_gen(cb, orc::quarter_dims(w, h), orc::LinearDepth(z_near, z_far), base, out);
+    return 0;
+}
+
+// The raymarch of quarter texels (pixels[i] = y * qw + x, or all) of the
+// viewport `v` (width / height = the viewport) at the checkerboard texels the
+// index selects.
+int oracle_cloud_render_quarter(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                                const skyr_cloud_material* m, const skyr_cloud_textures* tx, const skyr_cloud_view* v,
+                                const skyr_lut_sizes* s, const double* tlut_in, const double* apl_in,
+                                const double* apt_in, const float* blue_noise, const double* index, const double* cb,
+                                const int* pixels, int n, int threads, double* out_rgba, double* out_dist) {
+    orc::AtmosphereOracle<double> O{orc::derive_atmosphere<double>(*atmo)};
+    orc::Image<double> tl = image_from<double>(tlut_in, s->transmittance_width, s->transmittance_height);
+    int W = s->aerial_perspective_width, H = s->aerial_perspective_height, D = s->aerial_perspective_depth;
+    orc::Image<double> al = image_from<double>(apl_in, W, H, D), at = image_from<double>(apt_in, W, H, D);
+    auto C = cloud_oracle(O, atmo, cp, m, tx, v);
+    C->tlut = &tl;
+    C->ap_lum = &al;
+    C->ap_trans = &at;
+    C->blue_noise = blue_noise;
+    orc::QuarterDims Q = orc::quarter_dims(v->width, v->height);
+    parallel_for(n, threads, [&](int i) {
+        int p = pixels ? pixels[i] : i;
+        int x = p % Q.qw, y = p / Q.qw;
+        int dx, dy;
+        orc::index_offset(unsigned(int(index[2 * (size_t)p])) & 3u, dx, dy);
+        int cx = 2 * x + dx, cy = 2 * y + dy;
+        double rgba[4], dist;
+        C->PixelAt((cx + 0.5) / Q.hw, (cy + 0.5) / Q.hh, float(cb[(size_t)cy * Q.hw + cx]), x, y, rgba, dist);
+        for (int k = 0; k < 4; ++k) out_rgba[4 * (size_t)i + k] = rgba[k];
+        if (out_dist) out_dist[i] = dist;
+    });
+    return 0;
+}
+
+// VolumetricCloudReconstruct.comp over the half-resolution image (out[4] per texel)
+int oracle_cloud_reconstruct(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
+                             const skyr_cloud_material* m, const skyr_cloud_textures* tx, const skyr_cloud_view* v,
+                             const float* reproject, float z_near, float z_far, int history, const double* cb,
+                             const double* index, const double* render, const double* rdist, const double* previous,
+                             int threads, double* out) {
+    orc::CloudFrame<double> F = orc::derive_cloud_frame<double>(*atmo, *cp, *m, *tx, *v);
+    orc::QuarterDims Q = orc::quarter_dims(v->width, v->height);
+    orc::LinearDepth LD(z_near, z_far);
+    orc::M4<double> rp = orc::mat_from_floats<double>(reproject);
+    parallel_for(Q.hw * Q.hh, threads, [&](int i) {
+        orc::reconstruct_texel(F, Q, LD, rp, history != 0 && previous != nullptr, cb, index, render, rdist, previous,
+                               i % Q.hw, i / Q.hw, out + 4 * (size_t)i);
+    });
+    return 0;
+}
+
+// VolumetricCloudUpscale.comp over the viewport (hdr_in / out 4 per pixel; depth NULL = 1)
+int oracle_cloud_upscale(int w, int h, const float* depth, float z_near, float z_far, const double* cb,
+                         const double* rec, const double* hdr_in, int threads, double* out) {
+    orc::QuarterDims Q = orc::quarter_dims(w, h);
+    orc::LinearDepth LD(z_near, z_far);
+    parallel_for(h, threads, [&](int y) {
+        for (int x = 0; x < w; ++x) orc::upscale_pixel(Q, LD, depth, cb, rec, hdr_in, x, y, out + 4 * ((size_t)y * w + x));
     });
     return 0;
 }

@@ -437,7 +437,14 @@ struct CloudOracle {
     // main (VolumetricCloudRender.comp:139-210) at full resolution: pixel
     // (px, py) of a w x h image with window depth `depth`.
     void Pixel(int px, int py, int w, int h, float depth, T out_rgba[4], T& out_dist) const {
-        T u = (T(px) + T(0.5)) / T(w), v = (T(py) + T(0.5)) / T(h);
+        PixelAt((T(px) + T(0.5)) / T(w), (T(py) + T(0.5)) / T(h), depth, px, py, out_rgba, out_dist);
+    }
+
+    // The same for the ray through screen (u, v) at window depth `depth`, its
+    // blue noise taken at pixel (nx, ny): the quarter-resolution pass
+    // raymarches checkerboard texels and indexes the noise by its own pixel
+    // (VolumetricCloudRender.comp:140-166).
+    void PixelAt(T u, T v, float depth, int nx, int ny, T out_rgba[4], T& out_dist) const {
         V3<T> frag = projective_mul(F.inv_mvp, V3<T>(u * T(2) - T(1), v * T(2) - T(1), T(depth) * T(2) - T(1)));
         V3<T> view = normalize(frag - F.cam);
         T r = F.cam.z + F.R;
@@ -455,7 +462,7 @@ struct CloudOracle {
         c.trans = T(1);
         c.trans_sum = c.wsum = T(0);
         c.sun = c.env = T(0);
-        T noise = T(blue_noise[(py & 63) * 64 + (px & 63)]);
+        T noise = T(blue_noise[(ny & 63) * 64 + (nx & 63)]);
         T jitter = fractg(noise + F.frame_id * T(0.61803398875));
         c.t = it[0][0] + c.step * jitter;
         for (unsigned k = n; k != 0; --k, c.t += c.step) {

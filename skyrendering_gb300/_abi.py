@@ -287,6 +287,31 @@ _SIGNATURES.update({
 })
 
 
+# ---------------------------------------------------------------------------
+# skyr_cloud_quarter.h
+# ---------------------------------------------------------------------------
+class CloudTemporalFrame(C.Structure):
+    _fields_ = [("reproject", f16), ("z_near", C.c_float), ("z_far", C.c_float), ("base_shading_index", C.c_int),
+                ("has_previous", C.c_int)]
+
+
+class CloudQuarterBuffers(C.Structure):
+    _fields_ = [("checkerboard_depth", P), ("index_linear_depth", P), ("render_rgba", P), ("render_distance", P),
+                ("previous_reconstruct", P), ("reconstruct", P)]
+
+
+STRUCT_IDS.update({17: CloudTemporalFrame, 18: CloudQuarterBuffers})
+_SIGNATURES.update({
+    "skyr_cloud_temporal_frame_derive": (C.c_int, [C.POINTER(AtmosphereParameters), C.POINTER(CloudView),
+                                                   C.POINTER(CloudView), C.POINTER(C.c_float), C.c_float, C.c_float,
+                                                   C.c_int, C.POINTER(CloudTemporalFrame)]),
+    "skyr_cloud_render_quarter": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                            C.POINTER(CloudMaterial), C.POINTER(CloudTextures), C.POINTER(CloudView),
+                                            C.POINTER(LutSizes), P, P, P, P, P, C.POINTER(CloudTemporalFrame),
+                                            C.POINTER(CloudQuarterBuffers), P]),
+})
+
+
 # allocation-free LUT set (static device scratch, SKYR_NOALLOC_MAX_SETS sets)
 SKYR_NOALLOC_MAX_SETS = 256
 _SIGNATURES["skyr_update_lut_set_noalloc"] = (

@@ -8,6 +8,9 @@
 * ``CloudShadow`` ~ VolumetricCloud::RenderShadow (VolumetricCloud.cpp:282-325)
   with its state: the raw shadow maps used in turn, the blurred map, the
   shadow froxel and the previous frame's light transform.
+* ``CloudViewport`` ~ VolumetricCloud::Render's quarter-resolution pass with
+  its ViewportData (VolumetricCloud.cpp:120-136,327-423): checkerboard depth,
+  index, quarter-resolution raymarch, temporal reconstruction, upscale.
 """
 from __future__ import annotations
 
@@ -190,6 +193,75 @@ def detach_froxel(view: _abi.CloudView) -> _abi.CloudView:
     view.shadow_froxel = None
     view.shadow_froxel_width = view.shadow_froxel_height = view.shadow_froxel_depth = 0
     return view
+
+
+def temporal_frame(atmosphere: _abi.AtmosphereParameters, view: _abi.CloudView,
+                   previous_view: _abi.CloudView | None = None, wind_delta=None, z_near: float = 0.1,
+                   z_far: float = 1000.0, frame_index: int = 0) -> _abi.CloudTemporalFrame:
+    """The temporal constants of VolumetricCloud::Update (host only); the
+    planes default to the reference Camera's (Camera.h:39-40)."""
+    out = _abi.CloudTemporalFrame()
+    wind = None if wind_delta is None else (C.c_float * 2)(*wind_delta)
+    _abi.call("skyr_cloud_temporal_frame_derive", C.byref(atmosphere), C.byref(view),
+              None if previous_view is None else C.byref(previous_view), wind, z_near, z_far, frame_index,
+              C.byref(out))
+    return out
+
+
+class CloudViewport:
+    """The buffers of one viewport (ViewportData): half-resolution checkerboard
+    depth and two reconstructions used in turn, quarter-resolution index,
+    raymarch output and distance."""
+
+    def __init__(self, ctx: Context, width: int, height: int):
+        self.ctx, self.width, self.height = ctx, width, height
+        hw, hh = width // 2, height // 2
+        qw, qh = hw // 2, hh // 2
+        dev = dict(device="cuda")
+        self.checkerboard = torch.zeros((hh, hw), dtype=torch.float32, **dev)
+        self.index = torch.zeros((qh, qw, 2), dtype=torch.float32, **dev)
+        self.render_rgba = torch.zeros((qh, qw, 4), dtype=torch.float16, **dev)
+        self.render_distance = torch.zeros((qh, qw), dtype=torch.float32, **dev)
+        self.reconstruct = [torch.zeros((hh, hw, 4), dtype=torch.float16, **dev) for _ in range(2)]
+        self.current = 0        # the reconstruction written last
+        self.frames = 0
+        self.previous_view: _abi.CloudView | None = None
+
+    def buffers(self, history: bool = True) -> _abi.CloudQuarterBuffers:
+        b = _abi.CloudQuarterBuffers()
+        b.checkerboard_depth = self.checkerboard.data_ptr()
+        b.index_linear_depth = self.index.data_ptr()
+        b.render_rgba = self.render_rgba.data_ptr()
+        b.render_distance = self.render_distance.data_ptr()
+        k = 1 - self.current
+        b.previous_reconstruct = self.reconstruct[self.current].data_ptr() if (history and self.frames) else None
+        b.reconstruct = self.reconstruct[k].data_ptr()
+        return b
+
+    @property
+    def reconstruction(self) -> torch.Tensor:
+        return self.reconstruct[self.current]
+
+    def render(self, cloud: "VolumetricCloud", atmosphere: _abi.AtmosphereParameters, view: _abi.CloudView,
+               sizes: _abi.LutSizes, luts: LutSet, blue_noise: torch.Tensor, depth: torch.Tensor | None = None,
+               hdr: torch.Tensor | None = None, wind_delta=None, z_near: float = 0.1, z_far: float = 1000.0,
+               history: bool = True) -> _abi.CloudTemporalFrame:
+        """One frame of VolumetricCloud::Render (all five passes; the upscale
+        composites into `hdr` when given) and the swap of the reconstructions."""
+        assert view.width == self.width and view.height == self.height
+        prev = self.previous_view if (history and self.frames) else None
+        # uBaseShadingIndex and the raymarch's jitter both follow the view's frame id
+        frame = temporal_frame(atmosphere, view, prev, wind_delta, z_near, z_far, int(view.frame_id))
+        b = self.buffers(history)
+        _abi.call("skyr_cloud_render_quarter", self.ctx.handle, C.byref(atmosphere), C.byref(cloud.params),
+                  C.byref(cloud.material), C.byref(cloud.textures), C.byref(view), C.byref(sizes),
+                  _ptr(luts.transmittance), _ptr(luts.aerial_perspective_luminance),
+                  _ptr(luts.aerial_perspective_transmittance), _ptr(blue_noise), _ptr(depth), C.byref(frame),
+                  C.byref(b), _ptr(hdr))
+        self.current = 1 - self.current
+        self.frames += 1
+        self.previous_view = _abi.CloudView.from_buffer_copy(view)
+        return frame
 
 
 def blue_noise_tile(seed: int = 0x5EED) -> torch.Tensor:

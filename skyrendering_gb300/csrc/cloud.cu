@@ -71,6 +71,20 @@ void matmul4d(const double* a, const double* b, double* c) {  // column-major c 
         }
 }
 
+// The local z-up frame of VolumetricCloud::Update (VolumetricCloud.cpp:188-201):
+// columns front, right, up and the surface point below the camera.
+void cloud_local_frame(double R, const float cam_world[3], double model[16]) {
+    D3 center{0.0, -R, 0.0};
+    D3 cam{cam_world[0], cam_world[1], cam_world[2]};
+    D3 up = normd(sub(cam, center));
+    D3 origin = add(center, mul(up, R));
+    D3 front = normd(crossd(up, D3{1.0, 0.0, 0.0}));
+    D3 right = normd(crossd(up, front));
+    const double m[16] = {front.x, front.y, front.z, 0, right.x, right.y, right.z, 0,
+                          up.x,    up.y,    up.z,    0, origin.x, origin.y, origin.z, 1};
+    for (int i = 0; i < 16; ++i) model[i] = m[i];
+}
+
 namespace {
 
 int fill_tex(DTex& t, const void* p, const skyr_noise_texture_desc& d, bool border, bool required,
@@ -412,9 +426,21 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, 
     int py = blockIdx.y * (tile_h * warps_y) + (warp / warps_x) * tile_h + (lane / tile_w);
     if (px >= C.width || py >= C.height) return;
     size_t pix = (size_t)py * C.width + px;
-    float u = ((float)px + 0.5f) / (float)C.width, v = ((float)py + 0.5f) / (float)C.height;
+    float u, v, e;
+    if (C.cb_index) {
+        // VolumetricCloudRender.comp:140-146: the checkerboard texel chosen
+        // for this frame gives the ray; (px, py) the noise and the output
+        unsigned idx = (unsigned)(int)__ldg(&C.cb_index[pix].x) & 3u;
+        int cx = 2 * px + (int)(((idx + 1u) >> 1) & 1u), cy = 2 * py + (int)(((idx + 2u) >> 1) & 1u);
+        u = ((float)cx + 0.5f) / (float)C.cb_w;
+        v = ((float)cy + 0.5f) / (float)C.cb_h;
+        e = 2.f * (__ldg(C.cb_depth + (size_t)cy * C.cb_w + cx) - 1.f);
+    } else {
+        u = ((float)px + 0.5f) / (float)C.width;
+        v = ((float)py + 0.5f) / (float)C.height;
+        e = depth ? 2.f * (__ldg(depth + pix) - 1.f) : 0.f;
+    }
     float x = 2.f * u - 1.f, y = 2.f * v - 1.f;
-    float e = depth ? 2.f * (__ldg(depth + pix) - 1.f) : 0.f;
     float3 dir = C.a0 * x + C.a1 * y + C.a2 * e + C.af;
     float wv = fmaf(C.w0, x, fmaf(C.w1, y, fmaf(C.w2, e, C.wf)));
     float len = sqrtf(dot3(dir, dir));
@@ -509,7 +535,8 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
                     const skyr_cloud_textures* textures, const skyr_cloud_view* view, const skyr_lut_sizes* sizes,
                     const void* transmittance, const void* aerial_perspective_luminance,
                     const void* aerial_perspective_transmittance, const float* blue_noise, const float* depth,
-                    void* out_rgba, float* out_distance, unsigned long long* counters) {
+                    void* out_rgba, float* out_distance, unsigned long long* counters,
+                    const CloudCheckerboard* checkerboard) {
     if (!ctx) return set_error(SKYR_EINVAL, "null context");
     if (!atmosphere || !cloud || !material || !textures || !view || !sizes)
         return set_error(SKYR_EINVAL, "null parameter block");
@@ -530,12 +557,21 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
     CloudConsts C;
     MaterialConsts M;
     if (int st = derive_cloud_consts(*atmosphere, *cloud, *material, *textures, *view, *sizes, C, M)) return st;
+    if (checkerboard) {
+        C.width = checkerboard->quarter_w;
+        C.height = checkerboard->quarter_h;
+        C.cb_index = checkerboard->index;
+        C.cb_depth = checkerboard->depth;
+        C.cb_w = checkerboard->half_w;
+        C.cb_h = checkerboard->half_h;
+        depth = nullptr;
+    }
     AtmoConsts A;
     derive_atmo_consts(*atmosphere, A);
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     const int tile_w = ctx->tuning.cloud_tile_width, warps_x = ctx->tuning.cloud_block_warps_x;
     const int bw = tile_w * warps_x, bh = (32 / tile_w) * (4 / warps_x);
-    dim3 grid((view->width + bw - 1) / bw, (view->height + bh - 1) / bh);
+    dim3 grid((C.width + bw - 1) / bw, (C.height + bh - 1) / bh);
     const float4* T = reinterpret_cast<const float4*>(transmittance);
     auto launch = [&](auto tag, auto minb) {
         using S = decltype(tag);

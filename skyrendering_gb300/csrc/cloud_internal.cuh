@@ -175,6 +175,19 @@ struct CloudConsts {
     const uint16_t* froxel;  // shadow froxel, or null for a visibility of 1
     int fx_w, fx_h, fx_d;
     float inv_froxel_max_distance;
+    // checkerboard mode (the quarter-resolution pass): pixel (x, y) of the
+    // width x height raymarch is checkerboard texel 2 (x, y) + IndexToOffset(index)
+    // of the cb_w x cb_h checkerboard depth; null: a full-resolution raymarch
+    const float2* cb_index;
+    const float* cb_depth;
+    int cb_w, cb_h;
+};
+
+// The checkerboard input of a quarter-resolution raymarch.
+struct CloudCheckerboard {
+    const float2* index;  // quarter: (index, linear depth)
+    const float* depth;   // half: checkerboard depth
+    int half_w, half_h, quarter_w, quarter_h;
 };
 
 // SampleRayScatterVisibility (VolumetricCloudShadowInterface.glsl:10-13): the
@@ -208,6 +221,8 @@ __device__ __forceinline__ float froxel_visibility(const CloudConsts& C, float u
 // Column-major 4x4 helpers of the host derivations (double).
 bool invert4d(const double* m, double* out);
 void matmul4d(const double* a, const double* b, double* c);
+// The local z-up cloud frame of a camera (column-major model matrix).
+void cloud_local_frame(double R, const float cam_world[3], double model[16]);
 
 int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud_parameters& cp,
                         const skyr_cloud_material& m, const skyr_cloud_textures& tex, const skyr_cloud_view& v,

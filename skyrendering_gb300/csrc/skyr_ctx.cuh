@@ -58,7 +58,8 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
                     const skyr_cloud_textures* textures, const skyr_cloud_view* view, const skyr_lut_sizes* sizes,
                     const void* transmittance, const void* aerial_perspective_luminance,
                     const void* aerial_perspective_transmittance, const float* blue_noise, const float* depth,
-                    void* out_rgba, float* out_distance, unsigned long long* counters);
+                    void* out_rgba, float* out_distance, unsigned long long* counters,
+                    const struct CloudCheckerboard* checkerboard = nullptr);
 // Create the internal streams / events of a context if needed.
 int ensure_aux_streams(skyr_ctx* ctx);
 }  // namespace skyr

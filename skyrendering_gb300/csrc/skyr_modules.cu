@@ -5,6 +5,7 @@
 #include "../../include/skyr_surrogate.h"
 #include "../../include/skyr_pathtrace.h"
 #include "../../include/skyr_cloud_shadow.h"
+#include "../../include/skyr_cloud_quarter.h"
 #include "skyr_ctx.cuh"
 
 namespace skyr {
@@ -87,6 +88,8 @@ size_t skyr_struct_size_ext(int which) {
         case 14: return sizeof(skyr_tuning);
         case 15: return sizeof(skyr_cloud_shadow_sizes);
         case 16: return sizeof(skyr_cloud_light_frame);
+        case 17: return sizeof(skyr_cloud_temporal_frame);
+        case 18: return sizeof(skyr_cloud_quarter_buffers);
         default: return 0;
     }
 }

@@ -8,6 +8,7 @@ times on one stream, synchronise and exit 0.
     python -m skyrendering_gb300.profile_cases lattice --iters 2
     python -m skyrendering_gb300.profile_cases mlp --iters 3
     python -m skyrendering_gb300.profile_cases shadow --iters 3
+    python -m skyrendering_gb300.profile_cases quarter --iters 3
 
 Cases (seeded synthetic inputs from workloads.py):
   luts   the plain LUT set (T 256x64, MS 32x32, SV 192x108, AP 32^3) of the
@@ -24,6 +25,9 @@ Cases (seeded synthetic inputs from workloads.py):
          seeded random records.
   shadow the cloud shadow passes of the 1920x1080 frame (512^2 map blended
          into the previous frame's, blur, 160x90x128 froxel).
+  quarter the quarter-resolution cloud pass of that frame (checkerboard,
+         index, 480x270 raymarch, 960x540 reconstruction with history,
+         upscale into an HDR target; empty depth buffer).
 The per-iteration CUDA-event time is printed for orientation; it is not a
 benchmark figure (bench.py is).
 """
@@ -125,9 +129,33 @@ def shadow_case(ctx):
     return lambda: sh.render(vc, atmo, view, bn, wind_delta=(0.01, 0.0))
 
 
+def quarter_case(ctx):
+    from .cloud import CloudViewport
+
+    cam = W.frame_camera()
+    atmo, sizes, render, luts, lut_step = lut_case(ctx, cam)
+    lut_step()
+    tex = {"cloud_map": NoiseTexture(W.cloud_map_desc()).generate(ctx),
+           "detail": NoiseTexture(W.base_noise_desc()).generate(ctx)}
+    material = W.frame_material()
+    prepare_textures(ctx, material.type, tex)
+    bn = blue_noise_tile().cuda()
+    view = W.frame_view(cam, SUN_ZENITH)
+    vc = VolumetricCloud(ctx, W.frame_cloud_parameters(), material, textures_struct(**tex))
+    vp = CloudViewport(ctx, view.width, view.height)
+    hdr = torch.zeros((view.height, view.width, 4), dtype=torch.float16, device="cuda")
+    vp.render(vc, atmo, view, sizes, luts, bn, hdr=hdr, z_near=cam.z_near, z_far=cam.z_far)
+
+    def step():
+        view.frame_id = float((int(view.frame_id) + 1) & 0xFF)
+        vp.render(vc, atmo, view, sizes, luts, bn, hdr=hdr, z_near=cam.z_near, z_far=cam.z_far)
+
+    return step
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["luts", "cloud", "pt", "surrogate", "lattice", "mlp", "shadow"])
+    ap.add_argument("case", choices=["luts", "cloud", "pt", "surrogate", "lattice", "mlp", "shadow", "quarter"])
     ap.add_argument("--iters", type=int, default=3)
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--global-majorant", action="store_true")
@@ -146,6 +174,8 @@ def main(argv=None):
         step = surrogate_case(ctx, a.size, a.case)
     elif a.case == "shadow":
         step = shadow_case(ctx)
+    elif a.case == "quarter":
+        step = quarter_case(ctx)
     else:
         step = mlp_case(ctx)
     torch.cuda.synchronize()
