@@ -467,8 +467,9 @@ def quarter_pass(ctx, fs, lut_graph, reps: int = 20):
     the temporal reconstruction at 960x540 and the upscale composited into an
     RGBA16F HDR target, on an empty depth buffer in steady state (the previous
     frame's reconstruction as history).  Timed as one CUDA graph with and
-    without the upscale, and inside the production frame: LUT set + shadow
-    passes + quarter pass reading the shadow froxel, L2 flushed between frames."""
+    without the upscale, and inside the production frame: LUT set +
+    environment cube + shadow passes + quarter pass reading the shadow froxel,
+    L2 flushed between frames."""
     import ctypes as C
 
     import torch
@@ -527,14 +528,34 @@ def quarter_pass(ctx, fs, lut_graph, reps: int = 20):
                   C.byref(fs.vc.material), C.byref(fs.vc.textures), C.byref(view), C.byref(sh.sizes),
                   C.byref(shadow_frame), _ptr(fs.bn), _ptr(prev), _ptr(cur), _ptr(sh.map), _ptr(sh.froxel))
     shadow_graph = cap.graph
+    # AtmosphereRenderer::Render's environment cube (128^2 x 6 RGBA16F + mips) and IBL::Precompute (SH,
+    # 5 prefiltered roughness levels), every frame in the reference
+    from skyrendering_gb300.atmosphere import (environment_cube, environment_prefilter, environment_seamless,
+                                               environment_sh)
+
+    env_out = torch.empty((_abi.lib().skyr_environment_cube_level_offset(128, 8), 4), dtype=torch.float16,
+                          device="cuda")
+    env_seam = torch.empty((_abi.lib().skyr_environment_seamless_level_offset(128, 8), 4), dtype=torch.float32,
+                           device="cuda")
+    env_sh = torch.empty((9, 4), dtype=torch.float32, device="cuda")
+    env_pre = torch.empty((_abi.lib().skyr_environment_cube_level_offset(128, 5), 4), dtype=torch.float16,
+                          device="cuda")
+    with B.capture(ctx) as cap:
+        environment_cube(ctx, fs.atmo, fs.render, fs.sizes, fs.luts, 128, out=env_out)
+        environment_seamless(ctx, env_out, 128, 8, out=env_seam)
+        environment_sh(ctx, env_seam, 128, 8, out=env_sh)
+        environment_prefilter(ctx, env_seam, 128, 8, 128, 5, out=env_pre)
+    env_graph = cap.graph
+    t_env = timed(env_graph)
     fview = sh.attach(_abi.CloudView.from_buffer_copy(view))
     with B.capture(ctx) as cap:
         call(fview, hdr)
     quarter_graph = cap.graph
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(reps)]
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(reps)]
     for _ in range(3):
         lut_graph.launch()
+        env_graph.launch()
         shadow_graph.launch()
         quarter_graph.launch()
     torch.cuda.synchronize()
@@ -543,24 +564,30 @@ def quarter_pass(ctx, fs, lut_graph, reps: int = 20):
         ev[i][0].record(stream)
         lut_graph.launch()
         ev[i][1].record(stream)
-        shadow_graph.launch()
+        env_graph.launch()
         ev[i][2].record(stream)
-        quarter_graph.launch()
+        shadow_graph.launch()
         ev[i][3].record(stream)
+        quarter_graph.launch()
+        ev[i][4].record(stream)
     torch.cuda.synchronize()
     ctx.check_status()
     res = {"viewport": f"{W_}x{H_}", "raymarch": f"{W_ // 4}x{H_ // 4} checkerboard texels",
            "reconstruct": f"{W_ // 2}x{H_ // 2}", "depth": "empty (1)", "history": "previous reconstruction",
            "pass_ms": t_full, "pass_without_upscale_ms": t_no_up, "upscale_ms": t_full - t_no_up,
-           "production_frame_ms": statistics.mean(a.elapsed_time(d) for a, _, _, d in ev),
+           "environment_and_ibl_us": t_env * 1000.0,
+           "production_frame_ms": statistics.mean(e[0].elapsed_time(e[4]) for e in ev),
            "production_frame_parts_ms": {
-               "lut_set": statistics.mean(a.elapsed_time(b_) for a, b_, _, _ in ev),
-               "shadow_passes": statistics.mean(b_.elapsed_time(c) for _, b_, c, _ in ev),
-               "quarter_pass": statistics.mean(c.elapsed_time(d) for _, _, c, d in ev)},
+               "lut_set": statistics.mean(e[0].elapsed_time(e[1]) for e in ev),
+               "environment_cube_and_ibl": statistics.mean(e[1].elapsed_time(e[2]) for e in ev),
+               "shadow_passes": statistics.mean(e[2].elapsed_time(e[3]) for e in ev),
+               "quarter_pass": statistics.mean(e[3].elapsed_time(e[4]) for e in ev)},
            "kernels_per_pass": 5,
-           "note": "production frame = LUT set + shadow passes + quarter-resolution cloud pass with the froxel, "
-                   "three CUDA graphs, L2 flushed between frames; the composite is the upscale's"}
-    for g in (full, no_upscale, shadow_graph, quarter_graph):
+           "note": "production frame = LUT set + environment cube (128^2 x 6 + mips, SH, 5 prefiltered levels) + "
+                   "shadow passes + "
+                   "quarter-resolution cloud pass with the froxel, four CUDA graphs, L2 flushed between frames; "
+                   "the composite is the upscale's"}
+    for g in (full, no_upscale, shadow_graph, quarter_graph, env_graph):
         g.close()
     return res
 

@@ -654,3 +654,66 @@ def upscale(w: int, h: int, depth, z_near: float, z_far: float, cb, rec, hdr_in,
                                     nthreads or threads(), _dp(out.reshape(-1)))
     assert rc == 0
     return out
+
+
+# ---------------------------------------------------------------------------
+# environment cube
+# ---------------------------------------------------------------------------
+def _declare_env(lb):
+    lb.oracle_environment_cube.restype = C.c_int
+    lb.oracle_environment_cube.argtypes = [P, P, P, D, D, D, C.c_int, C.c_int, D]
+    lb.oracle_environment_seamless.restype = C.c_int
+    lb.oracle_environment_seamless.argtypes = [D, C.c_int, C.c_int, D]
+    lb.oracle_environment_sh.restype = C.c_int
+    lb.oracle_environment_sh.argtypes = [D, C.c_int, C.c_int, D]
+    lb.oracle_environment_prefilter.restype = C.c_int
+    lb.oracle_environment_prefilter.argtypes = [D, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, D]
+
+
+_EXT.append(_declare_env)
+
+
+def environment_cube(params, render, sizes, transmittance, sky_view_luminance, sky_view_transmittance, size: int,
+                     nthreads: int | None = None) -> np.ndarray:
+    """Level 0 of the environment cube: [6][size][size][4] (a = 0)."""
+    arrs = [_f64(a).reshape(-1) for a in (transmittance, sky_view_luminance, sky_view_transmittance)]
+    out = np.zeros((6, size, size, 4))
+    rc = lib().oracle_environment_cube(_ref(params), _ref(render), _ref(sizes), *[_dp(a) for a in arrs], size,
+                                       nthreads or threads(), _dp(out.reshape(-1)))
+    assert rc == 0
+    return out
+
+
+def box_mip(level: np.ndarray) -> np.ndarray:
+    """glGenerateTextureMipmap's 2x2 box filter of [6][s][s][4] half values,
+    rounded to half: the next level."""
+    a = level.astype(np.float64)
+    m = ((a[:, 0::2, 0::2] + a[:, 0::2, 1::2]) + (a[:, 1::2, 0::2] + a[:, 1::2, 1::2])) * 0.25
+    return m.astype(np.float16)
+
+
+def environment_sh(cube_texels: np.ndarray, size: int, levels: int) -> np.ndarray:
+    """[9][3] SH coefficients of a cube given as its flat texels ([n][4], all levels)."""
+    c = _f64(cube_texels).reshape(-1)
+    out = np.zeros((9, 3))
+    assert lib().oracle_environment_sh(_dp(c), size, levels, _dp(out.reshape(-1))) == 0
+    return out
+
+
+def environment_prefilter(cube_texels: np.ndarray, size: int, levels: int, n: int, roughness: float,
+                          nthreads: int | None = None) -> np.ndarray:
+    """[6][n][n][3]: one prefiltered level of side n."""
+    c = _f64(cube_texels).reshape(-1)
+    out = np.zeros((6, n, n, 3))
+    assert lib().oracle_environment_prefilter(_dp(c), size, levels, n, roughness, nthreads or threads(),
+                                              _dp(out.reshape(-1))) == 0
+    return out
+
+
+def environment_seamless(cube_texels: np.ndarray, size: int, levels: int) -> np.ndarray:
+    """The seamless copy ([n][4], apron texels from the adjacent faces) of a cube's flat texels."""
+    c = _f64(cube_texels).reshape(-1)
+    total = sum(6 * (max(size >> l, 1) + 2) ** 2 for l in range(levels))
+    out = np.zeros((total, 4))
+    assert lib().oracle_environment_seamless(_dp(c), size, levels, _dp(out.reshape(-1))) == 0
+    return out

@@ -13,6 +13,7 @@
 #include "oracle_pathtrace.hpp"
 #include "oracle_shadow.hpp"
 #include "oracle_quarter.hpp"
+#include "oracle_environment.hpp"
 #include "../include/skyr_cloud_shadow.h"
 #include "../include/skyr_surrogate.h"
 
@@ -856,6 +857,83 @@ int oracle_cloud_upscale(int w, int h, const float* depth, float z_near, float z
     parallel_for(h, threads, [&](int y) {
         for (int x = 0; x < w; ++x) orc::upscale_pixel(Q, LD, depth, cb, rec, hdr_in, x, y, out + 4 * ((size_t)y * w + x));
     });
+    return 0;
+}
+
+}  // extern "C"
+
+// ---- environment cube --------------------------------------------------------
+extern "C" {
+
+// Level 0 of a size^2 x 6 environment cube (out[4] per texel, a = 0), layout
+// as skyr_environment_cube.
+int oracle_environment_cube(const skyr_atmosphere_parameters* p, const skyr_atmosphere_render_parameters* r,
+                            const skyr_lut_sizes* s, const double* t_in, const double* svl_in, const double* svt_in,
+                            int size, int threads, double* out) {
+    orc::AtmosphereOracle<double> O{orc::derive_atmosphere<double>(*p)};
+    orc::RenderFrame<double> F = orc::derive_render_frame<double>(*p, *r);
+    orc::Image<double> tl = image_from<double>(t_in, s->transmittance_width, s->transmittance_height);
+    orc::Image<double> svl = image_from<double>(svl_in, s->sky_view_width, s->sky_view_height);
+    orc::Image<double> svt = image_from<double>(svt_in, s->sky_view_width, s->sky_view_height);
+    parallel_for(6 * size, threads, [&](int row) {
+        int face = row / size, y = row % size;
+        for (int x = 0; x < size; ++x) {
+            orc::V3<double> c = orc::environment_cube_texel(O, F, tl, svl, svt, size, face, x, y);
+            double* o = out + 4 * (((size_t)face * size + y) * size + x);
+            o[0] = c.x;
+            o[1] = c.y;
+            o[2] = c.z;
+            o[3] = 0.0;
+        }
+    });
+    return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// EnvRadianceSH.comp on a cube (4 doubles per texel, `levels` levels): out[9][3]
+int oracle_environment_sh(const double* cube, int size, int levels, double* out) {
+    orc::CubeImage C{cube, size, levels};
+    double r[9][3];
+    orc::environment_sh(C, r);
+    for (int k = 0; k < 9; ++k)
+        for (int c = 0; c < 3; ++c) out[3 * k + c] = r[k][c];
+    return 0;
+}
+
+// PrefilterRadiance.comp, one level of side n and roughness r: out[6][n][n][3]
+int oracle_environment_prefilter(const double* cube, int size, int levels, int n, double roughness, int threads,
+                                 double* out) {
+    orc::CubeImage C{cube, size, levels};
+    parallel_for(6 * n, threads, [&](int row) {
+        int face = row / n, y = row % n;
+        for (int x = 0; x < n; ++x) {
+            orc::V3<double> c = orc::prefilter_texel(C, n, roughness, face, x, y);
+            double* o = out + 3 * (((size_t)face * n + y) * n + x);
+            o[0] = c.x;
+            o[1] = c.y;
+            o[2] = c.z;
+        }
+    });
+    return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// The seamless copy of a cube (4 doubles per texel in and out), layout as skyr_environment_seamless.
+int oracle_environment_seamless(const double* cube, int size, int levels, double* out) {
+    orc::CubeImage C{cube, size, levels};
+    size_t k = 0;
+    for (int l = 0; l < levels; ++l) {
+        int n = C.side(l);
+        for (int face = 0; face < 6; ++face)
+            for (int j = -1; j <= n; ++j)
+                for (int i = -1; i <= n; ++i, ++k) orc::cube_texel(C, l, face, i, j, out + 4 * k);
+    }
     return 0;
 }
 

@@ -16,6 +16,7 @@
 
 #include "../include/skyr_pathtrace.h"
 #include "oracle_cloud.hpp"
+#include "oracle_environment.hpp"
 #include "oracle_noise.hpp"
 
 namespace orc {
@@ -259,30 +260,7 @@ struct PathTracerOracle {
     V3<T> sun_illuminance(V3<T> pos) const { return Cl.SunVisibilityAt(pos) * O.A.solar_illuminance; }
 
     // ENVIRONMENT_LUMINANCE (AtmosphereRenderer.glsl:250-273) for a world direction
-    V3<T> environment(V3<T> w) const {
-        T cos_lat = dot(Env.F.up, w);
-        V3<T> lon = w - Env.F.up * cos_lat;
-        T l2 = dot(lon, lon);
-        T cos_lon = l2 == T(0) ? T(1) : dot(lon / std::sqrt(l2), Env.F.front);
-        T r = Env.F.camera_earth_center_distance;
-        T hd = std::acos(std::sqrt(r * r - O.A.bottom_radius * O.A.bottom_radius) / r);
-        T hu = T(kPi) - hd;
-        T lat = std::acos(clampg(cos_lat, T(-1), T(1)));
-        T xl;
-        if (lat < hu) xl = T(0.5) - T(0.5) * std::sqrt(T(1) - lat / hu);
-        else xl = std::sqrt((lat - hu) / hd) * T(0.5) + T(0.5);
-        T xo = std::sqrt(std::max(T(0.5) - T(0.5) * cos_lon, T(0)));
-        T u = T(0.5) / T(svl->w) + xo * (T(1) - T(1) / T(svl->w));
-        T v = T(0.5) / T(svl->h) + xl * (T(1) - T(1) / T(svl->h));
-        V3<T> lum = sample_linear_clamp(*svl, u, v);
-        V3<T> tr = sample_linear_clamp(*svt, u, v);
-        if (O.RayIntersectsGround(r, cos_lat)) {
-            T dist = O.DistanceToBottomAtmosphereBoundary(r, cos_lat);
-            V3<T> gp = Env.F.camera_position + w * dist;
-            lum += O.ComputeGroundLuminance(*Cl.tlut, false, Env.F.earth_center, gp, Env.F.sun_direction) * tr;
-        }
-        return lum;
-    }
+    V3<T> environment(V3<T> w) const { return environment_luminance(O, Env.F, *Cl.tlut, *svl, *svt, w); }
 
     V3<T> env_local(V3<T> d) const { return environment(mul_dir(model3, d)); }
 

@@ -312,6 +312,20 @@ _SIGNATURES.update({
 })
 
 
+# ---------------------------------------------------------------------------
+# skyr_environment.h
+# ---------------------------------------------------------------------------
+_SIGNATURES.update({
+    "skyr_environment_cube_level_offset": (C.c_size_t, [C.c_int, C.c_int]),
+    "skyr_environment_cube": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(AtmosphereRenderParameters),
+                                        C.POINTER(LutSizes), P, P, P, C.c_int, C.c_int, P]),
+    "skyr_environment_seamless_level_offset": (C.c_size_t, [C.c_int, C.c_int]),
+    "skyr_environment_seamless": (C.c_int, [P, P, C.c_int, C.c_int, P]),
+    "skyr_environment_sh": (C.c_int, [P, P, C.c_int, C.c_int, P]),
+    "skyr_environment_prefilter": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, C.c_int, P]),
+})
+
+
 # allocation-free LUT set (static device scratch, SKYR_NOALLOC_MAX_SETS sets)
 SKYR_NOALLOC_MAX_SETS = 256
 _SIGNATURES["skyr_update_lut_set_noalloc"] = (

@@ -149,3 +149,68 @@ def update_lut_set(ctx: Context, params, render, sizes: _abi.LutSizes, out: LutS
               _ptr(out.multiscattering), _ptr(out.sky_view_luminance), _ptr(out.sky_view_transmittance),
               _ptr(out.aerial_perspective_luminance), _ptr(out.aerial_perspective_transmittance))
     return out
+
+
+def environment_cube_levels(face_size: int) -> list[tuple[int, int]]:
+    """(offset in half4 texels, side) of each level of a face_size cube."""
+    n = face_size.bit_length()
+    return [(_abi.lib().skyr_environment_cube_level_offset(face_size, l), max(face_size >> l, 1)) for l in range(n)]
+
+
+def environment_cube(ctx: Context, atmosphere: _abi.AtmosphereParameters,
+                     render: _abi.AtmosphereRenderParameters, sizes: _abi.LutSizes, luts: "LutSet",
+                     face_size: int = 128, levels: int | None = None, out: torch.Tensor | None = None,
+                     set_index: int = 0) -> list[torch.Tensor]:
+    """AtmosphereRenderer's environment luminance cube (128^2 x 6 RGBA16F in the
+    reference) with its box-filtered mip chain: one [6][s][s][4] half view per level."""
+    n = face_size.bit_length() if levels is None else levels
+    total = _abi.lib().skyr_environment_cube_level_offset(face_size, n)
+    if total == 0:
+        raise _abi.SkyrError(_abi.SKYR_EINVAL, "environment_cube", "bad face size or level count")
+    if out is None:
+        out = torch.empty((total, 4), dtype=torch.float16, device="cuda")
+    s = set_index
+    _abi.call("skyr_environment_cube", ctx.handle, C.byref(atmosphere), C.byref(render), C.byref(sizes),
+              _ptr(luts.transmittance[s]), _ptr(luts.sky_view_luminance[s]), _ptr(luts.sky_view_transmittance[s]),
+              face_size, n, _ptr(out))
+    views = []
+    for off, side in environment_cube_levels(face_size)[:n]:
+        views.append(out[off:off + 6 * side * side].view(6, side, side, 4))
+    return views
+
+
+def environment_seamless(ctx: Context, cube: torch.Tensor, face_size: int, levels: int,
+                         out: torch.Tensor | None = None) -> torch.Tensor:
+    """The cube's seamless copy (each face with a one-texel apron from its
+    neighbours), float4 texels: the input of the IBL passes."""
+    total = _abi.lib().skyr_environment_seamless_level_offset(face_size, levels)
+    if total == 0:
+        raise _abi.SkyrError(_abi.SKYR_EINVAL, "environment_seamless", "bad face size or level count")
+    if out is None:
+        out = torch.empty((total, 4), dtype=torch.float32, device="cuda")
+    _abi.call("skyr_environment_seamless", ctx.handle, _ptr(cube), face_size, levels, _ptr(out))
+    return out
+
+
+def environment_sh(ctx: Context, seamless: torch.Tensor, face_size: int, levels: int,
+                   out: torch.Tensor | None = None) -> torch.Tensor:
+    """IBL's 9 spherical-harmonic radiance coefficients: [9][4] float (a = 0)."""
+    if out is None:
+        out = torch.empty((9, 4), dtype=torch.float32, device="cuda")
+    _abi.call("skyr_environment_sh", ctx.handle, _ptr(seamless), face_size, levels, _ptr(out))
+    return out
+
+
+def environment_prefilter(ctx: Context, seamless: torch.Tensor, face_size: int, levels: int, resolution: int = 128,
+                          roughness_count: int = 5, out: torch.Tensor | None = None) -> list[torch.Tensor]:
+    """IBL's GGX-prefiltered radiance (128^2 cube, 5 roughness levels in the
+    reference): one [6][s][s][4] half view per roughness level."""
+    total = _abi.lib().skyr_environment_cube_level_offset(resolution, roughness_count)
+    if total == 0:
+        raise _abi.SkyrError(_abi.SKYR_EINVAL, "environment_prefilter", "bad resolution or roughness count")
+    if out is None:
+        out = torch.empty((total, 4), dtype=torch.float16, device="cuda")
+    _abi.call("skyr_environment_prefilter", ctx.handle, _ptr(seamless), face_size, levels, resolution,
+              roughness_count, _ptr(out))
+    return [out[off:off + 6 * side * side].view(6, side, side, 4)
+            for off, side in environment_cube_levels(resolution)[:roughness_count]]

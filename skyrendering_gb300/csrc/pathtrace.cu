@@ -19,6 +19,7 @@
 #include "atmosphere_kernels.cuh"
 #include "cloud_internal.cuh"
 #include "cloud_material.cuh"
+#include "environment.cuh"
 #include "lut_access.cuh"
 #include "noise_device.cuh"
 #include "skyr_ctx.cuh"
@@ -195,34 +196,6 @@ __device__ __forceinline__ float transmittance_estimation(const PtConsts& P, con
     return clamp01(tr);
 }
 
-// ENVIRONMENT_LUMINANCE (AtmosphereRenderer.glsl:250-273) for world direction w:
-// GetCosLatLonFromViewDirection, GetSkyViewTextureUvFromCosLatLon (:113-145),
-// sky-view luminance + ground term x sky-view transmittance.
-template <class S>
-__device__ float3 environment(const PtConsts& P, const AtmoConsts& A, const ViewConsts& E, const float4* tlut,
-                              int tw, int th, const S* svl, const S* svt, float3 w) {
-    float cos_lat = dot3(E.up, w);
-    float3 lon = w - E.up * cos_lat;
-    float l2 = dot3(lon, lon);
-    float cos_lon = l2 == 0.f ? 1.f : dot3(lon, E.front) * rsqrtf(l2);
-    float r = E.cam_r;
-    float hd = acosf(sqrtf(fmaxf(E.cam_rho2, 0.f)) / r);
-    float hu = SKYR_PI - hd;
-    float lat = acosf(fminf(fmaxf(cos_lat, -1.f), 1.f));
-    float xl = lat < hu ? 0.5f - 0.5f * sqrtf(fmaxf(1.f - lat / hu, 0.f)) : sqrtf(fmaxf((lat - hu) / hd, 0.f)) * 0.5f + 0.5f;
-    float xo = sqrtf(fmaxf(0.5f - 0.5f * cos_lon, 0.f));
-    float x = xo * (float)(P.sv_w - 1), y = xl * (float)(P.sv_h - 1);
-    float3 lum = bilinear_clamp(svl, P.sv_w, P.sv_h, x, y);
-    float3 tr = bilinear_clamp(svt, P.sv_w, P.sv_h, x, y);
-    if (ray_hits_ground(r, E.cam_rho2, cos_lat)) {
-        float dist = dist_to_bottom(r, E.cam_rho2, cos_lat);
-        float mu_s_g = fmaf(r, dot3(E.sun, E.up), dist * dot3(E.sun, w)) / A.R;
-        float3 sv = sun_visibility_lut(A, tlut, tw, th, A.R, 0.f, 0.f, mu_s_g);
-        lum += (A.ground_albedo * sv * A.solar_illuminance * (clamp01(mu_s_g) / SKYR_PI)) * tr;
-    }
-    return lum;
-}
-
 // Work items of one frame: the region in 8x4 pixel tiles, 32 items per tile
 // (items past the region's right / bottom edge are skipped).
 __device__ __forceinline__ bool item_pixel(const PtConsts& P, int item, int& px, int& py) {
@@ -356,7 +329,7 @@ __device__ __forceinline__ bool bounce(const CloudConsts& C, const MaterialConst
         if (P.env == SKYR_ENV_OFF || !ps.scattered) return false;
         if (P.env == SKYR_ENV_CONST_ENVIRONMENT_MAP) {
             float3 wd = P.m_front * ps.d.x + P.m_right * ps.d.y + P.m_up * ps.d.z;
-            ps.L += ps.thr * environment(P, A, E, tlut, tw, th, svl, svt, wd);
+            ps.L += ps.thr * environment(A, E, tlut, tw, th, svl, svt, P.sv_w, P.sv_h, wd);
             return false;
         }
         float3 o = ps.o, d = ps.d;
@@ -365,7 +338,7 @@ __device__ __forceinline__ bool bounce(const CloudConsts& C, const MaterialConst
         float mu = fmaf(d.x, o.x, fmaf(d.y, o.y, d.z * (o.z + C.R))) / r;
         if (!ray_hits_ground(r, rho2, mu)) {
             float3 wd = P.m_front * d.x + P.m_right * d.y + P.m_up * d.z;
-            ps.L += ps.thr * environment(P, A, E, tlut, tw, th, svl, svt, wd);
+            ps.L += ps.thr * environment(A, E, tlut, tw, th, svl, svt, P.sv_w, P.sv_h, wd);
             return false;
         }
         o = o + d * dist_to_bottom(r, rho2, mu);

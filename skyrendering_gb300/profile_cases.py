@@ -9,6 +9,7 @@ times on one stream, synchronise and exit 0.
     python -m skyrendering_gb300.profile_cases mlp --iters 3
     python -m skyrendering_gb300.profile_cases shadow --iters 3
     python -m skyrendering_gb300.profile_cases quarter --iters 3
+    python -m skyrendering_gb300.profile_cases environment --iters 3
 
 Cases (seeded synthetic inputs from workloads.py):
   luts   the plain LUT set (T 256x64, MS 32x32, SV 192x108, AP 32^3) of the
@@ -25,6 +26,8 @@ Cases (seeded synthetic inputs from workloads.py):
          seeded random records.
   shadow the cloud shadow passes of the 1920x1080 frame (512^2 map blended
          into the previous frame's, blur, 160x90x128 froxel).
+  environment the environment cube of that frame's LUT set (128^2 x 6 +
+         mips), its SH coefficients and 5 prefiltered roughness levels;
   quarter the quarter-resolution cloud pass of that frame (checkerboard,
          index, 480x270 raymarch, 960x540 reconstruction with history,
          upscale into an HDR target; empty depth buffer).
@@ -153,9 +156,29 @@ def quarter_case(ctx):
     return step
 
 
+def environment_case(ctx):
+    from .atmosphere import environment_cube, environment_prefilter, environment_seamless, environment_sh
+
+    atmo, sizes, render, luts, lut_step = lut_case(ctx, W.frame_camera())
+    lut_step()
+    total = sum(6 * (128 >> l) ** 2 for l in range(8))
+    out = torch.empty((total, 4), dtype=torch.float16, device="cuda")
+    seam = torch.empty((sum(6 * ((128 >> l) + 2) ** 2 for l in range(8)), 4), dtype=torch.float32, device="cuda")
+    sh = torch.empty((9, 4), dtype=torch.float32, device="cuda")
+    pre = torch.empty((sum(6 * (128 >> l) ** 2 for l in range(5)), 4), dtype=torch.float16, device="cuda")
+
+    def step():
+        environment_cube(ctx, atmo, render, sizes, luts, 128, out=out)
+        environment_seamless(ctx, out, 128, 8, out=seam)
+        environment_sh(ctx, seam, 128, 8, out=sh)
+        environment_prefilter(ctx, seam, 128, 8, 128, 5, out=pre)
+
+    return step
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["luts", "cloud", "pt", "surrogate", "lattice", "mlp", "shadow", "quarter"])
+    ap.add_argument("case", choices=["luts", "cloud", "pt", "surrogate", "lattice", "mlp", "shadow", "quarter", "environment"])
     ap.add_argument("--iters", type=int, default=3)
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--global-majorant", action="store_true")
@@ -176,6 +199,8 @@ def main(argv=None):
         step = shadow_case(ctx)
     elif a.case == "quarter":
         step = quarter_case(ctx)
+    elif a.case == "environment":
+        step = environment_case(ctx)
     else:
         step = mlp_case(ctx)
     torch.cuda.synchronize()
