@@ -717,3 +717,55 @@ def environment_seamless(cube_texels: np.ndarray, size: int, levels: int) -> np.
     out = np.zeros((total, 4))
     assert lib().oracle_environment_seamless(_dp(c), size, levels, _dp(out.reshape(-1))) == 0
     return out
+
+
+# ---------------------------------------------------------------------------
+# full-screen composite
+# ---------------------------------------------------------------------------
+def _declare_composite(lb):
+    lb.oracle_atmosphere_composite.restype = C.c_int
+    lb.oracle_atmosphere_composite.argtypes = [P, P, P, P, D, D, D, D, D, D, P, I32, C.c_int, C.c_int, D]
+
+
+_EXT.append(_declare_composite)
+
+
+def atmosphere_composite(params, render, cp, sizes, luts: dict, width: int, height: int, blue_noise=None, depth=None,
+                         object_luminance=None, star_map=None, froxel=None, froxel_max_distance: float = 20.0,
+                         pixels=None, nthreads: int | None = None) -> np.ndarray:
+    """The composite of listed pixels (or all): [n][4].  luts: name -> array
+    (transmittance, multiscattering, sky_view_*, aerial_perspective_*)."""
+    import skyrendering_gb300._abi as A  # struct layout only
+
+    keep = []
+    inp = A.CompositeInputs()
+    inp.width, inp.height = width, height
+
+    def host(a, dt):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return a.ctypes.data
+
+    inp.depth = host(depth, np.float32)
+    inp.object_luminance = host(object_luminance, np.float32)
+    inp.blue_noise = host(blue_noise, np.float32)
+    if star_map is not None:
+        inp.star_map = host(star_map, np.uint8)
+        inp.star_height, inp.star_width = star_map.shape[:2]
+    if froxel is not None:
+        inp.shadow_froxel = host(froxel, np.uint16)
+        inp.froxel_depth, inp.froxel_height, inp.froxel_width = froxel.shape
+        inp.shadow_froxel_max_distance = froxel_max_distance
+    names = ("transmittance", "multiscattering", "sky_view_luminance", "sky_view_transmittance",
+             "aerial_perspective_luminance", "aerial_perspective_transmittance")
+    arrs = [None if luts.get(k) is None else _f64(luts[k]).reshape(-1) for k in names]
+    n = width * height if pixels is None else len(pixels)
+    px = None if pixels is None else np.ascontiguousarray(pixels, dtype=np.int32)
+    out = np.zeros((n, 4))
+    rc = lib().oracle_atmosphere_composite(_ref(params), _ref(render), _ref(cp), _ref(sizes), *[_dp(a) for a in arrs],
+                                           _ref(inp), None if px is None else px.ctypes.data_as(I32), n,
+                                           nthreads or threads(), _dp(out))
+    assert rc == 0
+    return out

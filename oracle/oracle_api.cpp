@@ -14,6 +14,7 @@
 #include "oracle_shadow.hpp"
 #include "oracle_quarter.hpp"
 #include "oracle_environment.hpp"
+#include "oracle_composite.hpp"
 #include "../include/skyr_cloud_shadow.h"
 #include "../include/skyr_surrogate.h"
 
@@ -934,6 +935,36 @@ int oracle_environment_seamless(const double* cube, int size, int levels, double
             for (int j = -1; j <= n; ++j)
                 for (int i = -1; i <= n; ++i, ++k) orc::cube_texel(C, l, face, i, j, out + 4 * k);
     }
+    return 0;
+}
+
+}  // extern "C"
+
+// ---- full-screen composite ----------------------------------------------------
+extern "C" {
+
+// The composite of the listed pixels (y * width + x, or all); `in` holds host
+// pointers; LUTs as double RGBA images; out[4] per pixel.
+int oracle_atmosphere_composite(const skyr_atmosphere_parameters* p, const skyr_atmosphere_render_parameters* r,
+                                const skyr_composite_parameters* cp, const skyr_lut_sizes* s, const double* t_in,
+                                const double* ms_in, const double* svl_in, const double* svt_in, const double* apl_in,
+                                const double* apt_in, const skyr_composite_inputs* in, const int* pixels, int n,
+                                int threads, double* out) {
+    orc::AtmosphereOracle<double> O{orc::derive_atmosphere<double>(*p)};
+    orc::ViewLutOracle<double> VL{O, orc::derive_render_frame<double>(*p, *r)};
+    orc::Image<double> tl = image_from<double>(t_in, s->transmittance_width, s->transmittance_height);
+    orc::Image<double> ms = image_from<double>(ms_in, s->multiscattering_width, s->multiscattering_height);
+    orc::Image<double> svl, svt, apl, apt;
+    if (svl_in) svl = image_from<double>(svl_in, s->sky_view_width, s->sky_view_height);
+    if (svt_in) svt = image_from<double>(svt_in, s->sky_view_width, s->sky_view_height);
+    int aw = s->aerial_perspective_width, ah = s->aerial_perspective_height, ad = s->aerial_perspective_depth;
+    if (apl_in) apl = image_from<double>(apl_in, aw, ah, ad);
+    if (apt_in) apt = image_from<double>(apt_in, aw, ah, ad);
+    orc::CompositeOracle C{O, VL, tl, ms, svl, svt, apl, apt, *cp, *in};
+    parallel_for(n, threads, [&](int i) {
+        int q = pixels ? pixels[i] : i;
+        C.Pixel(q % in->width, q / in->width, out + 4 * (size_t)i);
+    });
     return 0;
 }
 

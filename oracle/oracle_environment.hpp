@@ -26,8 +26,31 @@ V3<T> cube_uv_to_dir(int face, T u, T v) {
 }
 
 // GetCosLatLonFromViewDirection + GetSkyViewTextureUvFromCosLatLon
-// (AtmosphereRenderer.glsl:113-145), the sky-view lookups and the ground term
-// (AtmosphereRenderer.glsl:258-270) for world direction w.
+// (AtmosphereRenderer.glsl:113-145) and the sky-view LUT samples for world
+// direction w seen from the frame's camera.
+template <class T>
+void sky_view_sample(const AtmosphereOracle<T>& O, const RenderFrame<T>& F, const Image<T>& svl, const Image<T>& svt,
+                     V3<T> w, V3<T>& lum, V3<T>& tr) {
+    T cos_lat = dot(F.up, w);
+    V3<T> lon = w - F.up * cos_lat;
+    T l2 = dot(lon, lon);
+    T cos_lon = l2 == T(0) ? T(1) : dot(lon / std::sqrt(l2), F.front);
+    T r = F.camera_earth_center_distance;
+    T hd = std::acos(std::sqrt(r * r - O.A.bottom_radius * O.A.bottom_radius) / r);
+    T hu = T(kPi) - hd;
+    T lat = std::acos(clampg(cos_lat, T(-1), T(1)));
+    T xl;
+    if (lat < hu) xl = T(0.5) - T(0.5) * std::sqrt(T(1) - lat / hu);
+    else xl = std::sqrt((lat - hu) / hd) * T(0.5) + T(0.5);
+    T xo = std::sqrt(std::max(T(0.5) - T(0.5) * cos_lon, T(0)));
+    T u = T(0.5) / T(svl.w) + xo * (T(1) - T(1) / T(svl.w));
+    T v = T(0.5) / T(svl.h) + xl * (T(1) - T(1) / T(svl.h));
+    lum = sample_linear_clamp(svl, u, v);
+    tr = sample_linear_clamp(svt, u, v);
+}
+
+// The sky-view lookups and the ground term (AtmosphereRenderer.glsl:258-270)
+// for world direction w.
 template <class T>
 V3<T> environment_luminance(const AtmosphereOracle<T>& O, const RenderFrame<T>& F, const Image<T>& tlut,
                             const Image<T>& svl, const Image<T>& svt, V3<T> w) {

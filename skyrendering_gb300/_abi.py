@@ -326,6 +326,31 @@ _SIGNATURES.update({
 })
 
 
+# ---------------------------------------------------------------------------
+# skyr_composite.h
+# ---------------------------------------------------------------------------
+class CompositeParameters(C.Structure):
+    _fields_ = [("star_luminance_scale", C.c_float), ("raymarching_steps", C.c_float),
+                ("use_sky_view_lut", C.c_int), ("use_aerial_perspective_lut", C.c_int),
+                ("dither_sample_point", C.c_int)]
+
+
+class CompositeInputs(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("depth", P), ("object_luminance", P),
+                ("blue_noise", P), ("star_map", P), ("star_width", C.c_int), ("star_height", C.c_int),
+                ("shadow_froxel", P), ("froxel_width", C.c_int), ("froxel_height", C.c_int),
+                ("froxel_depth", C.c_int), ("shadow_froxel_max_distance", C.c_float)]
+
+
+STRUCT_IDS.update({19: CompositeParameters, 20: CompositeInputs})
+_SIGNATURES.update({
+    "skyr_composite_parameters_default": (C.c_int, [C.POINTER(CompositeParameters)]),
+    "skyr_atmosphere_composite": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(AtmosphereRenderParameters),
+                                            C.POINTER(CompositeParameters), C.POINTER(LutSizes), P, P, P, P, P, P,
+                                            C.POINTER(CompositeInputs), P]),
+})
+
+
 # allocation-free LUT set (static device scratch, SKYR_NOALLOC_MAX_SETS sets)
 SKYR_NOALLOC_MAX_SETS = 256
 _SIGNATURES["skyr_update_lut_set_noalloc"] = (

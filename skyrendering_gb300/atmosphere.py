@@ -214,3 +214,45 @@ def environment_prefilter(ctx: Context, seamless: torch.Tensor, face_size: int, 
               roughness_count, _ptr(out))
     return [out[off:off + 6 * side * side].view(6, side, side, 4)
             for off, side in environment_cube_levels(resolution)[:roughness_count]]
+
+
+def composite_parameters(**overrides) -> _abi.CompositeParameters:
+    """AtmosphereRenderer's composite parameters (reference defaults: per-pixel
+    raymarch of 40 dithered samples, star scale 0.005), with overrides."""
+    cp = _abi.CompositeParameters()
+    _abi.call("skyr_composite_parameters_default", C.byref(cp))
+    for k, v in overrides.items():
+        setattr(cp, k, v)
+    return cp
+
+
+def composite(ctx: Context, atmosphere: _abi.AtmosphereParameters, render: _abi.AtmosphereRenderParameters,
+              parameters: _abi.CompositeParameters, sizes: _abi.LutSizes, luts: "LutSet", width: int, height: int,
+              blue_noise: torch.Tensor | None = None, depth: torch.Tensor | None = None,
+              object_luminance: torch.Tensor | None = None, star_map: torch.Tensor | None = None,
+              shadow_froxel: torch.Tensor | None = None, shadow_froxel_max_distance: float = 20.0,
+              out: torch.Tensor | None = None, set_index: int = 0) -> torch.Tensor:
+    """The full-screen atmosphere composite (AtmosphereRenderer's
+    ATMOSPHERE_RENDER pass) into a [height][width][4] half HDR target.
+    star_map: uint8 [h][w][3] sRGB; shadow_froxel: int16 words [d][h][w]."""
+    if out is None:
+        out = torch.empty((height, width, 4), dtype=torch.float16, device="cuda")
+    inp = _abi.CompositeInputs()
+    inp.width, inp.height = width, height
+    inp.depth = None if depth is None else depth.data_ptr()
+    inp.object_luminance = None if object_luminance is None else object_luminance.data_ptr()
+    inp.blue_noise = None if blue_noise is None else blue_noise.data_ptr()
+    if star_map is not None:
+        inp.star_map = star_map.data_ptr()
+        inp.star_height, inp.star_width = star_map.shape[0], star_map.shape[1]
+    if shadow_froxel is not None:
+        inp.shadow_froxel = shadow_froxel.data_ptr()
+        inp.froxel_depth, inp.froxel_height, inp.froxel_width = shadow_froxel.shape
+        inp.shadow_froxel_max_distance = shadow_froxel_max_distance
+    s = set_index
+    L = luts
+    _abi.call("skyr_atmosphere_composite", ctx.handle, C.byref(atmosphere), C.byref(render), C.byref(parameters),
+              C.byref(sizes), _ptr(L.transmittance[s]), _ptr(L.multiscattering[s]), _ptr(L.sky_view_luminance[s]),
+              _ptr(L.sky_view_transmittance[s]), _ptr(L.aerial_perspective_luminance[s]),
+              _ptr(L.aerial_perspective_transmittance[s]), C.byref(inp), _ptr(out))
+    return out

@@ -191,31 +191,37 @@ struct CloudCheckerboard {
 };
 
 // SampleRayScatterVisibility (VolumetricCloudShadowInterface.glsl:10-13): the
-// shadow froxel read with GL LINEAR + CLAMP_TO_EDGE at (u, v, dist / max) and
-// faded to 1 by clamp(1 / w, 0, 1) beyond its last slice; 1 without a froxel.
-__device__ __forceinline__ float froxel_visibility(const CloudConsts& C, float u, float v, float dist) {
-    if (!C.froxel) return 1.f;
-    float w = dist * C.inv_froxel_max_distance;
+// unorm16 shadow froxel (w x h x d) read with GL LINEAR + CLAMP_TO_EDGE at
+// (u, v, dist / max) and faded to 1 by clamp(1 / w, 0, 1) beyond its last
+// slice; 1 without a froxel.
+__device__ __forceinline__ float froxel_visibility_at(const uint16_t* froxel, int fw, int fh, int fd,
+                                                      float inv_max_distance, float u, float v, float dist) {
+    if (!froxel) return 1.f;
+    float w = dist * inv_max_distance;
     // clamping the texel coordinate first is CLAMP_TO_EDGE's rule for LINEAR
-    float x = fminf(fmaxf(u * (float)C.fx_w - 0.5f, 0.f), (float)(C.fx_w - 1));
-    float y = fminf(fmaxf(v * (float)C.fx_h - 0.5f, 0.f), (float)(C.fx_h - 1));
-    float z = fminf(fmaxf(w * (float)C.fx_d - 0.5f, 0.f), (float)(C.fx_d - 1));
+    float x = fminf(fmaxf(u * (float)fw - 0.5f, 0.f), (float)(fw - 1));
+    float y = fminf(fmaxf(v * (float)fh - 0.5f, 0.f), (float)(fh - 1));
+    float z = fminf(fmaxf(w * (float)fd - 0.5f, 0.f), (float)(fd - 1));
     int x0 = (int)x, y0 = (int)y, z0 = (int)z;
-    int x1 = min(x0 + 1, C.fx_w - 1), y1 = min(y0 + 1, C.fx_h - 1), z1 = min(z0 + 1, C.fx_d - 1);
+    int x1 = min(x0 + 1, fw - 1), y1 = min(y0 + 1, fh - 1), z1 = min(z0 + 1, fd - 1);
     float a = x - (float)x0, b = y - (float)y0, g = z - (float)z0;
-    const size_t slice = (size_t)C.fx_w * C.fx_h;
+    const size_t slice = (size_t)fw * fh;
     float r[2];
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-        const uint16_t* s = C.froxel + (size_t)(k ? z1 : z0) * slice;
-        float t00 = (float)__ldg(s + (size_t)y0 * C.fx_w + x0), t10 = (float)__ldg(s + (size_t)y0 * C.fx_w + x1);
-        float t01 = (float)__ldg(s + (size_t)y1 * C.fx_w + x0), t11 = (float)__ldg(s + (size_t)y1 * C.fx_w + x1);
+        const uint16_t* s = froxel + (size_t)(k ? z1 : z0) * slice;
+        float t00 = (float)__ldg(s + (size_t)y0 * fw + x0), t10 = (float)__ldg(s + (size_t)y0 * fw + x1);
+        float t01 = (float)__ldg(s + (size_t)y1 * fw + x0), t11 = (float)__ldg(s + (size_t)y1 * fw + x1);
         float top = t00 + (t10 - t00) * a, bot = t01 + (t11 - t01) * a;
         r[k] = top + (bot - top) * b;
     }
     float f = (r[0] + (r[1] - r[0]) * g) * (1.f / 65535.f);
     float k = fminf(fmaxf(__frcp_rn(w), 0.f), 1.f);  // w = 0 gives +inf, clamped to 1
     return 1.f + (f - 1.f) * k;
+}
+
+__device__ __forceinline__ float froxel_visibility(const CloudConsts& C, float u, float v, float dist) {
+    return froxel_visibility_at(C.froxel, C.fx_w, C.fx_h, C.fx_d, C.inv_froxel_max_distance, u, v, dist);
 }
 
 // Column-major 4x4 helpers of the host derivations (double).

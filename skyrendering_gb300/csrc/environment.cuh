@@ -8,12 +8,12 @@
 
 namespace skyr {
 
-// ENVIRONMENT_LUMINANCE (AtmosphereRenderer.glsl:250-273) for world direction w:
-// GetCosLatLonFromViewDirection, GetSkyViewTextureUvFromCosLatLon (:113-145),
-// sky-view luminance + ground term x sky-view transmittance.
+// GetCosLatLonFromViewDirection + GetSkyViewTextureUvFromCosLatLon
+// (AtmosphereRenderer.glsl:113-145) and the sky-view LUT reads for world
+// direction w seen from the view's camera.
 template <class S>
-__device__ float3 environment(const AtmoConsts& A, const ViewConsts& E, const float4* tlut, int tw, int th,
-                              const S* svl, const S* svt, int sv_w, int sv_h, float3 w) {
+__device__ __forceinline__ void sky_view_lookup(const ViewConsts& E, const S* svl, const S* svt, int sv_w, int sv_h,
+                                                float3 w, float3& lum, float3& tr) {
     float cos_lat = dot3(E.up, w);
     float3 lon = w - E.up * cos_lat;
     float l2 = dot3(lon, lon);
@@ -25,8 +25,20 @@ __device__ float3 environment(const AtmoConsts& A, const ViewConsts& E, const fl
     float xl = lat < hu ? 0.5f - 0.5f * sqrtf(fmaxf(1.f - lat / hu, 0.f)) : sqrtf(fmaxf((lat - hu) / hd, 0.f)) * 0.5f + 0.5f;
     float xo = sqrtf(fmaxf(0.5f - 0.5f * cos_lon, 0.f));
     float x = xo * (float)(sv_w - 1), y = xl * (float)(sv_h - 1);
-    float3 lum = bilinear_clamp(svl, sv_w, sv_h, x, y);
-    float3 tr = bilinear_clamp(svt, sv_w, sv_h, x, y);
+    lum = bilinear_clamp(svl, sv_w, sv_h, x, y);
+    tr = bilinear_clamp(svt, sv_w, sv_h, x, y);
+}
+
+// ENVIRONMENT_LUMINANCE (AtmosphereRenderer.glsl:250-273) for world direction w:
+// the sky-view luminance, plus the ground term x sky-view transmittance below
+// the horizon.
+template <class S>
+__device__ float3 environment(const AtmoConsts& A, const ViewConsts& E, const float4* tlut, int tw, int th,
+                              const S* svl, const S* svt, int sv_w, int sv_h, float3 w) {
+    float3 lum, tr;
+    sky_view_lookup(E, svl, svt, sv_w, sv_h, w, lum, tr);
+    float cos_lat = dot3(E.up, w);
+    float r = E.cam_r;
     if (ray_hits_ground(r, E.cam_rho2, cos_lat)) {
         float dist = dist_to_bottom(r, E.cam_rho2, cos_lat);
         float mu_s_g = fmaf(r, dot3(E.sun, E.up), dist * dot3(E.sun, w)) / A.R;

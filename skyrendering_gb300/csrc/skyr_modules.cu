@@ -6,6 +6,7 @@
 #include "../../include/skyr_pathtrace.h"
 #include "../../include/skyr_cloud_shadow.h"
 #include "../../include/skyr_cloud_quarter.h"
+#include "../../include/skyr_composite.h"
 #include "skyr_ctx.cuh"
 
 namespace skyr {
@@ -90,6 +91,8 @@ size_t skyr_struct_size_ext(int which) {
         case 16: return sizeof(skyr_cloud_light_frame);
         case 17: return sizeof(skyr_cloud_temporal_frame);
         case 18: return sizeof(skyr_cloud_quarter_buffers);
+        case 19: return sizeof(skyr_composite_parameters);
+        case 20: return sizeof(skyr_composite_inputs);
         default: return 0;
     }
 }

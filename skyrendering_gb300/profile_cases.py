@@ -10,6 +10,7 @@ times on one stream, synchronise and exit 0.
     python -m skyrendering_gb300.profile_cases shadow --iters 3
     python -m skyrendering_gb300.profile_cases quarter --iters 3
     python -m skyrendering_gb300.profile_cases environment --iters 3
+    python -m skyrendering_gb300.profile_cases composite --iters 3
 
 Cases (seeded synthetic inputs from workloads.py):
   luts   the plain LUT set (T 256x64, MS 32x32, SV 192x108, AP 32^3) of the
@@ -26,6 +27,8 @@ Cases (seeded synthetic inputs from workloads.py):
          seeded random records.
   shadow the cloud shadow passes of the 1920x1080 frame (512^2 map blended
          into the previous frame's, blur, 160x90x128 froxel).
+  composite the full-screen atmosphere composite of that frame (1920x1080,
+         per-pixel raymarch of 40 dithered samples, star map, no objects);
   environment the environment cube of that frame's LUT set (128^2 x 6 +
          mips), its SH coefficients and 5 prefiltered roughness levels;
   quarter the quarter-resolution cloud pass of that frame (checkerboard,
@@ -176,9 +179,23 @@ def environment_case(ctx):
     return step
 
 
+def composite_case(ctx):
+    from .atmosphere import composite, composite_parameters
+
+    cam = W.frame_camera()
+    atmo, sizes, render, luts, lut_step = lut_case(ctx, cam)
+    lut_step()
+    bn = blue_noise_tile().cuda()
+    stars = torch.from_numpy(W.star_map()).cuda()
+    out = torch.empty((cam.height, cam.width, 4), dtype=torch.float16, device="cuda")
+    cp = composite_parameters()
+    return lambda: composite(ctx, atmo, render, cp, sizes, luts, cam.width, cam.height, blue_noise=bn,
+                             star_map=stars, out=out)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["luts", "cloud", "pt", "surrogate", "lattice", "mlp", "shadow", "quarter", "environment"])
+    ap.add_argument("case", choices=["luts", "cloud", "pt", "surrogate", "lattice", "mlp", "shadow", "quarter", "environment", "composite"])
     ap.add_argument("--iters", type=int, default=3)
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--global-majorant", action="store_true")
@@ -201,6 +218,8 @@ def main(argv=None):
         step = quarter_case(ctx)
     elif a.case == "environment":
         step = environment_case(ctx)
+    elif a.case == "composite":
+        step = composite_case(ctx)
     else:
         step = mlp_case(ctx)
     torch.cuda.synchronize()

@@ -347,3 +347,49 @@ def pt_camera(width=1024, height=1024) -> Camera:
     alt = origin[2] + 0.5 * PT_GRID_DIMS[2] * voxel
     return Camera(position=(0.0, alt, 0.0), yaw=-90.0, pitch=0.0, fovy=35.0, width=width, height=height,
                   z_near=0.01, z_far=1000.0)
+
+
+# ---------------------------------------------------------------------------
+# Full-screen composite inputs: a seeded star map (the reference loads
+# data/NASA/starmap_2020_4k.jpg) and a depth buffer with the Earth's surface
+# and one near occluder
+# ---------------------------------------------------------------------------
+def star_map(width: int = 1024, height: int = 512, n_stars: int = 6000, seed: int = SEED) -> np.ndarray:
+    """sRGB8 RGB texels [height][width][3]: a faint band and n_stars point stars
+    of random magnitude and colour temperature."""
+    rng = np.random.default_rng(seed)
+    img = np.zeros((height, width, 3), dtype=np.float64)
+    v = (np.arange(height) + 0.5) / height
+    img += (0.03 * np.exp(-((v - 0.5) / 0.08) ** 2))[:, None, None]
+    ys, xs = rng.integers(0, height, n_stars), rng.integers(0, width, n_stars)
+    mag = rng.uniform(0.05, 1.0, n_stars) ** 3
+    tint = rng.uniform(-0.2, 0.2, n_stars)
+    col = np.stack([1.0 + tint, np.ones(n_stars), 1.0 - tint], -1) * mag[:, None]
+    np.add.at(img, (ys, xs), col)
+    return np.round(np.clip(img, 0.0, 1.0) * 255.0).astype(np.uint8)
+
+
+def ground_depth(cam: Camera, width: int, height: int, R: float, occluder: bool = True) -> np.ndarray:
+    """GL window depth [height][width] of the Earth's surface below the horizon
+    and, when `occluder`, of a screen rectangle 2.5 km away; 1 elsewhere."""
+    vp = cam.view_projection()
+    ivp = np.linalg.inv(vp)
+    ys, xs = np.mgrid[0:height, 0:width]
+    ndc = np.stack([(xs + 0.5) / width * 2 - 1, (ys + 0.5) / height * 2 - 1, np.zeros(xs.shape),
+                    np.ones(xs.shape)], -1)
+    p = ndc @ ivp.T
+    p = p[..., :3] / p[..., 3:]
+    o = np.asarray(cam.position, dtype=np.float64)
+    d = p - o
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    c = o - np.array([0.0, -R, 0.0])
+    b = d @ c
+    disc = b * b - (c @ c - R * R)
+    t = np.where((disc > 0) & (b < 0), -b - np.sqrt(np.maximum(disc, 0)), np.inf)
+    if occluder:
+        occ = (xs > 0.3 * width) & (xs < 0.45 * width) & (ys > 0.35 * height) & (ys < 0.75 * height)
+        t = np.where(occ, 2.5, t)
+    hit = np.isfinite(t)
+    q = o + d * np.where(hit, t, 1.0)[..., None]
+    clip = np.concatenate([q, np.ones_like(q[..., :1])], -1) @ vp.T
+    return np.where(hit, 0.5 * clip[..., 2] / clip[..., 3] + 0.5, 1.0).astype(np.float32)
