@@ -50,6 +50,12 @@ L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 SUN_ZENITH = 45.0
 
 
+def cloud_tile(tile_width: int, ray_lanes: int) -> str:
+    """The pixel tile of one raymarch warp for a tuning's tile width and lanes per ray."""
+    w = min(tile_width, 32 // ray_lanes)
+    return f"{w}x{32 // ray_lanes // w}"
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -325,10 +331,11 @@ def batched_frames(ctx, reps: int = 5, n_sets: int = 256, n_views: int = 64):
            "tuning": {"transmittance_lanes": lut_best.transmittance_lanes, "view_lanes": lut_best.view_lanes,
                       "cloud_tile_width": cloud_best.cloud_tile_width,
                       "cloud_block_warps_x": cloud_best.cloud_block_warps_x,
-                      "cloud_blocks_per_sm": cloud_best.cloud_blocks_per_sm},
+                      "cloud_blocks_per_sm": cloud_best.cloud_blocks_per_sm,
+                      "cloud_ray_lanes": cloud_best.cloud_ray_lanes},
            "autotune_lut_ms": {"transmittance_lanes_4_8_16": lut_times[:3], "view_lanes_4_8_16": lut_times[3:]},
-           "autotune_cloud_ms": {f"{w}x{32 // w}/{bx}/{occ}": t
-                                 for (w, bx, occ), t in zip(B.CLOUD_CANDIDATES, cloud_times)}}
+           "autotune_cloud_ms": {f"{cloud_tile(w, g)}/{bx}/{occ}/{g}": t
+                                 for (w, bx, occ, g), t in zip(B.CLOUD_CANDIDATES, cloud_times)}}
     cap.graph.close()
     lut_cap.graph.close()
     lb.close()
@@ -482,9 +489,13 @@ def quarter_pass(ctx, fs, lut_graph, reps: int = 20):
     stream = ctx.stream
     W_, H_ = fs.view.width, fs.view.height
     zn, zf = fs.cam.z_near, fs.cam.z_far
+    frame_tuning = B.tuning(ctx)
     vp = CL.CloudViewport(ctx, W_, H_)
     hdr = torch.zeros((H_, W_, 4), dtype=torch.float16, device="cuda")
     vp.render(fs.vc, fs.atmo, fs.view, fs.sizes, fs.luts, fs.bn, hdr=hdr, z_near=zn, z_far=zf)
+    # the quarter pass's raymarch has 1/16 of the rays: its own launch shape, autotuned on the
+    # pass itself and kept in the context while its graphs are captured
+    q_tuned, _ = vp.autotune(fs.vc, fs.atmo, fs.view, fs.sizes, fs.luts, fs.bn, z_near=zn, z_far=zf, reps=5)
     sh = CL.CloudShadow(ctx, CL.shadow_sizes(W_, H_))
     sh.render(fs.vc, fs.atmo, fs.view, fs.bn)
     view = _abi.CloudView.from_buffer_copy(fs.view)
@@ -551,6 +562,7 @@ def quarter_pass(ctx, fs, lut_graph, reps: int = 20):
     with B.capture(ctx) as cap:
         call(fview, hdr)
     quarter_graph = cap.graph
+    _abi.call("skyr_ctx_set_tuning", ctx.handle, C.byref(frame_tuning))
     # AtmosphereRenderer's full-screen composite (reference defaults: per-pixel raymarch, 40 dithered samples;
     # seeded star map; the cloud shadow froxel) into the HDR target the cloud upscale composites onto
     from skyrendering_gb300.atmosphere import composite, composite_parameters
@@ -587,6 +599,10 @@ def quarter_pass(ctx, fs, lut_graph, reps: int = 20):
            "production_frame_parts_ms": {
                name: statistics.mean(e[k].elapsed_time(e[k + 1]) for e in ev) for k, (name, _) in enumerate(order)},
            "kernels_per_pass": 5,
+           "raymarch_tuning": {"tile": cloud_tile(q_tuned.cloud_tile_width, q_tuned.cloud_ray_lanes),
+                               "block_warps_x": q_tuned.cloud_block_warps_x,
+                               "blocks_per_sm": q_tuned.cloud_blocks_per_sm,
+                               "ray_lanes": q_tuned.cloud_ray_lanes},
            "note": "production frame = the reference's per-frame GPU work of the sky and clouds, in its order: LUT "
                    "set, cloud shadow passes, environment cube (128^2 x 6 + mips, SH, 5 prefiltered levels), "
                    "full-screen atmosphere composite (per-pixel raymarch), quarter-resolution cloud pass with the "
@@ -735,9 +751,10 @@ def run_skyr(args):
                    "launch": "two CUDA graphs per step (LUT set, raymarch), captured once",
                    "tuning": {"transmittance_lanes": lut_tuned.transmittance_lanes,
                               "view_lanes": lut_tuned.view_lanes,
-                              "cloud_tile": f"{cloud_tuned.cloud_tile_width}x{32 // cloud_tuned.cloud_tile_width}",
+                              "cloud_tile": cloud_tile(cloud_tuned.cloud_tile_width, cloud_tuned.cloud_ray_lanes),
                               "cloud_block_warps_x": cloud_tuned.cloud_block_warps_x,
-                              "cloud_blocks_per_sm": cloud_tuned.cloud_blocks_per_sm}},
+                              "cloud_blocks_per_sm": cloud_tuned.cloud_blocks_per_sm,
+                              "cloud_ray_lanes": cloud_tuned.cloud_ray_lanes}},
         "components": {"lut_set_us": statistics.mean(lut_ms) * 1000.0, "cloud_frame_ms": cloud_mean,
                        "raymarch_samples": samples, "density_evaluations": evals,
                        "density_evaluations_per_s": evals / (cloud_mean * 1e-3)},
@@ -820,8 +837,8 @@ def cpu_baseline(sample_s: float):
     ms, n, lut_ms = cpu_frame_ms(sample_s, threads)
     return {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
             "lut_set_ms": lut_ms,
-            "sample": f"one full LUT set + {n} of 2073600 raymarched pixels (spread over the frame) in FP32 "
-                      f"on {threads} threads, scaled to the full frame"}
+            "sample": f"one full LUT set + {n} raymarched pixels ({n / 2073600:.2f} frames' worth, strided "
+                      f"passes over the 1920x1080 frame) in FP32 on {threads} threads, scaled to one frame"}
 
 
 def run_reference(args):

@@ -20,7 +20,7 @@
 #ifndef SKYR_CLOUD_QUARTER_H_
 #define SKYR_CLOUD_QUARTER_H_
 
-#include "skyr_cloud.h"
+#include "skyr_batch.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -72,6 +72,21 @@ int skyr_cloud_render_quarter(skyr_ctx* ctx, const skyr_atmosphere_parameters* a
                               const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
                               const float* blue_noise, const float* depth, const skyr_cloud_temporal_frame* frame,
                               const skyr_cloud_quarter_buffers* buffers, void* hdr);
+
+/* The cloud autotuner of skyr_batch.h (same SKYR_CLOUD_TUNE_CANDIDATES, same
+ * order of times_ms, same reps rule) timed on skyr_cloud_render_quarter's own
+ * passes up to the reconstruction (hdr NULL): the checkerboard raymarch has
+ * 1/16 of the viewport's rays, so it wants its own launch shape.  Keeps the
+ * fastest in the context; the buffers' outputs are overwritten. */
+int skyr_autotune_cloud_quarter(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                                const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                                const skyr_cloud_textures* textures, const skyr_cloud_view* view,
+                                const skyr_lut_sizes* sizes, const void* transmittance,
+                                const void* aerial_perspective_luminance,
+                                const void* aerial_perspective_transmittance, const float* blue_noise,
+                                const float* depth, const skyr_cloud_temporal_frame* frame,
+                                const skyr_cloud_quarter_buffers* buffers, int reps, skyr_tuning* best,
+                                float* times_ms);
 
 #ifdef __cplusplus
 }

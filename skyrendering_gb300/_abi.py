@@ -309,6 +309,11 @@ _SIGNATURES.update({
                                             C.POINTER(CloudMaterial), C.POINTER(CloudTextures), C.POINTER(CloudView),
                                             C.POINTER(LutSizes), P, P, P, P, P, C.POINTER(CloudTemporalFrame),
                                             C.POINTER(CloudQuarterBuffers), P]),
+    "skyr_autotune_cloud_quarter": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
+                                              C.POINTER(CloudMaterial), C.POINTER(CloudTextures),
+                                              C.POINTER(CloudView), C.POINTER(LutSizes), P, P, P, P, P,
+                                              C.POINTER(CloudTemporalFrame), C.POINTER(CloudQuarterBuffers), C.c_int,
+                                              P, P]),
 })
 
 
@@ -479,12 +484,12 @@ _SIGNATURES.update({
 # skyr_batch.h
 # ---------------------------------------------------------------------------
 SKYR_CLOUD_TILE_CANDIDATES = 12
-SKYR_CLOUD_TUNE_CANDIDATES = 24
+SKYR_CLOUD_TUNE_CANDIDATES = 96
 
 
 class Tuning(C.Structure):
     _fields_ = [("transmittance_lanes", C.c_int), ("view_lanes", C.c_int), ("cloud_tile_width", C.c_int),
-                ("cloud_block_warps_x", C.c_int), ("cloud_blocks_per_sm", C.c_int)]
+                ("cloud_block_warps_x", C.c_int), ("cloud_blocks_per_sm", C.c_int), ("cloud_ray_lanes", C.c_int)]
 
 
 STRUCT_IDS.update({14: Tuning})

@@ -18,8 +18,15 @@ from .atmosphere import Context, LutSet, _ptr
 TILE_CANDIDATES = ((4, 1), (4, 2), (4, 4), (8, 1), (8, 2), (8, 4), (16, 1), (16, 2), (16, 4), (32, 1), (32, 2),
                    (32, 4))
 OCCUPANCY_CANDIDATES = (5, 6)
-# (tile width, block warps x, blocks per SM) in the order of skyr_autotune_cloud's times
-CLOUD_CANDIDATES = tuple((w, bx, occ) for occ in OCCUPANCY_CANDIDATES for w, bx in TILE_CANDIDATES)
+RAY_LANE_CANDIDATES = (1, 2, 4, 8)
+# (tile width, block warps x, blocks per SM, ray lanes) in the order of skyr_autotune_cloud's times
+CLOUD_CANDIDATES = tuple((w, bx, occ, g) for g in RAY_LANE_CANDIDATES for occ in OCCUPANCY_CANDIDATES
+                         for w, bx in TILE_CANDIDATES)
+
+
+def cloud_tuning_key(t: _abi.Tuning) -> tuple:
+    """The CLOUD_CANDIDATES entry of a tuning."""
+    return (t.cloud_tile_width, t.cloud_block_warps_x, t.cloud_blocks_per_sm, t.cloud_ray_lanes)
 
 
 def tuning(ctx: Context) -> _abi.Tuning:

@@ -263,6 +263,26 @@ class CloudViewport:
         self.previous_view = _abi.CloudView.from_buffer_copy(view)
         return frame
 
+    def autotune(self, cloud: "VolumetricCloud", atmosphere: _abi.AtmosphereParameters, view: _abi.CloudView,
+                 sizes: _abi.LutSizes, luts: LutSet, blue_noise: torch.Tensor, depth: torch.Tensor | None = None,
+                 z_near: float = 0.1, z_far: float = 1000.0, reps: int = 5):
+        """skyr_autotune_cloud_quarter on this viewport's passes (the next
+        frame's, with history once a frame exists): keeps the fastest launch
+        shape in the context; returns (tuning, times ms per CLOUD_CANDIDATES
+        entry).  Writes the buffers of the next frame without swapping."""
+        assert view.width == self.width and view.height == self.height
+        prev = self.previous_view if self.frames else None
+        frame = temporal_frame(atmosphere, view, prev, None, z_near, z_far, int(view.frame_id))
+        b = self.buffers(True)
+        best = _abi.Tuning()
+        times = (C.c_float * _abi.SKYR_CLOUD_TUNE_CANDIDATES)()
+        _abi.call("skyr_autotune_cloud_quarter", self.ctx.handle, C.byref(atmosphere), C.byref(cloud.params),
+                  C.byref(cloud.material), C.byref(cloud.textures), C.byref(view), C.byref(sizes),
+                  _ptr(luts.transmittance), _ptr(luts.aerial_perspective_luminance),
+                  _ptr(luts.aerial_perspective_transmittance), _ptr(blue_noise), _ptr(depth), C.byref(frame),
+                  C.byref(b), reps, C.byref(best), times)
+        return best, list(times)
+
 
 def blue_noise_tile(seed: int = 0x5EED) -> torch.Tensor:
     """Seeded 64x64 blue-noise tile (host float32)."""

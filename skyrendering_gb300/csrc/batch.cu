@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/skyr_batch.h"
+#include "../../include/skyr_cloud_quarter.h"
 #include "skyr_ctx.cuh"
 #include "skyr_internal.cuh"
 
@@ -49,6 +50,7 @@ constexpr int kTileCandidates[SKYR_CLOUD_TILE_CANDIDATES][2] = {
 constexpr int kLaneCandidates[3] = {4, 8, 16};
 
 constexpr int kOccupancyCandidates[2] = {5, 6};
+constexpr int kRayLaneCandidates[4] = {1, 2, 4, 8};
 
 bool valid_lanes(int l) { return l == 4 || l == 8 || l == 16; }
 bool valid_tile(int w, int bx) { return (w == 4 || w == 8 || w == 16 || w == 32) && (bx == 1 || bx == 2 || bx == 4); }
@@ -73,13 +75,44 @@ int time_launches(skyr_ctx* ctx, int reps, F&& fn, float* ms) {
     return st;
 }
 
+// Times `run` for every cloud candidate (ray lanes x blocks per SM x tile
+// shapes, the order of skyr_autotune_cloud's times) and keeps the fastest.
+static_assert(SKYR_CLOUD_TUNE_CANDIDATES == 4 * 2 * SKYR_CLOUD_TILE_CANDIDATES, "cloud candidate table");
+
+template <class F>
+int autotune_cloud_candidates(skyr_ctx* ctx, int reps, skyr_tuning* best, float* times_ms, F&& run) {
+    if (!ctx || !best) return set_error(SKYR_EINVAL, "null argument");
+    if (reps < 1 || reps > 1000) return set_error(SKYR_EINVAL, "reps must be in [1, 1000]");
+    const skyr_tuning start = ctx->tuning;
+    float tt[SKYR_CLOUD_TUNE_CANDIDATES] = {};
+    int best_i = -1, st = SKYR_OK;
+    auto apply = [&](int i) {
+        const int* tile = kTileCandidates[i % SKYR_CLOUD_TILE_CANDIDATES];
+        ctx->tuning.cloud_tile_width = tile[0];
+        ctx->tuning.cloud_block_warps_x = tile[1];
+        ctx->tuning.cloud_blocks_per_sm = kOccupancyCandidates[(i / SKYR_CLOUD_TILE_CANDIDATES) % 2];
+        ctx->tuning.cloud_ray_lanes = kRayLaneCandidates[i / (2 * SKYR_CLOUD_TILE_CANDIDATES)];
+    };
+    for (int i = 0; i < SKYR_CLOUD_TUNE_CANDIDATES && !st; ++i) {
+        apply(i);
+        st = time_launches(ctx, reps, run, &tt[i]);
+        if (!st && (best_i < 0 || tt[i] < tt[best_i])) best_i = i;
+    }
+    ctx->tuning = start;
+    if (st) return st;
+    apply(best_i);
+    if (times_ms) std::memcpy(times_ms, tt, sizeof(tt));
+    *best = ctx->tuning;
+    return SKYR_OK;
+}
+
 }  // namespace
 
 extern "C" {
 
 int skyr_tuning_default(skyr_tuning* t) {
     if (!t) return set_error(SKYR_EINVAL, "null tuning");
-    *t = skyr_tuning{8, 8, 8, 2, 5};
+    *t = skyr_tuning{8, 8, 8, 2, 5, 1};
     return SKYR_OK;
 }
 
@@ -91,6 +124,8 @@ int skyr_ctx_set_tuning(skyr_ctx* ctx, const skyr_tuning* t) {
         return set_error(SKYR_EINVAL, "cloud tile width must be 4, 8, 16 or 32 and block warps 1, 2 or 4");
     if (t->cloud_blocks_per_sm != 5 && t->cloud_blocks_per_sm != 6)
         return set_error(SKYR_EINVAL, "cloud blocks per SM must be 5 or 6");
+    if (t->cloud_ray_lanes != 1 && t->cloud_ray_lanes != 2 && t->cloud_ray_lanes != 4 && t->cloud_ray_lanes != 8)
+        return set_error(SKYR_EINVAL, "cloud ray lanes must be 1, 2, 4 or 8");
     ctx->tuning = *t;
     return SKYR_OK;
 }
@@ -243,31 +278,27 @@ int skyr_autotune_cloud(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosph
                         const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
                         const float* blue_noise, void* out_rgba, float* out_distance, int reps, skyr_tuning* best,
                         float* times_ms) {
-    if (!ctx || !best) return set_error(SKYR_EINVAL, "null argument");
-    if (reps < 1 || reps > 1000) return set_error(SKYR_EINVAL, "reps must be in [1, 1000]");
-    const skyr_tuning start = ctx->tuning;
-    float tt[SKYR_CLOUD_TUNE_CANDIDATES] = {};
-    int best_i = -1, st = SKYR_OK;
-    for (int i = 0; i < SKYR_CLOUD_TUNE_CANDIDATES && !st; ++i) {
-        const int* tile = kTileCandidates[i % SKYR_CLOUD_TILE_CANDIDATES];
-        ctx->tuning.cloud_tile_width = tile[0];
-        ctx->tuning.cloud_block_warps_x = tile[1];
-        ctx->tuning.cloud_blocks_per_sm = kOccupancyCandidates[i / SKYR_CLOUD_TILE_CANDIDATES];
-        st = time_launches(ctx, reps, [&]() {
-            return cloud_render_on(ctx, ctx->stream, atmosphere, cloud, material, textures, view, sizes, transmittance,
-                                   aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise, nullptr,
-                                   out_rgba, out_distance, nullptr);
-        }, &tt[i]);
-        if (!st && (best_i < 0 || tt[i] < tt[best_i])) best_i = i;
-    }
-    ctx->tuning = start;
-    if (st) return st;
-    ctx->tuning.cloud_tile_width = kTileCandidates[best_i % SKYR_CLOUD_TILE_CANDIDATES][0];
-    ctx->tuning.cloud_block_warps_x = kTileCandidates[best_i % SKYR_CLOUD_TILE_CANDIDATES][1];
-    ctx->tuning.cloud_blocks_per_sm = kOccupancyCandidates[best_i / SKYR_CLOUD_TILE_CANDIDATES];
-    if (times_ms) std::memcpy(times_ms, tt, sizeof(tt));
-    *best = ctx->tuning;
-    return SKYR_OK;
+    return autotune_cloud_candidates(ctx, reps, best, times_ms, [&]() {
+        return cloud_render_on(ctx, ctx->stream, atmosphere, cloud, material, textures, view, sizes, transmittance,
+                               aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise, nullptr,
+                               out_rgba, out_distance, nullptr);
+    });
+}
+
+int skyr_autotune_cloud_quarter(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                                const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                                const skyr_cloud_textures* textures, const skyr_cloud_view* view,
+                                const skyr_lut_sizes* sizes, const void* transmittance,
+                                const void* aerial_perspective_luminance,
+                                const void* aerial_perspective_transmittance, const float* blue_noise,
+                                const float* depth, const skyr_cloud_temporal_frame* frame,
+                                const skyr_cloud_quarter_buffers* buffers, int reps, skyr_tuning* best,
+                                float* times_ms) {
+    return autotune_cloud_candidates(ctx, reps, best, times_ms, [&]() {
+        return skyr_cloud_render_quarter(ctx, atmosphere, cloud, material, textures, view, sizes, transmittance,
+                                         aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise,
+                                         depth, frame, buffers, nullptr);
+    });
 }
 
 int skyr_graph_begin(skyr_ctx* ctx) {

@@ -7,6 +7,7 @@
 // texture units interpolate with 8-bit weights).  The shell intersections use
 // cancellation-free FP32 forms; all frame derivations are done on the host in
 // double.
+#include <algorithm>
 #include <cmath>
 #include <type_traits>
 #include <cstring>
@@ -14,6 +15,7 @@
 #include "atmosphere_kernels.cuh"
 #include "cloud_internal.cuh"
 #include "cloud_material.cuh"
+#include "cloud_march.cuh"
 #include "lut_access.cuh"
 #include "skyr_ctx.cuh"
 
@@ -267,269 +269,6 @@ int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud
     return SKYR_OK;
 }
 
-// ---------------------------------------------------------------------------
-// Device: the raymarch
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float hg(float c, float g) {  // VolumetricCloudCommon.glsl:58-63
-    float a = 1.f - g * g;
-    float b = fmaf(-2.f * g, c, 1.f + g * g);
-    return (0.25f / SKYR_PI) * __fdividef(a, b * sqrtf(b));
-}
-
-// 1 - exp(-x) without cancellation (x >= 0); also returns exp(-x)
-__device__ __forceinline__ float one_minus_exp(float x, float& e) {
-    float phi = seg_phi(x, e);
-    return x * phi;
-}
-
-// SampleShadow (VolumetricCloudRender.comp:98-114).  The loop variable
-// accumulates in FP32 exactly as the reference's `t += inv_shadow_steps`.
-// Sample heights come from rho2(d) = rho2_p + d (2 q + d) with
-// q = sun . (p + R z^), exact relative to the primary sample.
-__device__ __forceinline__ float sample_shadow(const CloudConsts& C, const MaterialConsts& M, float3 pos,
-                                               float rho2_p) {
-    float od = 0.f;
-    float inv = 1.f / C.shadow_steps;
-    float3 sv = C.sun * C.shadow_distance;
-    float q2 = 2.f * fmaf(C.sun.x, pos.x, fmaf(C.sun.y, pos.y, C.sun.z * (pos.z + C.R)));
-    float prev = 0.f;
-    for (float t = inv; t <= 1.f; t += inv) {
-        float cur = t * t;
-        float dt = cur - prev;
-        float f = fmaf(0.5f, dt, prev);
-        float3 sp = pos + sv * f;
-        float d = C.shadow_distance * f;
-        float h = height01_rho2(C, fmaf(d, q2 + d, rho2_p));
-        float3 dc = sp - C.cam;
-        od += sigma_t(C, M, sp, h, sqrtf(dot3(dc, dc))) * C.shadow_distance * dt;
-        prev = cur;
-    }
-    return __expf(-od);
-}
-
-// number of light-march samples of `for (float t = inv; t <= 1; t += inv)`
-__device__ __forceinline__ unsigned shadow_sample_count(float steps) {
-    unsigned n = 0;
-    float inv = 1.f / steps;
-    for (float t = inv; t <= 1.f; t += inv) ++n;
-    return n;
-}
-
-struct March {
-    float trans, trans_sum, wsum, sun, env;
-    unsigned samples, evals;  // work counters (instrumented launches only)
-};
-
-// One shell segment [t0, t1] of the raymarch loop (VolumetricCloudRender.comp:160-187).
-// Sample heights are taken relative to the segment entry, whose
-// rho2_e = R_e^2 - R^2 is exact: rho2(t0 + e) = rho2_e + e (k_e + e) with
-// k_e = 2 (r mu + t0) = 2 R_e mu_e.
-__device__ __forceinline__ void march_segment(const CloudConsts& C, const MaterialConsts& M, float3 view,
-                                              float t0, float t1, float rho2_e, float k_e, float jitter,
-                                              float ph_back, float ph_fwd, March& S) {
-    float dist = fminf(t1 - t0, C.max_raymarch_distance);
-    unsigned n = (unsigned)fmaxf(C.max_raymarch_steps * (dist / C.max_raymarch_distance), 1.f);
-    float step = dist / (float)n;
-    float e = step * jitter;
-    float t = t0 + e;
-    for (unsigned k = n; k != 0; --k, t += step, e += step) {
-        float3 pos = C.cam + view * t;
-        float rho2 = fmaf(e, k_e + e, rho2_e);
-        float h = height01_rho2(C, rho2);
-        // RayMarchStep (VolumetricCloudRender.comp:116-137)
-        float sigma = sigma_t(C, M, pos, h, t);
-        S.samples++;
-        S.evals++;
-        if (sigma >= 1e-5f) {
-            S.evals += shadow_sample_count(C.shadow_steps);
-            float tr;
-            float one_m_tr = one_minus_exp(step * sigma, tr);
-            float tsun = sample_shadow(C, M, pos, rho2);
-            float w = __expf(-C.sun_ms_sigma_scale * sigma);
-            float phase = ph_back * (1.f - w) + ph_fwd * w;
-            float e_dummy;
-            float env = fmaf(h, 1.f - C.env_bottom_visibility, C.env_bottom_visibility) *
-                        one_minus_exp(C.env_ms_sigma_scale * sigma, e_dummy);
-            S.sun += S.trans * (tsun * phase) * one_m_tr;
-            S.env += S.trans * env * one_m_tr;
-            S.trans_sum += S.trans;
-            S.wsum += t * S.trans;
-            S.trans *= tr;
-        }
-        if (S.trans < 0.01f) break;
-    }
-}
-
-// Shell intersections (RayShellIntersect, VolumetricCloudRender.comp:39-71) in
-// cancellation-free form: with c = (R_x - r)(R_x + r), -r mu + sqrt(d) equals
-// c / (r mu + sqrt(d)) for mu > 0, and -r mu - sqrt(d) equals
-// -c / (-r mu + sqrt(d)) for mu < 0.
-__device__ __forceinline__ void shell_intersect(const CloudConsts& C, float mu, float t[4], float e[2]) {
-    float r = C.R + C.cam.z;
-    float rm = r * mu;
-    float cb = (C.bottom - C.cam.z) * (C.rb + r);
-    float ct = (C.top - C.cam.z) * (C.rt + r);
-    float db = fmaf(rm, rm, cb), dt = fmaf(rm, rm, ct);
-    float sb = sqrtf(fmaxf(db, 0.f)), st = sqrtf(fmaxf(dt, 0.f));
-    auto plus = [&](float c, float s) { return rm > 0.f ? c / (rm + s) : s - rm; };
-    auto minus = [&](float c, float s) { return -c / (s - rm); };
-    t[0] = t[1] = t[2] = t[3] = 0.f;
-    // entry rho2 of each segment: the bottom / top sphere or the camera
-    e[0] = C.cam_rho2;
-    e[1] = C.rho2_bottom;
-    if (C.cam.z < C.bottom) {
-        t[0] = plus(cb, sb);
-        t[1] = plus(ct, st);
-        e[0] = C.rho2_bottom;
-    } else if (C.cam.z < C.top) {
-        if (db >= 0.f && mu < 0.f) {
-            t[1] = minus(cb, sb);
-            t[2] = sb - rm;
-            t[3] = st - rm;
-        } else {
-            t[1] = plus(ct, st);
-        }
-    } else {
-        if (db >= 0.f && mu < 0.f) {
-            t[0] = minus(ct, st);
-            t[1] = minus(cb, sb);
-            t[2] = sb - rm;
-            t[3] = st - rm;
-            e[0] = C.rho2_top;
-        } else if (dt >= 0.f && mu < 0.f) {
-            t[0] = minus(ct, st);
-            t[1] = st - rm;
-            e[0] = C.rho2_top;
-        }
-    }
-}
-
-// counters (optional): the frame's raymarch samples and density evaluations.
-// MINB: resident blocks per SM the register budget is cut for (a tuning
-// choice, skyr_tuning::cloud_blocks_per_sm).
-template <class S, int MINB>
-__global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
-                                                           const float4* __restrict__ tlut, int tw, int th,
-                                                           const S* __restrict__ ap_lum,
-                                                           const S* __restrict__ ap_trans,
-                                                           const float* __restrict__ blue_noise,
-                                                           const float* __restrict__ depth,
-                                                           __half2* __restrict__ out_rgba,
-                                                           float* __restrict__ out_dist,
-                                                           unsigned long long* __restrict__ counters,
-                                                           int tile_w, int warps_x) {
-    // a warp covers tile_w x (32 / tile_w) pixels; the block's 4 warps sit
-    // warps_x across and 4 / warps_x down (skyr_tuning)
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int tile_h = 32 / tile_w, warps_y = 4 / warps_x;
-    int px = blockIdx.x * (tile_w * warps_x) + (warp % warps_x) * tile_w + (lane % tile_w);
-    int py = blockIdx.y * (tile_h * warps_y) + (warp / warps_x) * tile_h + (lane / tile_w);
-    if (px >= C.width || py >= C.height) return;
-    size_t pix = (size_t)py * C.width + px;
-    float u, v, e;
-    if (C.cb_index) {
-        // VolumetricCloudRender.comp:140-146: the checkerboard texel chosen
-        // for this frame gives the ray; (px, py) the noise and the output
-        unsigned idx = (unsigned)(int)__ldg(&C.cb_index[pix].x) & 3u;
-        int cx = 2 * px + (int)(((idx + 1u) >> 1) & 1u), cy = 2 * py + (int)(((idx + 2u) >> 1) & 1u);
-        u = ((float)cx + 0.5f) / (float)C.cb_w;
-        v = ((float)cy + 0.5f) / (float)C.cb_h;
-        e = 2.f * (__ldg(C.cb_depth + (size_t)cy * C.cb_w + cx) - 1.f);
-    } else {
-        u = ((float)px + 0.5f) / (float)C.width;
-        v = ((float)py + 0.5f) / (float)C.height;
-        e = depth ? 2.f * (__ldg(depth + pix) - 1.f) : 0.f;
-    }
-    float x = 2.f * u - 1.f, y = 2.f * v - 1.f;
-    float3 dir = C.a0 * x + C.a1 * y + C.a2 * e + C.af;
-    float wv = fmaf(C.w0, x, fmaf(C.w1, y, fmaf(C.w2, e, C.wf)));
-    float len = sqrtf(dot3(dir, dir));
-    float3 view = dir * (copysignf(1.f, wv) / len);
-    float frag_dist = len / fabsf(wv);
-    float mu = view.z;
-    float it[4], ent[2];
-    shell_intersect(C, mu, it, ent);
-    float vis = fminf(frag_dist, C.max_visible_distance);
-    it[1] = fminf(fmaxf(vis, it[0]), it[1]);
-    it[3] = fminf(fmaxf(vis, it[2]), it[3]);
-    float cos_sv = dot3(C.sun, view);
-    float ph_back = hg(cos_sv, C.g_back) * C.back_scale, ph_fwd = hg(cos_sv, C.g_fwd);
-    float noise = __ldg(blue_noise + (py & 63) * 64 + (px & 63));
-    float j = noise + C.jitter_offset;
-    float jitter = j - floorf(j);
-    March mk{1.f, 0.f, 0.f, 0.f, 0.f, 0u, 0u};
-    float rmu = (C.R + C.cam.z) * mu;
-    // the (up to) two shell segments share one inlined copy of the march
-#pragma unroll 1
-    for (int sg = 0; sg < 2; ++sg) {
-        float t0 = sg ? it[2] : it[0], t1 = sg ? it[3] : it[1];
-        if (sg && !(t1 - t0 > 0.f)) break;
-        march_segment(C, M, view, t0, t1, sg ? ent[1] : ent[0], 2.f * (rmu + t0), jitter, ph_back, ph_fwd, mk);
-    }
-
-    float avg_t = mk.wsum == 0.f ? frag_dist : mk.wsum / mk.trans_sum;
-    float3 ap = C.cam + view * avg_t;
-    // GetSunVisibility(transmittance_texture, pos) at the mean depth
-    float rho2 = fmaf(ap.x, ap.x, fmaf(ap.y, ap.y, ap.z * (ap.z + 2.f * C.R)));
-    float r2 = fmaf(C.R, C.R, rho2);
-    float inv_r = rsqrtf(r2);
-    float rr = r2 * inv_r;
-    float hh = __fdividef(rho2, rr + C.R);
-    float mu_s = fmaf(C.sun.x, ap.x, fmaf(C.sun.y, ap.y, C.sun.z * (ap.z + C.R))) * inv_r;
-    float3 sunvis = sun_visibility_lut(A, tlut, tw, th, rr, rho2, hh, mu_s);
-    float sun_cos = clamp01(mu_s);
-    float3 lum = sunvis * (mk.sun * C.sun_illuminance_scale) * A.solar_illuminance +
-                 C.env_color_scale * (mk.env * __powf(sun_cos, C.env_sun_height_curve_exp));
-    // GetAerialPerspective (VolumetricCloudCommon.glsl:81-98)
-    float ta = avg_t;
-    if (C.atmo_in_space != 0.f) {
-        float r = C.R + C.cam.z, rm = r * mu;
-        float c = (C.cam.z - A.thickness) * (r + A.top);
-        float disc = rm * rm - c;
-        if (mu < 0.f && disc >= 0.f) ta -= fmaxf(c / (-rm + sqrtf(disc)), 0.f);
-        else ta = 0.f;
-    }
-    float wz = sqrtf(fmaxf(ta, 0.f) * C.inv_ap_max_distance);
-    float3 at = trilinear_clamp(ap_trans, C.ap_w, C.ap_h, C.ap_d, u * (float)(C.ap_w - 1), v * (float)(C.ap_h - 1),
-                                wz * (float)(C.ap_d - 1));
-    float3 al = trilinear_clamp(ap_lum, C.ap_w, C.ap_h, C.ap_d, u * (float)(C.ap_w - 1), v * (float)(C.ap_h - 1),
-                                wz * (float)(C.ap_d - 1));
-    al = al * froxel_visibility(C, u, v, avg_t);  // VolumetricCloudRender.comp:198
-    lum = lum * at + al * (1.f - mk.trans);
-    lum = lum * (1.f / fmaxf(1e-5f, 1.f - mk.trans));
-    float fade = smoothstepf(C.max_visible_distance * 0.75f, C.max_visible_distance, it[0]);
-    float trans = mk.trans + (1.f - mk.trans) * fade;
-    lum = lum * (1.f - trans);
-    if (out_rgba) {
-        __half2 lo = __floats2half2_rn(lum.x, lum.y), hi = __floats2half2_rn(lum.z, trans);
-        uint2 raw;
-        raw.x = *reinterpret_cast<uint32_t*>(&lo);
-        raw.y = *reinterpret_cast<uint32_t*>(&hi);
-        reinterpret_cast<uint2*>(out_rgba)[pix] = raw;
-    }
-    if (out_dist) out_dist[pix] = avg_t;
-    if (counters) {
-        unsigned long long a = mk.samples, b = mk.evals;
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_xor_sync(__activemask(), a, o);
-            b += __shfl_xor_sync(__activemask(), b, o);
-        }
-        if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) {
-            atomicAdd(counters, a);
-            atomicAdd(counters + 1, b);
-        }
-    }
-}
-
-}  // namespace skyr
-
-using namespace skyr;
-
-extern "C" {
-
-}  // extern "C"
-
-namespace skyr {
 int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_parameters* atmosphere,
                     const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
                     const skyr_cloud_textures* textures, const skyr_cloud_view* view, const skyr_lut_sizes* sizes,
@@ -570,28 +309,35 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
     derive_atmo_consts(*atmosphere, A);
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     const int tile_w = ctx->tuning.cloud_tile_width, warps_x = ctx->tuning.cloud_block_warps_x;
-    const int bw = tile_w * warps_x, bh = (32 / tile_w) * (4 / warps_x);
+    const int G = ctx->tuning.cloud_ray_lanes, tw = std::min(tile_w, 32 / G);
+    const int bw = tw * warps_x, bh = (32 / G / tw) * (4 / warps_x);
     dim3 grid((C.width + bw - 1) / bw, (C.height + bh - 1) / bh);
     const float4* T = reinterpret_cast<const float4*>(transmittance);
-    auto launch = [&](auto tag, auto minb) {
-        using S = decltype(tag);
-        cloud_render_kernel<S, decltype(minb)::value><<<grid, 128, 0, stream>>>(
-            C, M, A, T, sizes->transmittance_width, sizes->transmittance_height,
-            reinterpret_cast<const S*>(aerial_perspective_luminance),
-            reinterpret_cast<const S*>(aerial_perspective_transmittance), blue_noise, depth,
-            reinterpret_cast<__half2*>(out_rgba), out_distance, counters, tile_w, warps_x);
-    };
     const bool half = sizes->format == SKYR_FORMAT_RGBA16F;
-    if (ctx->tuning.cloud_blocks_per_sm == 6) {
-        if (half) launch(__half2{}, std::integral_constant<int, 6>{});
-        else launch(float4{}, std::integral_constant<int, 6>{});
-    } else {
-        if (half) launch(__half2{}, std::integral_constant<int, 5>{});
-        else launch(float4{}, std::integral_constant<int, 5>{});
-    }
+    const int occ = ctx->tuning.cloud_blocks_per_sm;
+    auto* out = reinterpret_cast<__half2*>(out_rgba);
+    const int tlw = sizes->transmittance_width, tlh = sizes->transmittance_height;
+    if (G == 8)
+        launch_cloud_render<8>(half, occ, grid, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
+                               aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,
+                               tile_w, warps_x);
+    else if (G == 4)
+        launch_cloud_render<4>(half, occ, grid, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
+                               aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,
+                               tile_w, warps_x);
+    else if (G == 2)
+        launch_cloud_render<2>(half, occ, grid, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
+                               aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,
+                               tile_w, warps_x);
+    else
+        launch_cloud_render<1>(half, occ, grid, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
+                               aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,
+                               tile_w, warps_x);
     return check_cuda(cudaGetLastError(), "cloud raymarch kernel");
 }
 }  // namespace skyr
+
+using namespace skyr;
 
 extern "C" {
 

@@ -1,0 +1,10 @@
+// cloud_lanes4.cu — the cloud raymarch kernel with 4 lanes per ray
+// (skyr_tuning::cloud_ray_lanes = 4), in its own translation unit so that
+// the raymarch variants compile in parallel.
+#include "cloud_march.cuh"
+
+namespace skyr {
+template void launch_cloud_render<4>(bool, int, dim3, cudaStream_t, const CloudConsts&, const MaterialConsts&,
+                                      const AtmoConsts&, const float4*, int, int, const void*, const void*,
+                                      const float*, const float*, __half2*, float*, unsigned long long*, int, int);
+}  // namespace skyr

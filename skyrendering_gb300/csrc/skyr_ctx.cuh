@@ -20,7 +20,7 @@ struct skyr_ctx {
     size_t pt_scratch_bytes = 0;
     int* d_status = nullptr;  // device-side error flags of bounded waits
     // launch shapes (skyr_batch.h)
-    skyr_tuning tuning{8, 8, 8, 2, 5};
+    skyr_tuning tuning{8, 8, 8, 2, 5, 1};
     // internal streams and events that fan a call's independent launches out
     // from the context's stream and join them back (created on first use)
     static constexpr int kAux = 4;

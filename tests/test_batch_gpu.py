@@ -5,9 +5,10 @@ launch-shape tuning, the autotuners, multi-view raymarches and CUDA graphs.
   constants: bit-identical LUTs;
 * lanes per texel change only the order of the per-ray sums: LUTs within 2e-6
   relative (FP32) / one FP16 step (FP16) of the default;
-* the raymarch's warp-tile shape and register budget change only which lane
-  computes a pixel and how it is scheduled: the 24 shapes give bit-identical
-  frames;
+* the raymarch's warp-tile shape, register budget and lanes per ray change
+  only which lane computes a step and how it is scheduled (with 2 or 4 lanes
+  per ray the steps are folded in step order with the same FP32 operations):
+  the 96 shapes give bit-identical frames;
 * views rendered together (forked streams) or replayed from a CUDA graph are
   bit-identical to one skyr_cloud_render per view;
 * a seeded subset of the batched workload (perturbed atmospheres, altitudes up
@@ -100,12 +101,12 @@ def test_cloud_tile_shapes_are_identical(sctx):
     view = W.frame_view(cam, 45.0, width=320, height=180)
     ref_rgba, ref_dist = cl.vc.render(atmo, view, sizes, luts, cl.bn)
     ref_rgba, ref_dist = ref_rgba.clone(), ref_dist.clone()
-    for w, bx, occ in B.CLOUD_CANDIDATES:
-        B.set_tuning(sctx, cloud_tile_width=w, cloud_block_warps_x=bx, cloud_blocks_per_sm=occ)
+    for w, bx, occ, g in B.CLOUD_CANDIDATES:
+        B.set_tuning(sctx, cloud_tile_width=w, cloud_block_warps_x=bx, cloud_blocks_per_sm=occ, cloud_ray_lanes=g)
         rgba, dist = cl.vc.render(atmo, view, sizes, luts, cl.bn)
         sctx.synchronize()
-        assert torch.equal(rgba, ref_rgba), (w, bx, occ)
-        assert torch.equal(dist, ref_dist), (w, bx, occ)
+        assert torch.equal(rgba, ref_rgba), (w, bx, occ, g)
+        assert torch.equal(dist, ref_dist), (w, bx, occ, g)
 
 
 def _batched(ctx, n_sets=6, n_views=5, fmt=1):
@@ -170,8 +171,8 @@ def test_autotuners(sctx):
     dist = torch.empty((360, 640), dtype=torch.float32, device="cuda")
     best, times = B.autotune_cloud(sctx, atmo, cl.cloud, cl.material, cl.textures, view, sizes, l1, cl.bn, rgba,
                                    dist, reps=2)
-    key = (best.cloud_tile_width, best.cloud_block_warps_x, best.cloud_blocks_per_sm)
-    assert key in B.CLOUD_CANDIDATES
+    key = B.cloud_tuning_key(best)
+    assert key in B.CLOUD_CANDIDATES and len(times) == len(B.CLOUD_CANDIDATES) == 96
     assert min(times) == pytest.approx(times[B.CLOUD_CANDIDATES.index(key)])
 
 
@@ -211,6 +212,10 @@ def test_invalid_arguments(sctx):
         B.set_tuning(sctx, transmittance_lanes=5)
     with pytest.raises(_abi.SkyrError):
         B.set_tuning(sctx, cloud_tile_width=64)
+    with pytest.raises(_abi.SkyrError):
+        B.set_tuning(sctx, cloud_ray_lanes=3)
+    with pytest.raises(_abi.SkyrError):
+        B.set_tuning(sctx, cloud_ray_lanes=16)
     cl = Clouds(sctx)
     params, renders, views, sov, sizes, luts, b = _batched(sctx, n_sets=2, n_views=2)
     out = B.ViewOutputs(views, 2)

@@ -14,7 +14,10 @@ and as a whole chain.
   raymarch, reconstruct and upscale): mean relative error <= 1e-3;
 * a synthetic depth buffer (the Earth's surface and a near occluder) drives
   the depth-aware paths; viewport 480x270 gives odd half / quarter sizes;
-* graph replay is bit-identical; bad arguments are refused.
+* graph replay is bit-identical, and so is the raymarch with 2, 4 or 8 lanes
+  per ray; bad arguments are refused;
+* the quarter-pass autotuner times all 96 launch shapes on the pass itself and
+  keeps the fastest, which renders the same texels as the default shape.
 """
 import numpy as np
 import pytest
@@ -214,6 +217,15 @@ def test_graph_replay_and_invalid_arguments(sctx):
     for a, r in zip(got, ref):
         assert torch.equal(a, r)
     cap.graph.close()
+    # the checkerboard raymarch with 2, 4 or 8 lanes per ray: the same texels bit for bit
+    for g in (2, 4, 8):
+        B.set_tuning(sctx, cloud_ray_lanes=g, cloud_tile_width=8)
+        hdr.copy_(q.hdr_in)
+        _abi.call("skyr_cloud_render_quarter", *args, C.c_void_p(hdr.data_ptr()))
+        sctx.synchronize()
+        for a, r in zip((q.vp.render_rgba, q.vp.render_distance, hdr), (ref[2], ref[3], ref[5])):
+            assert torch.equal(a, r), g
+    B.set_tuning(sctx, cloud_ray_lanes=1)
     bad = _abi.CloudQuarterBuffers.from_buffer_copy(b)
     bad.previous_reconstruct = bad.reconstruct
     with pytest.raises(_abi.SkyrError):
@@ -222,3 +234,26 @@ def test_graph_replay_and_invalid_arguments(sctx):
     bad.render_rgba = None
     with pytest.raises(_abi.SkyrError):
         _abi.call("skyr_cloud_render_quarter", *args[:-1], C.byref(bad), None)
+
+
+def test_quarter_autotuner(sctx):
+    cam = W.frame_camera()
+    q = Quarter(sctx, cam, 640, 360, depth=False)
+    q.render(history=False)
+    f = q.f
+    best, times = q.vp.autotune(f.vc, f.atmo, f.view, f.sizes, f.luts, f.bn, z_near=Z_NEAR, z_far=Z_FAR, reps=2)
+    key = B.cloud_tuning_key(best)
+    assert key in B.CLOUD_CANDIDATES and len(times) == len(B.CLOUD_CANDIDATES)
+    assert all(t > 0 for t in times)
+    assert min(times) == pytest.approx(times[B.CLOUD_CANDIDATES.index(key)])
+    assert B.cloud_tuning_key(B.tuning(sctx)) == key
+    # the chosen shape renders the same texels as the default one
+    B.set_tuning(sctx, cloud_ray_lanes=1, cloud_tile_width=8, cloud_block_warps_x=2, cloud_blocks_per_sm=5)
+    q.vp.frames = 0
+    q.render(history=False)
+    got_default = q.vp.render_rgba.clone()
+    B.set_tuning(sctx, cloud_tile_width=best.cloud_tile_width, cloud_block_warps_x=best.cloud_block_warps_x,
+                 cloud_blocks_per_sm=best.cloud_blocks_per_sm, cloud_ray_lanes=best.cloud_ray_lanes)
+    q.vp.frames = 0
+    q.render(history=False)
+    assert torch.equal(q.vp.render_rgba, got_default)
