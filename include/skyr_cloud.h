@@ -195,6 +195,29 @@ int skyr_cloud_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmospher
                       const void* aerial_perspective_luminance, const void* aerial_perspective_transmittance,
                       const float* blue_noise, const float* depth, void* out_rgba, float* out_distance);
 
+/* skyr_cloud_render for a caller that reads the frame on the host: the kernel
+ * stores each pixel straight into `host_rgba` (half4 per pixel) and
+ * `host_distance` (float per pixel), so the device-to-host transfer of the
+ * frame (12 bytes per pixel) runs over the GPU's link to host memory while the
+ * raymarch is still going, instead of as a copy after it.  Same inputs, pixel
+ * values and layouts as skyr_cloud_render.  The reference leaves the pass's
+ * images on the GPU (VolumetricCloud::Render, VolumetricCloud.cpp:327) and
+ * reads frames back only as a copy after rendering (glReadPixels in
+ * GLWindow::ScreenShot, src/Base/src/GLWindow.cpp:247-252).  Both outputs
+ * must be page-locked host memory mapped for the context's device
+ * (cudaHostAlloc / cudaMallocHost under unified addressing, or cudaHostRegister
+ * with cudaHostRegisterMapped); pageable, device or misaligned pointers
+ * (host_rgba 8-byte, host_distance 4-byte) return SKYR_EINVAL before any
+ * launch.  Either may be NULL.  The writes are complete when the context's
+ * stream reaches the end of the call. */
+int skyr_cloud_render_to_host(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                              const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                              const skyr_cloud_textures* textures, const skyr_cloud_view* view,
+                              const skyr_lut_sizes* sizes, const void* transmittance,
+                              const void* aerial_perspective_luminance,
+                              const void* aerial_perspective_transmittance, const float* blue_noise,
+                              const float* depth, void* host_rgba, float* host_distance);
+
 /* skyr_cloud_render that also accumulates work counters into device memory
  * `counters` (2 x uint64, not cleared): [0] raymarch samples taken,
  * [1] SampleSigmaT evaluations (raymarch + light march).  Same outputs as

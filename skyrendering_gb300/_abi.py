@@ -257,6 +257,9 @@ _SIGNATURES.update({
     "skyr_noise_expanded_bytes": (C.c_size_t, [C.POINTER(NoiseTextureDesc), C.c_int]),
     "skyr_noise_expand": (C.c_int, [P, C.POINTER(NoiseTextureDesc), P, C.c_int, P]),
 })
+_SIGNATURES["skyr_cloud_render_to_host"] = (
+    C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters), C.POINTER(CloudMaterial),
+              C.POINTER(CloudTextures), C.POINTER(CloudView), C.POINTER(LutSizes), P, P, P, P, P, P, P])
 _SIGNATURES["skyr_cloud_render_counted"] = (
     C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters), C.POINTER(CloudMaterial),
               C.POINTER(CloudTextures), C.POINTER(CloudView), C.POINTER(LutSizes), P, P, P, P, P, P, P, P])

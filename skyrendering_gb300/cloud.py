@@ -124,6 +124,23 @@ class VolumetricCloud:
                   _ptr(out_distance))
         return out_rgba, out_distance
 
+    def render_to_host(self, atmosphere: _abi.AtmosphereParameters, view: _abi.CloudView, sizes: _abi.LutSizes,
+                       luts: LutSet, blue_noise: torch.Tensor, depth: torch.Tensor | None = None,
+                       out_rgba: torch.Tensor | None = None, out_distance: torch.Tensor | None = None):
+        """render() with the frame stored by the kernel straight into pinned
+        host tensors (skyr_cloud_render_to_host); valid once the context's
+        stream has passed the call."""
+        if out_rgba is None:
+            out_rgba = torch.empty((view.height, view.width, 4), dtype=torch.float16, pin_memory=True)
+        if out_distance is None:
+            out_distance = torch.empty((view.height, view.width), dtype=torch.float32, pin_memory=True)
+        _abi.call("skyr_cloud_render_to_host", self.ctx.handle, C.byref(atmosphere), C.byref(self.params),
+                  C.byref(self.material), C.byref(self.textures), C.byref(view), C.byref(sizes),
+                  _ptr(luts.transmittance), _ptr(luts.aerial_perspective_luminance),
+                  _ptr(luts.aerial_perspective_transmittance), _ptr(blue_noise), _ptr(depth), _ptr(out_rgba),
+                  _ptr(out_distance))
+        return out_rgba, out_distance
+
 
 def shadow_sizes(viewport_width: int, viewport_height: int) -> _abi.CloudShadowSizes:
     """512 x 512 map, (w / 12) x (h / 12) x 128 froxel (VolumetricCloud.cpp:52,134-135)."""

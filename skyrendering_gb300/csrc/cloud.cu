@@ -352,6 +352,41 @@ int skyr_cloud_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmospher
                            depth, out_rgba, out_distance, nullptr);
 }
 
+int skyr_cloud_render_to_host(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                              const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
+                              const skyr_cloud_textures* textures, const skyr_cloud_view* view,
+                              const skyr_lut_sizes* sizes, const void* transmittance,
+                              const void* aerial_perspective_luminance,
+                              const void* aerial_perspective_transmittance, const float* blue_noise,
+                              const float* depth, void* host_rgba, float* host_distance) {
+    if (!ctx) return set_error(SKYR_EINVAL, "null context");
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    // Both outputs must be page-locked host memory mapped into this device's
+    // address space; the kernel then stores through the mapped alias.  Anything
+    // else (pageable or device memory) is refused here, before any launch.
+    void* alias[2] = {nullptr, nullptr};
+    void* host[2] = {host_rgba, host_distance};
+    const size_t align[2] = {8, 4};
+    const char* name[2] = {"host_rgba", "host_distance"};
+    for (int k = 0; k < 2; ++k) {
+        if (!host[k]) continue;
+        cudaPointerAttributes a{};
+        cudaError_t e = cudaPointerGetAttributes(&a, host[k]);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(SKYR_EINVAL, "%s: not page-locked host memory (%s)", name[k], cudaGetErrorString(e));
+        }
+        if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr)
+            return set_error(SKYR_EINVAL, "%s: not page-locked host memory mapped for the device", name[k]);
+        if (reinterpret_cast<uintptr_t>(a.devicePointer) % align[k] != 0)
+            return set_error(SKYR_EINVAL, "%s: not %zu-byte aligned", name[k], align[k]);
+        alias[k] = a.devicePointer;
+    }
+    return cloud_render_on(ctx, ctx->stream, atmosphere, cloud, material, textures, view, sizes, transmittance,
+                           aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise, depth,
+                           alias[0], static_cast<float*>(alias[1]), nullptr);
+}
+
 int skyr_cloud_render_counted(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
                               const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
                               const skyr_cloud_textures* textures, const skyr_cloud_view* view,

@@ -182,3 +182,72 @@ def test_cloud_invalid_arguments(ctx):
     assert lib.skyr_noise_texture_levels(C.byref(bad)) == 0
     rc = lib.skyr_noise_generate(ctx.handle, C.byref(bad), C.c_void_p(1))
     assert rc == _abi.SKYR_EINVAL
+
+
+def _host_call(f, rgba, dist):
+    """skyr_cloud_render_to_host on Frame f's inputs with raw output pointers."""
+    import ctypes as C
+
+    L = f.luts
+    return _abi.lib().skyr_cloud_render_to_host(
+        f.vc.ctx.handle, C.byref(f.atmo), C.byref(f.vc.params), C.byref(f.vc.material), C.byref(f.vc.textures),
+        C.byref(f.view), C.byref(f.sizes), C.c_void_p(L.transmittance.data_ptr()),
+        C.c_void_p(L.aerial_perspective_luminance.data_ptr()),
+        C.c_void_p(L.aerial_perspective_transmittance.data_ptr()), C.c_void_p(f.bn.data_ptr()), None,
+        C.c_void_p(rgba), C.c_void_p(dist))
+
+
+@pytest.mark.parametrize("size", [None, (481, 271)])
+def test_render_to_host_is_the_device_frame(ctx, size):
+    """The raymarch storing into pinned host memory gives the device render's
+    frame bit for bit (1080p and a ragged size), on two calls in a row."""
+    cam = W.frame_camera() if size is None else W.Camera(pitch=10.0, width=size[0], height=size[1])
+    f = Frame(ctx, cam, 45.0)
+    want_rgba = f.rgba.cpu().view(torch.int16)
+    want_dist = f.dist.cpu().view(torch.int32)
+    rgba = torch.full(tuple(f.rgba.shape), float("nan"), dtype=torch.float16, pin_memory=True)
+    dist = torch.full(tuple(f.dist.shape), float("nan"), dtype=torch.float32, pin_memory=True)
+    for _ in range(2):
+        out_rgba, out_dist = f.vc.render_to_host(f.atmo, f.view, f.sizes, f.luts, f.bn, out_rgba=rgba,
+                                                 out_distance=dist)
+        ctx.synchronize()
+        assert out_rgba.data_ptr() == rgba.data_ptr() and out_dist.data_ptr() == dist.data_ptr()
+        assert torch.equal(rgba.view(torch.int16), want_rgba)
+        assert torch.equal(dist.view(torch.int32), want_dist)
+        rgba.fill_(float("nan"))
+        dist.fill_(float("nan"))
+    # one output alone
+    assert _host_call(f, 0, dist.data_ptr()) == _abi.SKYR_OK
+    ctx.synchronize()
+    assert torch.equal(dist.view(torch.int32), want_dist)
+
+
+def test_render_to_host_refuses_memory_the_kernel_cannot_store_to(ctx):
+    """Device, misaligned and pageable outputs are refused before any launch."""
+    cam = W.Camera(pitch=10.0, width=64, height=36)
+    f = Frame(ctx, cam, 45.0)
+    lib = _abi.lib()
+    pinned = torch.zeros(64 * 36 * 4 + 8, dtype=torch.float16, pin_memory=True)
+    pinned_d = torch.zeros(64 * 36 + 4, dtype=torch.float32, pin_memory=True)
+    # device memory
+    assert _host_call(f, f.rgba.data_ptr(), pinned_d.data_ptr()) == _abi.SKYR_EINVAL
+    assert b"host_rgba" in lib.skyr_last_error()
+    assert _host_call(f, pinned.data_ptr(), f.dist.data_ptr()) == _abi.SKYR_EINVAL
+    assert b"host_distance" in lib.skyr_last_error()
+    # misaligned pinned memory (2 bytes into the allocation)
+    assert _host_call(f, pinned.data_ptr() + 2, pinned_d.data_ptr()) == _abi.SKYR_EINVAL
+    assert b"aligned" in lib.skyr_last_error()
+    assert _host_call(f, pinned.data_ptr(), pinned_d.data_ptr() + 2) == _abi.SKYR_EINVAL
+    # pageable memory: refused, unless the platform maps it for the device, in
+    # which case the frame must be the device frame
+    pageable = torch.full((36, 64, 4), float("nan"), dtype=torch.float16)
+    assert not pageable.is_pinned()
+    rc = _host_call(f, pageable.data_ptr(), None)
+    ctx.synchronize()
+    assert rc == _abi.SKYR_EINVAL or (
+        rc == _abi.SKYR_OK and torch.equal(pageable.view(torch.int16), f.rgba.cpu().view(torch.int16)))
+    # the context still renders after the refusals
+    assert _host_call(f, pinned.data_ptr(), pinned_d.data_ptr()) == _abi.SKYR_OK
+    ctx.synchronize()
+    got = pinned[:64 * 36 * 4].view(36, 64, 4)
+    assert torch.equal(got.view(torch.int16), f.rgba.cpu().view(torch.int16))
