@@ -487,7 +487,7 @@ _SIGNATURES.update({
 # skyr_batch.h
 # ---------------------------------------------------------------------------
 SKYR_CLOUD_TILE_CANDIDATES = 12
-SKYR_CLOUD_TUNE_CANDIDATES = 96
+SKYR_CLOUD_TUNE_CANDIDATES = 192
 
 
 class Tuning(C.Structure):

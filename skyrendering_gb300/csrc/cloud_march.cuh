@@ -348,42 +348,57 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, 
     }
 }
 
-// Launches the raymarch kernel for G lanes per ray with the LUT storage type
-// (half: RGBA16F, else RGBA32F) and the register cut (MINB 5 or 6).  G = 2,
-// 4 and 8 are instantiated in their own translation units (cloud_lanes2.cu,
-// cloud_lanes4.cu, cloud_lanes8.cu) so the kernel variants compile in parallel.
+// Launches the raymarch kernel for G lanes per ray and the register cut MINB
+// (resident blocks per SM: 5, 6, 7 or 8) with the LUT storage type (half:
+// RGBA16F, else RGBA32F).  Every (G, MINB) pair is instantiated in one of the
+// cloud_raymarch_l<G>_c<cuts>.cu translation units, two cuts per unit, so the
+// kernel variants compile in parallel.
+template <int G, int MINB>
+void launch_cloud_render_cut(bool half, dim3 grid, cudaStream_t stream, const CloudConsts& C,
+                             const MaterialConsts& M, const AtmoConsts& A, const float4* tlut, int tw, int th,
+                             const void* ap_lum, const void* ap_trans, const float* blue_noise, const float* depth,
+                             __half2* out_rgba, float* out_dist, unsigned long long* counters, int tile_w,
+                             int warps_x) {
+    auto go = [&](auto tag) {
+        using S = decltype(tag);
+        cloud_render_kernel<S, MINB, G><<<grid, 128, 0, stream>>>(
+            C, M, A, tlut, tw, th, reinterpret_cast<const S*>(ap_lum), reinterpret_cast<const S*>(ap_trans),
+            blue_noise, depth, out_rgba, out_dist, counters, tile_w, warps_x);
+    };
+    if (half) go(__half2{});
+    else go(float4{});
+}
+
+#define SKYR_CLOUD_CUT_SIGNATURE(G, B)                                                                          \
+    void launch_cloud_render_cut<G, B>(bool, dim3, cudaStream_t, const CloudConsts&, const MaterialConsts&,    \
+                                       const AtmoConsts&, const float4*, int, int, const void*, const void*,   \
+                                       const float*, const float*, __half2*, float*, unsigned long long*, int, \
+                                       int)
+#define SKYR_CLOUD_CUTS(X, G) X(G, 5); X(G, 6); X(G, 7); X(G, 8)
+#define SKYR_CLOUD_CUT_EXTERN(G, B) extern template SKYR_CLOUD_CUT_SIGNATURE(G, B)
+SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 1);
+SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 2);
+SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 4);
+SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 8);
+
+// The raymarch launch for G lanes per ray at the tuning's register cut.
 template <int G>
 void launch_cloud_render(bool half, int blocks_per_sm, dim3 grid, cudaStream_t stream, const CloudConsts& C,
                          const MaterialConsts& M, const AtmoConsts& A, const float4* tlut, int tw, int th,
                          const void* ap_lum, const void* ap_trans, const float* blue_noise, const float* depth,
                          __half2* out_rgba, float* out_dist, unsigned long long* counters, int tile_w,
                          int warps_x) {
-    auto go = [&](auto tag, auto minb) {
-        using S = decltype(tag);
-        cloud_render_kernel<S, decltype(minb)::value, G><<<grid, 128, 0, stream>>>(
-            C, M, A, tlut, tw, th, reinterpret_cast<const S*>(ap_lum), reinterpret_cast<const S*>(ap_trans),
-            blue_noise, depth, out_rgba, out_dist, counters, tile_w, warps_x);
+    auto cut = [&](auto minb) {
+        launch_cloud_render_cut<G, decltype(minb)::value>(half, grid, stream, C, M, A, tlut, tw, th, ap_lum,
+                                                          ap_trans, blue_noise, depth, out_rgba, out_dist,
+                                                          counters, tile_w, warps_x);
     };
-    if (blocks_per_sm == 6) {
-        if (half) go(__half2{}, std::integral_constant<int, 6>{});
-        else go(float4{}, std::integral_constant<int, 6>{});
-    } else {
-        if (half) go(__half2{}, std::integral_constant<int, 5>{});
-        else go(float4{}, std::integral_constant<int, 5>{});
+    switch (blocks_per_sm) {
+        case 8: cut(std::integral_constant<int, 8>{}); break;
+        case 7: cut(std::integral_constant<int, 7>{}); break;
+        case 6: cut(std::integral_constant<int, 6>{}); break;
+        default: cut(std::integral_constant<int, 5>{}); break;
     }
 }
-
-extern template void launch_cloud_render<2>(bool, int, dim3, cudaStream_t, const CloudConsts&, const MaterialConsts&,
-                                            const AtmoConsts&, const float4*, int, int, const void*, const void*,
-                                            const float*, const float*, __half2*, float*, unsigned long long*, int,
-                                            int);
-extern template void launch_cloud_render<8>(bool, int, dim3, cudaStream_t, const CloudConsts&, const MaterialConsts&,
-                                            const AtmoConsts&, const float4*, int, int, const void*, const void*,
-                                            const float*, const float*, __half2*, float*, unsigned long long*, int,
-                                            int);
-extern template void launch_cloud_render<4>(bool, int, dim3, cudaStream_t, const CloudConsts&, const MaterialConsts&,
-                                            const AtmoConsts&, const float4*, int, int, const void*, const void*,
-                                            const float*, const float*, __half2*, float*, unsigned long long*, int,
-                                            int);
 
 }  // namespace skyr
