@@ -403,8 +403,12 @@ __device__ __forceinline__ void deposit(const CloudConsts& C, const AtmoConsts& 
     if (acc_sq) atomicAdd(acc_sq + pix, make_float4(x.x * x.x, x.y * x.y, x.z * x.z, x.w * x.w));
 }
 
+// Registers are cut for 6 resident blocks per SM (80 registers, ~200 B spilled,
+// from 116 at 4 blocks): the random density fetches are latency-bound and the
+// extra warps hide more of it (2.16 -> 2.01 ms per 1024^2 frame on a GB300;
+// 8 blocks: 2.05 ms).  The persistent grid follows from the occupancy query.
 template <class S>
-__global__ void __launch_bounds__(128, 4) pathtrace_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
+__global__ void __launch_bounds__(128, 6) pathtrace_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
                                                            PtConsts P, ViewConsts E,
                                                            const float4* __restrict__ tlut, int tw, int th,
                                                            const S* __restrict__ svl, const S* __restrict__ svt,
