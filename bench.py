@@ -133,6 +133,12 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def ncu_capture(kernel: str) -> dict:
+    """The committed ncu figures of one launch of `kernel` (profiles/dram_bytes_per_launch.json)."""
+    f = ROOT / "profiles" / "dram_bytes_per_launch.json"
+    return json.loads(f.read_text()).get(kernel, {}) if f.exists() else {}
+
+
 def ncu_traffic(kernel: str):
     """dram__bytes_read.sum + dram__bytes_write.sum of one launch of `kernel`
     from the committed ncu capture (profiles/dram_bytes_per_launch.json)."""
@@ -788,6 +794,7 @@ def run_skyr(args):
                      "note": "compulsory bytes; the raymarch is issue/FP32-bound on L1-resident textures"},
         "roofline_fp32": {"kernel": "cloud_render_kernel", "peak_tflops_nominal": fp32_peak,
                           "note": "152 SMs x 128 FP32 lanes x 2 x median SM clock; pipe use in profiles/"},
+        "roofline_issue": roofline_issue(cloud_mean, sm_mhz, cloud_tuned),
         "clocks": clocks,
         "wall_s": wall,
     }
@@ -850,6 +857,26 @@ def cpu_frame_ms(sample_s: float, threads: int):
         stride = max(stride // 2, 1)
     cloud_s = spent / done * npx
     return (lut_s + cloud_s) * 1000.0, done, lut_s * 1e3
+
+
+def roofline_issue(cloud_ms: float, sm_mhz: float, tuned) -> dict:
+    """The raymarch against its real bound, instruction issue: the warp
+    instructions of one launch (ncu capture of the same frame and launch shape,
+    profiles/dram_bytes_per_launch.json) over the launch's CUDA-event time,
+    against 152 SMs x 4 schedulers x one issue per cycle at the sampled clock."""
+    cap = ncu_capture("cloud_render_kernel")
+    shape = {"cloud_tile": cloud_tile(tuned.cloud_tile_width, tuned.cloud_ray_lanes),
+             "cloud_block_warps_x": tuned.cloud_block_warps_x, "cloud_blocks_per_sm": tuned.cloud_blocks_per_sm,
+             "cloud_ray_lanes": tuned.cloud_ray_lanes}
+    inst = cap.get("warp_instructions")
+    if not inst:
+        return {"kernel": "cloud_render_kernel", "achieved": None, "note": "no committed ncu instruction count"}
+    achieved = inst / (cloud_ms * 1e-3) / 1e9
+    peak = 152 * 4 * sm_mhz * 1e6 / 1e9
+    return {"kernel": "cloud_render_kernel", "bound": "issue", "achieved": achieved, "peak": peak,
+            "unit": "G warp-instructions/s", "frac": achieved / peak, "warp_instructions_per_launch": inst,
+            "capture_shape": cap.get("tuning"), "timed_shape": shape, "same_shape": cap.get("tuning") == shape,
+            "note": "peak = 152 SMs x 4 schedulers x 1 instruction/cycle x median SM clock"}
 
 
 def cpu_baseline(sample_s: float):
