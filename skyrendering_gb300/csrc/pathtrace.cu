@@ -405,8 +405,10 @@ __device__ __forceinline__ void deposit(const CloudConsts& C, const AtmoConsts& 
 
 // Registers are cut for 6 resident blocks per SM (80 registers, ~200 B spilled,
 // from 116 at 4 blocks): the random density fetches are latency-bound and the
-// extra warps hide more of it (2.16 -> 2.01 ms per 1024^2 frame on a GB300;
-// 8 blocks: 2.05 ms).  The persistent grid follows from the occupancy query.
+// extra warps hide more of it (16 frames of 1024^2: 31.7 -> 28.9 ms on a
+// GB300; 8 blocks lose, 450 B spilled).  Short jobs lose a little instead (4
+// frames of 512^2: 3.10 -> 3.23 ms).  The persistent grid follows from the
+// occupancy query.
 template <class S>
 __global__ void __launch_bounds__(128, 6) pathtrace_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
                                                            PtConsts P, ViewConsts E,
