@@ -45,8 +45,11 @@ __device__ __forceinline__ float dtex_texel(const DTex& t, int l, int c, int x, 
         y &= H - 1;
         z &= D - 1;
     }
-    size_t i = (l ? dtex_level_offset(t, l) : 0) + (size_t)c * W * H * D + ((size_t)z * H + y) * W + x;
-    return (float)__ldg(t.base + i) * (1.f / 255.f);
+    // the index within one channel of one level stays below 2^31 (noise texture
+    // sizes are capped at 2^31 texels), so only the level and channel offsets need 64 bits
+    unsigned i = ((unsigned)z * (unsigned)H + (unsigned)y) * (unsigned)W + (unsigned)x;
+    size_t off = (l ? dtex_level_offset(t, l) : 0) + (size_t)c * W * H * D;
+    return (float)__ldg(t.base + off + i) * (1.f / 255.f);
 }
 
 __device__ __forceinline__ float dtex_nearest(const DTex& t, int l, int c, float u, float v, float s) {
@@ -63,10 +66,11 @@ __device__ __forceinline__ float dtex_linear(const DTex& t, int l, int c, float 
     int x0 = (int)fx, y0 = (int)fy;
     if (l == 0 && t.ex != nullptr && c < t.ex_channels && !t.border) {
         // expanded level 0: one word holds every corner of the footprint
+        // indices within one channel stay below 2^31 (see dtex_texel)
         size_t n = (size_t)W * H * D;
-        int ix = x0 & (W - 1), iy = y0 & (H - 1);
+        unsigned ix = (unsigned)(x0 & (W - 1)), iy = (unsigned)(y0 & (H - 1));
         if (t.d <= 1) {
-            uint32_t q = __ldg(reinterpret_cast<const uint32_t*>(t.ex) + (size_t)c * n + (size_t)iy * W + ix);
+            uint32_t q = __ldg(reinterpret_cast<const uint32_t*>(t.ex) + (size_t)c * n + (iy * (unsigned)W + ix));
             float t00 = byte_f(q, 0), t10 = byte_f(q, 1), t01 = byte_f(q, 2), t11 = byte_f(q, 3);
             float top = fmaf(a, t10 - t00, t00), bot = fmaf(a, t11 - t01, t01);
             return fmaf(b, bot - top, top) * (1.f / 255.f);
@@ -74,9 +78,9 @@ __device__ __forceinline__ float dtex_linear(const DTex& t, int l, int c, float 
         float z = s * (float)D - 0.5f;
         float fz = floorf(z);
         float g = z - fz;
-        int iz = (int)fz & (D - 1);
+        unsigned iz = (unsigned)((int)fz & (D - 1));
         unsigned long long q = __ldg(reinterpret_cast<const unsigned long long*>(t.ex) + (size_t)c * n +
-                                     ((size_t)iz * H + iy) * W + ix);
+                                     ((iz * (unsigned)H + iy) * (unsigned)W + ix));
         uint32_t lo = (uint32_t)q, hi = (uint32_t)(q >> 32);
         float t000 = byte_f(lo, 0), t100 = byte_f(lo, 1), t010 = byte_f(lo, 2), t110 = byte_f(lo, 3);
         float t001 = byte_f(hi, 0), t101 = byte_f(hi, 1), t011 = byte_f(hi, 2), t111 = byte_f(hi, 3);

@@ -77,6 +77,7 @@ __device__ __forceinline__ void march_segment(const CloudConsts& C, const Materi
     float step = dist / (float)n;
     float e = step * jitter;
     float t = t0 + e;
+    const unsigned light_samples = shadow_sample_count(C.shadow_steps);  // work counter only
     for (unsigned k = n; k != 0; --k, t += step, e += step) {
         float3 pos = C.cam + view * t;
         float rho2 = fmaf(e, k_e + e, rho2_e);
@@ -86,7 +87,7 @@ __device__ __forceinline__ void march_segment(const CloudConsts& C, const Materi
         S.samples++;
         S.evals++;
         if (sigma >= 1e-5f) {
-            S.evals += shadow_sample_count(C.shadow_steps);
+            S.evals += light_samples;
             float tr;
             float one_m_tr = one_minus_exp(step * sigma, tr);
             float tsun = sample_shadow(C, M, pos, rho2);
