@@ -72,6 +72,15 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(value: float, device: str) -> float:
+    """The largest of the ranks' values (replicas: the slowest rank sets the step time)."""
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -720,9 +729,7 @@ def run_skyr(args):
     frame_ms = [a.elapsed_time(c) for a, _, c in ev]
     ms = statistics.mean(frame_ms)
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, "cuda")
 
     # work counters of one frame (instrumented launch, outside the timing)
     counters = torch.zeros(2, dtype=torch.int64, device="cuda")
