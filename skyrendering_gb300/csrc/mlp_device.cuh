@@ -83,6 +83,54 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 
 // Copy the packed network (global) into shared memory; all threads of the
 // block take part, caller synchronises.
+// The packed network into shared memory `s` by one bulk copy on the TMA
+// engine (cp.async.bulk, completion counted in bytes on the mbarrier `bar`),
+// for every thread of the block.  `g` and `s` are 16-byte aligned and
+// kPackedBytes is a multiple of 16.  The wait is bounded by ~2^31 SM cycles
+// (about a second); if any thread's wait expires, the status word gets bit 1,
+// the block waits once more (bounded) for its copy in flight, and every thread
+// gets false: the caller leaves without touching the shared copy.
+constexpr long long kBulkWaitCycles = 1ll << 31;
+
+__device__ __forceinline__ bool bulk_wait(uint32_t bar, long long budget) {
+    const long long t0 = clock64();
+    uint32_t done = 0;
+    do {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar)
+            : "memory");
+    } while (!done && clock64() - t0 < budget);
+    return done != 0;
+}
+
+__device__ __forceinline__ bool load_packed_bulk(unsigned char* s, const unsigned char* g, unsigned long long* bar,
+                                                 int* status) {
+    static_assert(kPackedBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
+    const uint32_t b = smem_u32(bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"((uint32_t)kPackedBytes)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(s)),
+                     "l"(g), "r"((uint32_t)kPackedBytes), "r"(b)
+                     : "memory");
+    }
+    // one decision for the whole block: a thread that gave up makes every thread leave
+    if (__syncthreads_and(bulk_wait(b, kBulkWaitCycles))) return true;
+    if (status && threadIdx.x == 0) atomicOr(status, 2);
+    bulk_wait(b, kBulkWaitCycles);
+    return false;
+}
+
 __device__ __forceinline__ void load_packed(unsigned char* s, const unsigned char* g) {
     const uint4* src = reinterpret_cast<const uint4*>(g);
     uint4* dst = reinterpret_cast<uint4*>(s);

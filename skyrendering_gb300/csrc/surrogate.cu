@@ -274,10 +274,8 @@ __global__ void __launch_bounds__(128, 4) surrogate_render_kernel(CloudConsts C,
     extern __shared__ __align__(16) unsigned char sm[];
     const unsigned full = 0xffffffffu;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (R.use_network) {
-        mlp::load_packed(sm, packed);
-        __syncthreads();
-    }
+    __shared__ unsigned long long net_bar;
+    if (R.use_network && !mlp::load_packed_bulk(sm, packed, &net_bar, P.status)) return;
     __nv_bfloat16* tile = reinterpret_cast<__nv_bfloat16*>(sm + mlp::kPackedBytes + warp * (kSmTile + kSmOut));
     float* yout = reinterpret_cast<float*>(sm + mlp::kPackedBytes + warp * (kSmTile + kSmOut) + kSmTile);
     const int tiles_x = (P.width + 7) / 8;
@@ -561,6 +559,9 @@ int skyr_surrogate_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmos
     P.box_max = make_float3(fminf(hw, B.hi.x), fminf(hw, B.hi.y), fminf(C.top, B.hi.z));
     P.width = view->width;
     P.height = view->height;
+    // bounded waits in the kernel (the network's bulk copy) report here
+    if (int e = ensure_status(ctx)) return e;
+    P.status = ctx->d_status;
     RenderConsts R;
     R.steps = sp->steps;
     R.use_network = sp->use_network ? 1 : 0;
