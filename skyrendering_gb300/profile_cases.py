@@ -13,7 +13,9 @@ times on one stream, synchronise and exit 0.
     python -m skyrendering_gb300.profile_cases composite --iters 3
 
 --tuning W,BX,OCC,LANES sets the cloud raymarch's launch shape (tile width,
-block warps x, blocks per SM, lanes per ray) before the case is set up.
+block warps x, blocks per SM, lanes per ray) before the case is set up;
+--lut-lanes T,V the lanes per transmittance texel and per sky-view /
+aerial-perspective ray of the LUT passes.
 
 Cases (seeded synthetic inputs from workloads.py):
   luts   the plain LUT set (T 256x64, MS 32x32, SV 192x108, AP 32^3) of the
@@ -204,6 +206,7 @@ def main(argv=None):
     ap.add_argument("--global-majorant", action="store_true")
     ap.add_argument("--frames", type=int, default=4)
     ap.add_argument("--tuning", default=None, help="W,BX,OCC,LANES of the cloud raymarch")
+    ap.add_argument("--lut-lanes", default=None, help="T,V lanes of the transmittance and view LUT passes")
     a = ap.parse_args(argv)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -213,6 +216,11 @@ def main(argv=None):
 
         w, bx, occ, g = (int(v) for v in a.tuning.split(","))
         B.set_tuning(ctx, cloud_tile_width=w, cloud_block_warps_x=bx, cloud_blocks_per_sm=occ, cloud_ray_lanes=g)
+    if a.lut_lanes:
+        from . import batch as B
+
+        tl, vl = (int(v) for v in a.lut_lanes.split(","))
+        B.set_tuning(ctx, transmittance_lanes=tl, view_lanes=vl)
     if a.case == "luts":
         step = lut_case(ctx, W.frame_camera())[-1]
     elif a.case == "cloud":
