@@ -251,3 +251,37 @@ def test_render_to_host_refuses_memory_the_kernel_cannot_store_to(ctx):
     ctx.synchronize()
     got = pinned[:64 * 36 * 4].view(36, 64, 4)
     assert torch.equal(got.view(torch.int16), f.rgba.cpu().view(torch.int16))
+
+
+def test_render_to_host_replays_from_a_graph(cuda):
+    """skyr_cloud_render_to_host captured into a CUDA graph (its pointer checks
+    run at capture) and replayed twice gives the device frame each time."""
+    from skyrendering_gb300 import batch as B
+    from skyrendering_gb300.atmosphere import Context
+
+    s = torch.cuda.Stream()  # graph capture needs a context on a created stream
+    with torch.cuda.stream(s):
+        ctx = Context(s)
+        try:
+            _replay_to_host(ctx, B)
+        finally:
+            ctx.close()
+
+
+def _replay_to_host(ctx, B):
+    cam = W.Camera(pitch=10.0, width=320, height=180)
+    f = Frame(ctx, cam, 45.0)
+    rgba = torch.full(tuple(f.rgba.shape), float("nan"), dtype=torch.float16, pin_memory=True)
+    dist = torch.full(tuple(f.dist.shape), float("nan"), dtype=torch.float32, pin_memory=True)
+    with B.capture(ctx) as cap:
+        f.vc.render_to_host(f.atmo, f.view, f.sizes, f.luts, f.bn, out_rgba=rgba, out_distance=dist)
+    try:
+        for _ in range(2):
+            rgba.fill_(float("nan"))
+            dist.fill_(float("nan"))
+            cap.graph.launch()
+            ctx.synchronize()
+            assert torch.equal(rgba.view(torch.int16), f.rgba.cpu().view(torch.int16))
+            assert torch.equal(dist.view(torch.int32), f.dist.cpu().view(torch.int32))
+    finally:
+        cap.graph.close()
