@@ -14,7 +14,13 @@
 //   * the host learns the table's device address once per device, with that
 //     device current, from cudaGetSymbolAddress (the array's name is only a
 //     host-side stand-in); the first call on a device does this and should
-//     come before any stream capture;
+//     come before any stream capture.  The address is kept for the life of
+//     the process, so a cudaDeviceReset while the library is loaded is not
+//     supported;
+//   * every call validates all of its sets first, then derives their
+//     constants on the host and copies them into the table with
+//     cudaMemcpyAsync on the context's stream, so a rejected call leaves the
+//     table as it was;
 //   * every call shares the one table and overwrites the entries it uses, so
 //     calls whose GPU work overlaps (two streams or contexts at once) race.
 #include <mutex>
@@ -81,9 +87,19 @@ extern "C" int skyr_update_lut_set_noalloc(skyr_ctx* ctx, const skyr_atmosphere_
         return set_error(SKYR_EINVAL, "n_sets %d outside [1, %d], the capacity of the static scratch table", n_sets,
                          kNoAllocMaxSets);
     if (int st = validate_sizes(sizes, true)) return st;
-    if (!transmittance || !multiscattering || !sky_view_luminance || !sky_view_transmittance ||
-        !aerial_perspective_luminance || !aerial_perspective_transmittance)
-        return set_error(SKYR_EINVAL, "null LUT output buffer");
+    if (!transmittance || !multiscattering)
+        return set_error(SKYR_EINVAL, "null transmittance or multi-scattering buffer");
+    // the view outputs as skyr_update_lut_set takes them: each (luminance, transmittance) pair given together or
+    // left out together, at least one pair given
+    if ((sky_view_luminance == nullptr) != (sky_view_transmittance == nullptr) ||
+        (aerial_perspective_luminance == nullptr) != (aerial_perspective_transmittance == nullptr))
+        return set_error(SKYR_EINVAL, "luminance and transmittance outputs must be given together");
+    if (!sky_view_luminance && !aerial_perspective_luminance) return set_error(SKYR_EINVAL, "no view LUT output given");
+    // every set is checked before the first upload, so a rejected call leaves the shared table untouched
+    for (int i = 0; i < n_sets; ++i) {
+        if (int st = validate_atmosphere(&params[i], i)) return st;
+        if (int st = validate_render(&render[i], &params[i], i)) return st;
+    }
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     void* table = nullptr;
     if (int st = jobs_address(ctx->device, &table)) return st;
@@ -91,11 +107,8 @@ extern "C" int skyr_update_lut_set_noalloc(skyr_ctx* ctx, const skyr_atmosphere_
     for (int i0 = 0; i0 < n_sets; i0 += kChunk) {
         int k = n_sets - i0 < kChunk ? n_sets - i0 : kChunk;
         for (int j = 0; j < k; ++j) {
-            int i = i0 + j;
-            if (int st = validate_atmosphere(&params[i], i)) return st;
-            if (int st = validate_render(&render[i], &params[i], i)) return st;
-            derive_atmo_consts(params[i], chunk[j].a);
-            derive_view_consts(params[i], render[i], chunk[j].v);
+            derive_atmo_consts(params[i0 + j], chunk[j].a);
+            derive_view_consts(params[i0 + j], render[i0 + j], chunk[j].v);
         }
         // pageable source: the copy is staged before cudaMemcpyAsync returns
         if (int e = check_cuda(cudaMemcpyAsync(reinterpret_cast<LutSetJob*>(table) + i0, chunk,
@@ -103,11 +116,15 @@ extern "C" int skyr_update_lut_set_noalloc(skyr_ctx* ctx, const skyr_atmosphere_
                                "upload of the static LUT job table"))
             return e;
     }
+    skyr_lut_sizes s = *sizes;  // a missing view pair launches no texels of that LUT
+    if (!sky_view_luminance) s.sky_view_width = s.sky_view_height = 0;
+    if (!aerial_perspective_luminance)
+        s.aerial_perspective_width = s.aerial_perspective_height = s.aerial_perspective_depth = 0;
     const LutSetJob* jobs = reinterpret_cast<const LutSetJob*>(table);
-    if (sizes->format == SKYR_FORMAT_RGBA16F)
-        return launch_all<__half2>(ctx, jobs, n_sets, *sizes, transmittance, multiscattering, sky_view_luminance,
+    if (s.format == SKYR_FORMAT_RGBA16F)
+        return launch_all<__half2>(ctx, jobs, n_sets, s, transmittance, multiscattering, sky_view_luminance,
                                    sky_view_transmittance, aerial_perspective_luminance,
                                    aerial_perspective_transmittance);
-    return launch_all<float4>(ctx, jobs, n_sets, *sizes, transmittance, multiscattering, sky_view_luminance,
+    return launch_all<float4>(ctx, jobs, n_sets, s, transmittance, multiscattering, sky_view_luminance,
                               sky_view_transmittance, aerial_perspective_luminance, aerial_perspective_transmittance);
 }
