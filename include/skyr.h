@@ -73,6 +73,29 @@ int skyr_ctx_synchronize(skyr_ctx* ctx);
  * reference has no device-side error reporting.) */
 int skyr_ctx_check_status(skyr_ctx* ctx);
 
+/* Bounds of the device loops that could otherwise run long on bad input or a
+ * broken device.  A loop that reaches its bound stops, sets the context's
+ * status word, and skyr_ctx_check_status reports SKYR_ETIMEOUT; nothing waits
+ * without a bound.  Each context starts with skyr_device_limits_default.
+ * (No reference counterpart: the reference has no device-side bounds.)
+ * struct id 21 of skyr_struct_size. */
+typedef struct skyr_device_limits {
+    /* samples of one free-flight or ratio-tracking walk of the path tracer
+     * (a valid scene needs ~ sigma_max x chord, tens to hundreds); default
+     * 2^20, range [1, 2^30] */
+    int32_t tracking_steps;
+    int32_t reserved; /* 0 */
+    /* SM clock cycles a block of the surrogate raymarch waits for the bulk
+     * copy of the network into its shared memory before it gives up (the
+     * block then waits for the copy in flight with the default bound and
+     * leaves without rendering); default 2^31 (about a second), range
+     * [0, 2^40] (0: no block waits, every block gives up at once) */
+    int64_t copy_wait_cycles;
+} skyr_device_limits;
+int skyr_device_limits_default(skyr_device_limits* out);
+int skyr_ctx_set_limits(skyr_ctx* ctx, const skyr_device_limits* limits); /* SKYR_EINVAL outside the ranges */
+int skyr_ctx_get_limits(const skyr_ctx* ctx, skyr_device_limits* out);
+
 /* ======================================================================== */
 /* Atmosphere                                                                */
 /* ======================================================================== */
@@ -179,13 +202,20 @@ int skyr_update_lut_set(skyr_ctx* ctx, const skyr_atmosphere_parameters* params,
  * library allocate device memory: hosts that own every device allocation
  * through their own pool or budget, or frame loops that must not take
  * cudaMalloc / cudaFree (cudaFree synchronises the device).  Same arguments,
- * outputs and results as skyr_update_lut_set; the caller still allocates the
+ * outputs and results as skyr_update_lut_set (a sky-view or aerial-perspective
+ * output pair may be left out, as there); the caller still allocates the
  * outputs.  The per-set kernel constants go to a static device table of this
  * library (SKYR_NOALLOC_MAX_SETS sets, under 100 KB, held by every GPU that
  * loads the library until exit) instead of a cudaMalloc'ed one:
  *   - n_sets above SKYR_NOALLOC_MAX_SETS is rejected with SKYR_EINVAL;
+ *   - every set is validated before anything is copied, so a rejected call
+ *     leaves the table as it was;
+ *   - each call derives the constants on the host and copies them into the
+ *     table with cudaMemcpyAsync on the context's stream;
  *   - the first call on a device looks up the table's device address
- *     (cudaGetSymbolAddress) and should come before any stream capture;
+ *     (cudaGetSymbolAddress) and should come before any stream capture; the
+ *     address is kept until exit, so cudaDeviceReset is not supported while
+ *     the library is loaded;
  *   - every call shares the one table, so calls whose GPU work overlaps
  *     (two streams or contexts at once) race.
  * No counterpart in the reference. */

@@ -80,8 +80,15 @@ class LutSizes(C.Structure):
     ]
 
 
+class DeviceLimits(C.Structure):
+    """skyr_device_limits: bounds of the device loops (skyr_ctx_set_limits)."""
+
+    _fields_ = [("tracking_steps", C.c_int32), ("reserved", C.c_int32), ("copy_wait_cycles", C.c_int64)]
+
+
 # struct id (skyr_struct_size) -> ctypes type; extended by later modules
-STRUCT_IDS: dict[int, type] = {0: AtmosphereParameters, 1: AtmosphereRenderParameters, 2: LutSizes}
+STRUCT_IDS: dict[int, type] = {0: AtmosphereParameters, 1: AtmosphereRenderParameters, 2: LutSizes,
+                               21: DeviceLimits}
 
 P = C.c_void_p
 _SIGNATURES = {
@@ -93,6 +100,9 @@ _SIGNATURES = {
     "skyr_ctx_destroy": (C.c_int, [P]),
     "skyr_ctx_synchronize": (C.c_int, [P]),
     "skyr_ctx_check_status": (C.c_int, [P]),
+    "skyr_device_limits_default": (C.c_int, [C.POINTER(DeviceLimits)]),
+    "skyr_ctx_set_limits": (C.c_int, [P, C.POINTER(DeviceLimits)]),
+    "skyr_ctx_get_limits": (C.c_int, [P, C.POINTER(DeviceLimits)]),
     "skyr_atmosphere_parameters_default": (C.c_int, [C.POINTER(AtmosphereParameters)]),
     "skyr_lut_bytes": (C.c_size_t, [C.POINTER(LutSizes), C.c_int]),
     "skyr_update_luts": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.c_int, C.POINTER(LutSizes), P, P]),
@@ -446,6 +456,8 @@ _SIGNATURES.update({
     "skyr_mlp_trainer_steps": (C.c_int, [P]),
     "skyr_mlp_trainer_copy_params": (C.c_int, [P, P]),
     "skyr_mlp_trainer_copy_packed": (C.c_int, [P, P]),
+    "skyr_mlp_trainer_save_state": (C.c_int, [P, P, P, P, C.POINTER(C.c_int)]),
+    "skyr_mlp_trainer_load_state": (C.c_int, [P, P, P, P, C.c_int]),
     "skyr_mlp_trainer_set_learning_rate": (C.c_int, [P, C.c_float]),
 })
 

@@ -43,6 +43,17 @@ class Context:
         its device status word (a tracking walk that hit its iteration cap)."""
         _abi.call("skyr_ctx_check_status", self._ctx)
 
+    @property
+    def limits(self) -> _abi.DeviceLimits:
+        """The bounds of this context's device loops (skyr_device_limits)."""
+        out = _abi.DeviceLimits()
+        _abi.call("skyr_ctx_get_limits", self._ctx, C.byref(out))
+        return out
+
+    @limits.setter
+    def limits(self, value: _abi.DeviceLimits) -> None:
+        _abi.call("skyr_ctx_set_limits", self._ctx, C.byref(value))
+
     def close(self) -> None:
         if self._ctx:
             _abi.call("skyr_ctx_destroy", self._ctx)

@@ -86,16 +86,20 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // The packed network into shared memory `s` by one bulk copy on the TMA
 // engine (cp.async.bulk, completion counted in bytes on the mbarrier `bar`),
 // for every thread of the block.  `g` and `s` are 16-byte aligned and
-// kPackedBytes is a multiple of 16.  The wait is bounded by ~2^31 SM cycles
-// (about a second); if any thread's wait expires, the status word gets bit 1,
-// the block waits once more (bounded) for its copy in flight, and every thread
-// gets false: the caller leaves without touching the shared copy.
+// kPackedBytes is a multiple of 16.  The wait is bounded by `budget` SM cycles
+// (skyr_device_limits::copy_wait_cycles, default 2^31, about a second; 0 never waits); if any
+// thread's wait expires, the status word gets bit 1, the block waits once more
+// for its copy in flight, bounded by kBulkWaitCycles whatever `budget` is (the
+// copy must land before the block's shared memory is released), and every
+// thread gets false: the caller leaves without touching the shared copy.
 constexpr long long kBulkWaitCycles = 1ll << 31;
 
+// Waits for phase 0 of the mbarrier at most `budget` SM cycles (the clock is
+// read before every try, so a budget of 0 never waits); true if it completed.
 __device__ __forceinline__ bool bulk_wait(uint32_t bar, long long budget) {
     const long long t0 = clock64();
     uint32_t done = 0;
-    do {
+    while (!done && clock64() - t0 < budget) {
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
@@ -103,12 +107,12 @@ __device__ __forceinline__ bool bulk_wait(uint32_t bar, long long budget) {
             : "=r"(done)
             : "r"(bar)
             : "memory");
-    } while (!done && clock64() - t0 < budget);
+    }
     return done != 0;
 }
 
 __device__ __forceinline__ bool load_packed_bulk(unsigned char* s, const unsigned char* g, unsigned long long* bar,
-                                                 int* status) {
+                                                 int* status, long long budget = kBulkWaitCycles) {
     static_assert(kPackedBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
     const uint32_t b = smem_u32(bar);
     if (threadIdx.x == 0) {
@@ -125,7 +129,7 @@ __device__ __forceinline__ bool load_packed_bulk(unsigned char* s, const unsigne
                      : "memory");
     }
     // one decision for the whole block: a thread that gave up makes every thread leave
-    if (__syncthreads_and(bulk_wait(b, kBulkWaitCycles))) return true;
+    if (__syncthreads_and(bulk_wait(b, budget))) return true;
     if (status && threadIdx.x == 0) atomicOr(status, 2);
     bulk_wait(b, kBulkWaitCycles);
     return false;

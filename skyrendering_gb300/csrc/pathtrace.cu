@@ -98,7 +98,7 @@ __device__ __forceinline__ bool free_flight(const PtConsts& P, const CloudConsts
                                             uint32_t& seed, float3 o, float3 d, float& t, float t_max) {
     if (!P.use_bricks) {
         float smax = P.sigma_t_max;
-        for (int it = 0; it < kMaxTrackingSteps; ++it) {
+        for (int it = 0; it < P.tracking_steps; ++it) {
             if (smax <= 0.f) return false;
             t += -logf(1.f - rand01(P, seed)) / smax;
             if (!(t <= t_max)) return false;
@@ -119,7 +119,7 @@ __device__ __forceinline__ bool free_flight(const PtConsts& P, const CloudConsts
     for (;;) {
         float m;
         for (;;) {
-            if (++it > kMaxTrackingSteps) {
+            if (++it > P.tracking_steps) {
                 flag_overrun(P);
                 return false;
             }
@@ -152,7 +152,7 @@ __device__ __forceinline__ float transmittance_estimation(const PtConsts& P, con
     if (!P.use_bricks) {
         float smax = P.sigma_t_max;
         for (int it = 0;; ++it) {
-            if (it >= kMaxTrackingSteps) {
+            if (it >= P.tracking_steps) {
                 flag_overrun(P);
                 break;
             }
@@ -171,7 +171,7 @@ __device__ __forceinline__ float transmittance_estimation(const PtConsts& P, con
         float m;
         bool done = false;
         for (;;) {
-            if (++it > kMaxTrackingSteps) {
+            if (++it > P.tracking_steps) {
                 flag_overrun(P);
                 done = true;
                 break;
@@ -734,6 +734,7 @@ int pathtrace_launch(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     if (int e = ensure_status(ctx)) return e;
     P.status = ctx->d_status;
+    P.tracking_steps = ctx->limits.tracking_steps;
     if (items * n_frames > (1LL << 30))
         return set_error(SKYR_EINVAL, "work items x frames too large for one call (2^30 paths)");
     P.n_items = (int)items;

@@ -19,6 +19,8 @@ struct skyr_ctx {
     void* pt_scratch = nullptr;
     size_t pt_scratch_bytes = 0;
     int* d_status = nullptr;  // device-side error flags of bounded waits
+    // bounds of the device loops (skyr_ctx_set_limits)
+    skyr_device_limits limits{1 << 20, 0, 1ll << 31};
     // launch shapes (skyr_batch.h)
     skyr_tuning tuning{8, 8, 8, 2, 5, 1};
     // internal streams and events that fan a call's independent launches out

@@ -73,6 +73,32 @@ extern "C" int skyr_ctx_check_status(skyr_ctx* ctx) {
     return set_error(SKYR_ETIMEOUT, "a device loop hit its iteration bound (status 0x%x)", v);
 }
 
+extern "C" int skyr_device_limits_default(skyr_device_limits* out) {
+    using namespace skyr;
+    if (!out) return set_error(SKYR_EINVAL, "null skyr_device_limits");
+    *out = skyr_ctx{}.limits;
+    return SKYR_OK;
+}
+
+extern "C" int skyr_ctx_set_limits(skyr_ctx* ctx, const skyr_device_limits* limits) {
+    using namespace skyr;
+    if (!ctx || !limits) return set_error(SKYR_EINVAL, "null argument");
+    if (limits->tracking_steps < 1 || limits->tracking_steps > (1 << 30))
+        return set_error(SKYR_EINVAL, "tracking_steps %d outside [1, 2^30]", limits->tracking_steps);
+    if (limits->copy_wait_cycles < 0 || limits->copy_wait_cycles > (1ll << 40))
+        return set_error(SKYR_EINVAL, "copy_wait_cycles %lld outside [0, 2^40]", (long long)limits->copy_wait_cycles);
+    if (limits->reserved != 0) return set_error(SKYR_EINVAL, "reserved field must be 0");
+    ctx->limits = *limits;
+    return SKYR_OK;
+}
+
+extern "C" int skyr_ctx_get_limits(const skyr_ctx* ctx, skyr_device_limits* out) {
+    using namespace skyr;
+    if (!ctx || !out) return set_error(SKYR_EINVAL, "null argument");
+    *out = ctx->limits;
+    return SKYR_OK;
+}
+
 size_t skyr_struct_size_ext(int which) {
     switch (which) {
         case 3: return sizeof(skyr_noise_texture_desc);
@@ -93,6 +119,7 @@ size_t skyr_struct_size_ext(int which) {
         case 18: return sizeof(skyr_cloud_quarter_buffers);
         case 19: return sizeof(skyr_composite_parameters);
         case 20: return sizeof(skyr_composite_inputs);
+        case 21: return sizeof(skyr_device_limits);
         default: return 0;
     }
 }

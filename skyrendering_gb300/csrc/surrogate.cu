@@ -238,6 +238,7 @@ struct RenderConsts {
     float g_fwd, g_back, ratio;
     const float* error_table;
     float nbr, inv_ref;  // view-neighbour distance and 1 / sigma_ref
+    long long copy_wait_cycles;  // bound of the wait for the network's bulk copy
 };
 
 constexpr int kBins = SKYR_SURROGATE_ERROR_BINS;
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(128, 4) surrogate_render_kernel(CloudConsts C,
     const unsigned full = 0xffffffffu;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __shared__ unsigned long long net_bar;
-    if (R.use_network && !mlp::load_packed_bulk(sm, packed, &net_bar, P.status)) return;
+    if (R.use_network && !mlp::load_packed_bulk(sm, packed, &net_bar, P.status, R.copy_wait_cycles)) return;
     __nv_bfloat16* tile = reinterpret_cast<__nv_bfloat16*>(sm + mlp::kPackedBytes + warp * (kSmTile + kSmOut));
     float* yout = reinterpret_cast<float*>(sm + mlp::kPackedBytes + warp * (kSmTile + kSmOut) + kSmTile);
     const int tiles_x = (P.width + 7) / 8;
@@ -372,6 +373,7 @@ int grid_setup(const skyr_density_grid* grid, PtConsts& P, GridBox& B) {
         !std::isfinite(grid->origin[1]) || !std::isfinite(grid->origin[2]))
         return set_error(SKYR_EINVAL, "bad density grid");
     std::memset(&P, 0, sizeof(P));
+    P.tracking_steps = skyr_ctx{}.limits.tracking_steps;
     P.grid = reinterpret_cast<const unsigned short*>(grid->data);
     P.nx = grid->nx;
     P.ny = grid->ny;
@@ -563,6 +565,7 @@ int skyr_surrogate_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmos
     if (int e = ensure_status(ctx)) return e;
     P.status = ctx->d_status;
     RenderConsts R;
+    R.copy_wait_cycles = ctx->limits.copy_wait_cycles;
     R.steps = sp->steps;
     R.use_network = sp->use_network ? 1 : 0;
     R.network_error = sp->network_error;

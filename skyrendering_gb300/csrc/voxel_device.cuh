@@ -13,10 +13,10 @@
 
 namespace skyr {
 
-// Upper bound on the samples of one free-flight / ratio-tracking walk.  A valid
-// scene needs ~sigma_max x chord samples (tens to hundreds); the cap only
-// stops pathological inputs, ends the path and raises the status flag.
-constexpr int kMaxTrackingSteps = 1 << 20;
+// The samples of one free-flight / ratio-tracking walk are bounded by
+// PtConsts::tracking_steps (skyr_device_limits, default 2^20).  A valid scene
+// needs ~sigma_max x chord samples (tens to hundreds); the bound only stops
+// pathological inputs, ends the path and raises the status flag.
 
 struct PtConsts {
     float3 box_min, box_max;
@@ -44,7 +44,8 @@ struct PtConsts {
     // point_out[i] (rgb)
     const float* points;
     float* point_out;
-    int* status;  // bit 0: a tracking walk hit kMaxTrackingSteps
+    int* status;         // bit 0: a tracking walk hit tracking_steps
+    int tracking_steps;  // bound on the samples of one walk
 };
 
 __device__ __forceinline__ void flag_overrun(const PtConsts& P) {

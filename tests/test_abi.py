@@ -84,3 +84,34 @@ def test_product_package_never_imports_the_oracle():
     pkg = ROOT / "skyrendering_gb300"
     for f in pkg.rglob("*.py"):
         assert "oracle" not in re.findall(r"^\s*(?:from|import)\s+(\w+)", f.read_text(), flags=re.M), f
+
+
+def test_device_limits_defaults():
+    d = _abi.DeviceLimits()
+    _abi.call("skyr_device_limits_default", C.byref(d))
+    assert d.tracking_steps == 1 << 20 and d.reserved == 0 and d.copy_wait_cycles == 1 << 31
+    assert _abi.lib().skyr_ctx_set_limits(None, C.byref(d)) == _abi.SKYR_EINVAL
+
+
+def _fields_equal(a, b):
+    from skyrendering_gb300.config import struct_dict
+
+    return struct_dict(a) == struct_dict(b)
+
+
+def test_loader_defaults_equal_library_defaults():
+    """The reference defaults the config loader restates (no CUDA library needed)
+    are the library's skyr_*_default, field for field."""
+    from skyrendering_gb300 import config as K
+
+    p = _abi.AtmosphereParameters()
+    _abi.call("skyr_atmosphere_parameters_default", C.byref(p))
+    assert _fields_equal(K.atmosphere_defaults(), p)
+    c = _abi.CloudParameters()
+    _abi.call("skyr_cloud_parameters_default", C.byref(c))
+    assert _fields_equal(K.cloud_defaults(), c)
+    for kind in (_abi.SKYR_MATERIAL_DEFAULT0, _abi.SKYR_MATERIAL_DEFAULT1, _abi.SKYR_MATERIAL_MINIMAL,
+                 _abi.SKYR_MATERIAL_VOXEL):
+        m = _abi.CloudMaterial()
+        _abi.call("skyr_cloud_material_default", kind, C.byref(m))
+        assert _fields_equal(K.material_defaults(kind), m), kind

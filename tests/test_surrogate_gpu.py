@@ -267,6 +267,30 @@ def test_fallback_replaces_flagged_pixels(ctx, small):
     torch.testing.assert_close(res.image[keep], base[keep])
 
 
+def test_copy_wait_bound_reports_timeout(ctx, small):
+    """With a copy-wait bound of 0 every block of the surrogate raymarch gives
+    up on the bulk copy of the network at once: it waits for the copy in
+    flight (bounded), leaves without writing a pixel, and the call is reported
+    as SKYR_ETIMEOUT; the default bound renders normally afterwards."""
+    sc, grid, fv = small
+    net = S.load_model(S.MODEL_PATH).packed(ctx)
+    sp = S.parameters(use_network=1)
+    default = ctx.limits
+    tight = _abi.DeviceLimits.from_buffer_copy(default)
+    tight.copy_wait_cycles = 0
+    out = torch.full((sc.view.height, sc.view.width, 4), float("nan"), device="cuda")
+    ctx.limits = tight
+    S.render(ctx, sc.atmo, sc.cloud, grid, sc.pt, sc.view, sc.sizes, sc.luts, fv, net, sp, out=out)
+    with pytest.raises(_abi.SkyrError) as exc:
+        ctx.check_status()
+    assert exc.value.status == _abi.SKYR_ETIMEOUT
+    assert bool(torch.isnan(out).all())
+    ctx.limits = default
+    S.render(ctx, sc.atmo, sc.cloud, grid, sc.pt, sc.view, sc.sizes, sc.luts, fv, net, sp, out=out)
+    ctx.check_status()
+    assert bool(torch.isfinite(out).all())
+
+
 def test_invalid_arguments(ctx, small):
     sc, grid, fv = small
     lib = _abi.lib()
