@@ -83,6 +83,17 @@ int skyr_mlp_trainer_set_learning_rate(skyr_mlp_trainer* tr, float learning_rate
  * caller device buffers, ordered on the trainer's stream. */
 int skyr_mlp_trainer_copy_params(const skyr_mlp_trainer* tr, float* out);
 int skyr_mlp_trainer_copy_packed(const skyr_mlp_trainer* tr, void* out);
+/* Checkpoint and resume of a training run.  save_state copies the FP32
+ * parameters and both Adam moment vectors (each FP32[SKYR_MLP_PARAMS], caller
+ * device buffers, ordered on the trainer's stream) and writes the step count
+ * to *steps (host).  load_state replaces the trainer's parameters, moments and
+ * step count with a saved state and repacks the network; the hyper-parameters
+ * (learning rate included) stay the trainer's.  Training is deterministic, so
+ * a run saved after k steps and resumed gives the same parameters, bit for
+ * bit, as the run that went on. */
+int skyr_mlp_trainer_save_state(const skyr_mlp_trainer* tr, float* params, float* m, float* v, int* steps);
+int skyr_mlp_trainer_load_state(skyr_mlp_trainer* tr, const float* params, const float* m, const float* v,
+                                int steps);
 
 #ifdef __cplusplus
 }

@@ -492,8 +492,12 @@ int skyr_mlp_infer(skyr_ctx* ctx, const void* packed, const uint16_t* x, int n, 
         return set_error(SKYR_EINVAL, "records and packed network must be 16-byte aligned");
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     if (int e = mlp::ensure_grad_attr()) return e;
+    int sms = 0;
+    if (int e = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device),
+                           "multiprocessor count"))
+        return e;
     int tiles = (n + 31) / 32;
-    int blocks = std::min((tiles + mlp::kWarps - 1) / mlp::kWarps, 152 * 8);
+    int blocks = std::min((tiles + mlp::kWarps - 1) / mlp::kWarps, sms * 8);
     mlp::mlp_infer_kernel<<<blocks, 32 * mlp::kWarps, mlp::kSmInfer, ctx->stream>>>(
         reinterpret_cast<const unsigned char*>(packed), reinterpret_cast<const uint4*>(x), n, y);
     return check_cuda(cudaGetLastError(), "mlp inference kernel");
@@ -604,6 +608,39 @@ int skyr_mlp_trainer_copy_packed(const skyr_mlp_trainer* tr, void* out) {
     if (int e = check_cuda(cudaSetDevice(tr->ctx->device), "cudaSetDevice")) return e;
     return check_cuda(cudaMemcpyAsync(out, tr->packed, mlp::kPackedBytes, cudaMemcpyDeviceToDevice, tr->ctx->stream),
                       "copy packed network");
+}
+
+int skyr_mlp_trainer_save_state(const skyr_mlp_trainer* tr, float* params, float* m, float* v, int* steps) {
+    if (!tr || !params || !m || !v || !steps) return set_error(SKYR_EINVAL, "null argument");
+    if (int e = check_cuda(cudaSetDevice(tr->ctx->device), "cudaSetDevice")) return e;
+    const size_t pb = SKYR_MLP_PARAMS * sizeof(float);
+    cudaStream_t st = tr->ctx->stream;
+    if (int e = check_cuda(cudaMemcpyAsync(params, tr->params, pb, cudaMemcpyDeviceToDevice, st), "save parameters"))
+        return e;
+    if (int e = check_cuda(cudaMemcpyAsync(m, tr->m, pb, cudaMemcpyDeviceToDevice, st), "save first moments"))
+        return e;
+    if (int e = check_cuda(cudaMemcpyAsync(v, tr->v, pb, cudaMemcpyDeviceToDevice, st), "save second moments"))
+        return e;
+    *steps = tr->steps;
+    return SKYR_OK;
+}
+
+int skyr_mlp_trainer_load_state(skyr_mlp_trainer* tr, const float* params, const float* m, const float* v,
+                                int steps) {
+    if (!tr || !params || !m || !v) return set_error(SKYR_EINVAL, "null argument");
+    if (steps < 0) return set_error(SKYR_EINVAL, "negative step count");
+    if (int e = check_cuda(cudaSetDevice(tr->ctx->device), "cudaSetDevice")) return e;
+    const size_t pb = SKYR_MLP_PARAMS * sizeof(float);
+    cudaStream_t st = tr->ctx->stream;
+    if (int e = check_cuda(cudaMemcpyAsync(tr->params, params, pb, cudaMemcpyDeviceToDevice, st), "load parameters"))
+        return e;
+    if (int e = check_cuda(cudaMemcpyAsync(tr->m, m, pb, cudaMemcpyDeviceToDevice, st), "load first moments"))
+        return e;
+    if (int e = check_cuda(cudaMemcpyAsync(tr->v, v, pb, cudaMemcpyDeviceToDevice, st), "load second moments"))
+        return e;
+    if (int e = skyr_mlp_pack(tr->ctx, tr->params, tr->h.label_scale, tr->packed)) return e;
+    tr->steps = steps;
+    return SKYR_OK;
 }
 
 }  // extern "C"

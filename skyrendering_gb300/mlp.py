@@ -120,6 +120,22 @@ class Trainer:
         _abi.call("skyr_mlp_trainer_copy_packed", self._tr, _ptr(m.buf))
         return m
 
+    def state(self) -> dict:
+        """Checkpoint: parameters, Adam moments (device FP32[PARAMS] each) and the step count."""
+        out = {k: torch.empty(PARAMS, dtype=torch.float32, device="cuda") for k in ("params", "m", "v")}
+        steps = C.c_int()
+        _abi.call("skyr_mlp_trainer_save_state", self._tr, _ptr(out["params"]), _ptr(out["m"]), _ptr(out["v"]),
+                  C.byref(steps))
+        out["steps"] = steps.value
+        return out
+
+    def load_state(self, state: dict) -> None:
+        """Resume from a checkpoint of state() (tensors on the device or host)."""
+        dev = {k: state[k].to("cuda", torch.float32).contiguous() for k in ("params", "m", "v")}
+        _abi.call("skyr_mlp_trainer_load_state", self._tr, _ptr(dev["params"]), _ptr(dev["m"]), _ptr(dev["v"]),
+                  int(state["steps"]))
+        self.ctx.synchronize()  # the sources may go away
+
     def close(self):
         if self._tr:
             _abi.call("skyr_mlp_trainer_destroy", self._tr)

@@ -101,6 +101,41 @@ def test_gradient_is_deterministic(ctx):
     assert torch.equal(g1, g2) and torch.equal(l1, l2)
 
 
+def test_trainer_checkpoint_resumes_bit_for_bit(ctx):
+    """Save after k steps, go on for j more; a new trainer loaded from the save
+    and stepped j times holds the same parameters, moments and step count, bit
+    for bit (training is deterministic)."""
+    p = _params(45)
+    batches = []
+    for i in range(6):
+        rec, _, t = _data(4096, 46 + i)
+        batches.append((rec, torch.from_numpy(t).cuda()))
+    h = mlp.hparams(learning_rate=2e-3)
+    a = mlp.Trainer(ctx, p, h)
+    for rec, tt in batches[:3]:
+        a.step(rec, tt)
+    saved = {k: (v.cpu() if torch.is_tensor(v) else v) for k, v in a.state().items()}
+    assert saved["steps"] == 3
+    for rec, tt in batches[3:]:
+        a.step(rec, tt)
+    b = mlp.Trainer(ctx, _params(99), h)  # other parameters: all of them come from the checkpoint
+    b.load_state(saved)
+    assert b.steps == 3
+    for rec, tt in batches[3:]:
+        b.step(rec, tt)
+    sa, sb = a.state(), b.state()
+    ctx.synchronize()
+    assert sa["steps"] == sb["steps"] == 6
+    for k in ("params", "m", "v"):
+        assert torch.equal(sa[k], sb[k]), k
+    # the packed networks agree too
+    na, nb = a.packed(), b.packed()
+    ctx.synchronize()
+    assert torch.equal(na.buf, nb.buf)
+    a.close()
+    b.close()
+
+
 def test_adam_step_matches_oracle(ctx):
     p = _params(41)
     rec, _, t = _data(2048, 42)
