@@ -88,9 +88,11 @@ class Camera:
 
 
 def atmosphere_defaults() -> _abi.AtmosphereParameters:
-    p = _abi.AtmosphereParameters()
-    _abi.call("skyr_atmosphere_parameters_default", C_ref(p))
-    return p
+    """The reference's AtmosphereParameters defaults (config.py restates them; equal to
+    skyr_atmosphere_parameters_default, checked on the CPU)."""
+    from .config import atmosphere_defaults as reference_defaults
+
+    return reference_defaults()
 
 
 def C_ref(x):
@@ -261,8 +263,9 @@ def frame_cloud_parameters() -> _abi.CloudParameters:
     """Cloud layer 1.5-4.0 km, 64 primary steps, 6 light-march steps,
     dual-lobe HG g = 0.8 / -0.3; the other fields are the reference defaults
     (src/SkyRendering/VolumetricCloud.h:20-35)."""
-    c = _abi.CloudParameters()
-    _abi.call("skyr_cloud_parameters_default", C_ref(c))
+    from .config import cloud_defaults
+
+    c = cloud_defaults()
     c.bottom_altitude, c.thickness = 1.5, 2.5
     c.max_raymarch_steps = 64.0
     c.shadow_steps = 6.0
@@ -272,9 +275,10 @@ def frame_cloud_parameters() -> _abi.CloudParameters:
 
 def frame_material(kind: int = None) -> _abi.CloudMaterial:
     """VolumetricCloudDefaultMaterial1 defaults with density 50/km (0.05/m)."""
+    from .config import material_defaults
+
     kind = _abi.SKYR_MATERIAL_DEFAULT1 if kind is None else kind
-    m = _abi.CloudMaterial()
-    _abi.call("skyr_cloud_material_default", kind, C_ref(m))
+    m = material_defaults(kind)
     if kind in (_abi.SKYR_MATERIAL_DEFAULT0, _abi.SKYR_MATERIAL_DEFAULT1):
         m.density = 50.0
     return m
