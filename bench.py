@@ -48,6 +48,16 @@ METRIC = "LUT-set regen µs; 1080p cloud frame ms; surrogate vs path-trace GPU t
 UNIT = "ms per 1920x1080 frame (LUT set + cloud raymarch)"
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 SUN_ZENITH = 45.0
+# FP32 operations of one density evaluation (SampleSigmaT of Material1 with its
+# sample position, VolumetricCloudDefaultMaterial1.glsl:14-29), counted from the
+# reference formulas with GL's bilinear filter written out (FMA = 2):
+#   sample position 6, CalHeight01 14, GetUVWLod of the cloud map 18, bilinear
+#   R 17, coverage / height terms 9                                   -> 64
+# Every evaluation runs these.  One that passes the coverage test also runs
+# GetUVWLod of the detail texture 18, trilinear R 33 and the detail terms 15
+# (66 more); the counted launch reports how many do (DETAIL_FLOPS).
+COVERAGE_FLOPS = 64
+DETAIL_FLOPS = 66
 
 
 def cloud_tile(tile_width: int, ray_lanes: int) -> str:
@@ -142,6 +152,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def reference_blue_noise():
+    """The reference's 64x64 blue-noise jitter tile (data/BlueNoise/64_64/HDR_L_0.png,
+    committed as tests/golden/blue_noise_64x64.npy) as its GL_R16 values / 65535."""
+    import numpy as np
+
+    raw = np.load(ROOT / "tests" / "golden" / "blue_noise_64x64.npy")
+    return (raw.astype(np.float64) / 65535.0).astype(np.float32)
+
+
 def ncu_capture(kernel: str) -> dict:
     """The committed ncu figures of one launch of `kernel` (profiles/dram_bytes_per_launch.json)."""
     f = ROOT / "profiles" / "dram_bytes_per_launch.json"
@@ -167,8 +186,7 @@ class FrameState:
 
         from skyrendering_gb300 import workloads as W
         from skyrendering_gb300.atmosphere import LutSet
-        from skyrendering_gb300.cloud import (NoiseTexture, VolumetricCloud, blue_noise_tile, prepare_textures,
-                                              textures_struct)
+        from skyrendering_gb300.cloud import NoiseTexture, VolumetricCloud, prepare_textures, textures_struct
 
         self.W = W
         self.ctx = ctx
@@ -181,7 +199,7 @@ class FrameState:
                     "detail": NoiseTexture(W.base_noise_desc()).generate(ctx)}
         self.material = W.frame_material()
         prepare_textures(ctx, self.material.type, self.tex)
-        self.bn_host = blue_noise_tile().pin_memory()
+        self.bn_host = torch.from_numpy(reference_blue_noise()).pin_memory()
         self.bn = self.bn_host.cuda()
         self.view = W.frame_view(self.cam, SUN_ZENITH)
         self.vc = VolumetricCloud(ctx, W.frame_cloud_parameters(), self.material, textures_struct(**self.tex))
@@ -291,7 +309,7 @@ def batched_frames(ctx, reps: int = 5, n_sets: int = 256, n_views: int = 64):
     from skyrendering_gb300 import batch as B
     from skyrendering_gb300 import workloads as W
     from skyrendering_gb300.atmosphere import LutSet
-    from skyrendering_gb300.cloud import NoiseTexture, blue_noise_tile, prepare_textures, textures_struct
+    from skyrendering_gb300.cloud import NoiseTexture, prepare_textures, textures_struct
 
     stream = ctx.stream
     params, renders, views, sov = W.batched_frame(n_sets, n_views)
@@ -301,7 +319,7 @@ def batched_frames(ctx, reps: int = 5, n_sets: int = 256, n_views: int = 64):
            "detail": NoiseTexture(W.base_noise_desc()).generate(ctx)}
     prepare_textures(ctx, material.type, tex)
     textures = textures_struct(**tex)
-    bn = blue_noise_tile().cuda()
+    bn = torch.from_numpy(reference_blue_noise()).cuda()
     luts = LutSet.allocate(sizes, n_sets)
     lut_best, lut_times = B.autotune_luts(ctx, params, renders, n_sets, sizes, luts, reps=3)
     k = next(i for i in range(n_views) if views[i].width == 1920) if any(
@@ -731,15 +749,16 @@ def run_skyr(args):
     if world > 1:
         ms = max_over_ranks(ms, "cuda")
 
-    # work counters of one frame (instrumented launch, outside the timing)
-    counters = torch.zeros(2, dtype=torch.int64, device="cuda")
+    # work counters of one frame (instrumented launch, outside the timing):
+    # raymarch samples, density evaluations, evaluations past the coverage test
+    counters = torch.zeros(3, dtype=torch.int64, device="cuda")
     L = fs.luts
     _abi.call("skyr_cloud_render_counted", ctx.handle, C.byref(fs.atmo), C.byref(fs.vc.params),
               C.byref(fs.vc.material), C.byref(fs.vc.textures), C.byref(fs.view), C.byref(fs.sizes),
               _ptr(L.transmittance), _ptr(L.aerial_perspective_luminance), _ptr(L.aerial_perspective_transmittance),
               _ptr(fs.bn), None, _ptr(fs.rgba), _ptr(fs.dist), _ptr(counters))
     torch.cuda.synchronize()
-    samples, evals = (int(x) for x in counters.cpu())
+    samples, evals, detail_evals = (int(x) for x in counters.cpu())
     # the frame the e2e steps left in host memory is the device frame, bit for bit
     e2e_matches = bool(torch.equal(host_rgba.view(torch.int16), fs.rgba.cpu().view(torch.int16)) and
                        torch.equal(host_dist.view(torch.int32), fs.dist.cpu().view(torch.int32)))
@@ -758,7 +777,10 @@ def run_skyr(args):
     cloud_mean = statistics.mean(cloud_ms)
     achieved = alg_bytes / (cloud_mean * 1e-3) / 1e9
     sm_mhz = clocks.get("sm_mhz") or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = sms * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s: FP32 lanes x FMA x sampled clock
+    flops = evals * COVERAGE_FLOPS + detail_evals * DETAIL_FLOPS
+    fp32_achieved = flops / (cloud_mean * 1e-3) / 1e12
     result = {
         "metric": METRIC,
         "value": ms,
@@ -785,8 +807,11 @@ def run_skyr(args):
                               "cloud_block_warps_x": cloud_tuned.cloud_block_warps_x,
                               "cloud_blocks_per_sm": cloud_tuned.cloud_blocks_per_sm,
                               "cloud_ray_lanes": cloud_tuned.cloud_ray_lanes}},
+        "lut_set_us": statistics.mean(lut_ms) * 1000.0,
+        "cloud_frame_ms": cloud_mean,
         "components": {"lut_set_us": statistics.mean(lut_ms) * 1000.0, "cloud_frame_ms": cloud_mean,
                        "raymarch_samples": samples, "density_evaluations": evals,
+                       "density_evaluations_past_coverage": detail_evals,
                        "density_evaluations_per_s": evals / (cloud_mean * 1e-3)},
         "e2e": {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": fs.bn_host.numel() * 4,
                 "d2h_bytes_per_step": host_rgba.numel() * 2 + host_dist.numel() * 4,
@@ -794,14 +819,19 @@ def run_skyr(args):
                         "raymarch stores the frame into mapped pinned host buffers while it runs",
                 "matches_device_frame": e2e_matches},
         "gpu_launches": kernels_per_step * args.steps,
-        "roofline": {"kernel": "cloud_render_kernel", "bound": "hbm", "achieved": achieved,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+        "roofline": {"kernel": "cloud_render_kernel", "bound": "fp32", "achieved": fp32_achieved,
+                     "peak": fp32_peak, "unit": "TFLOP/s", "frac": fp32_achieved / fp32_peak,
+                     "peak_kind": f"nominal: {sms} SMs (queried) x 128 FP32 lanes x 2 x median sampled SM clock",
                      "traffic": ncu_traffic("cloud_render_kernel"),
-                     "algorithmic_bytes_per_launch": alg_bytes,
-                     "note": "compulsory bytes; the raymarch is issue/FP32-bound on L1-resident textures"},
-        "roofline_fp32": {"kernel": "cloud_render_kernel", "peak_tflops_nominal": fp32_peak,
-                          "note": "152 SMs x 128 FP32 lanes x 2 x median SM clock; pipe use in profiles/"},
-        "roofline_issue": roofline_issue(cloud_mean, sm_mhz, cloud_tuned),
+                     "algorithmic_flops_per_launch": flops,
+                     "flops_per_evaluation": {"coverage": COVERAGE_FLOPS, "past_coverage": DETAIL_FLOPS},
+                     "note": "algorithmic FP32 FLOPs of the counted density evaluations of one frame (reference "
+                             "formulas, texture filters written out) over the launch's CUDA-event time"},
+        "roofline_hbm": {"kernel": "cloud_render_kernel", "bound": "hbm", "achieved": achieved,
+                         "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "note": "compulsory bytes; the textures are read from L1 / L2, so HBM is not the bound"},
+        "roofline_issue": roofline_issue(cloud_mean, sm_mhz, cloud_tuned, sms),
         "clocks": clocks,
         "wall_s": wall,
     }
@@ -846,9 +876,7 @@ def cpu_frame_ms(sample_s: float, threads: int):
         _HOST_TEXTURES["detail"] = (W.base_noise_desc(), orc.noise_generate(W.base_noise_desc(), 32, threads))
     host = dict(_HOST_TEXTURES)
     view = W.frame_view(cam, SUN_ZENITH)
-    from skyrendering_gb300.cloud import blue_noise_tile
-
-    bn = blue_noise_tile().numpy()
+    bn = reference_blue_noise()
     npx = view.width * view.height
     args = (W.frame_cloud_parameters(), W.frame_material(), host, view, sizes, luts["transmittance"],
             luts["aerial_perspective_luminance"], luts["aerial_perspective_transmittance"], bn)
@@ -866,11 +894,12 @@ def cpu_frame_ms(sample_s: float, threads: int):
     return (lut_s + cloud_s) * 1000.0, done, lut_s * 1e3
 
 
-def roofline_issue(cloud_ms: float, sm_mhz: float, tuned) -> dict:
-    """The raymarch against its real bound, instruction issue: the warp
-    instructions of one launch (ncu capture of the same frame and launch shape,
+def roofline_issue(cloud_ms: float, sm_mhz: float, tuned, sms: int) -> dict:
+    """The raymarch against instruction issue: the warp instructions of one
+    launch (ncu capture of the same frame and launch shape,
     profiles/dram_bytes_per_launch.json) over the launch's CUDA-event time,
-    against 152 SMs x 4 schedulers x one issue per cycle at the sampled clock."""
+    against the SMs (queried) x 4 schedulers x one issue per cycle at the
+    sampled clock."""
     cap = ncu_capture("cloud_render_kernel")
     shape = {"cloud_tile": cloud_tile(tuned.cloud_tile_width, tuned.cloud_ray_lanes),
              "cloud_block_warps_x": tuned.cloud_block_warps_x, "cloud_blocks_per_sm": tuned.cloud_blocks_per_sm,
@@ -879,11 +908,11 @@ def roofline_issue(cloud_ms: float, sm_mhz: float, tuned) -> dict:
     if not inst:
         return {"kernel": "cloud_render_kernel", "achieved": None, "note": "no committed ncu instruction count"}
     achieved = inst / (cloud_ms * 1e-3) / 1e9
-    peak = 152 * 4 * sm_mhz * 1e6 / 1e9
+    peak = sms * 4 * sm_mhz * 1e6 / 1e9
     return {"kernel": "cloud_render_kernel", "bound": "issue", "achieved": achieved, "peak": peak,
             "unit": "G warp-instructions/s", "frac": achieved / peak, "warp_instructions_per_launch": inst,
             "capture_shape": cap.get("tuning"), "timed_shape": shape, "same_shape": cap.get("tuning") == shape,
-            "note": "peak = 152 SMs x 4 schedulers x 1 instruction/cycle x median SM clock"}
+            "note": f"peak = {sms} SMs x 4 schedulers x 1 instruction/cycle x median SM clock"}
 
 
 def cpu_baseline(sample_s: float):

@@ -219,9 +219,11 @@ int skyr_cloud_render_to_host(skyr_ctx* ctx, const skyr_atmosphere_parameters* a
                               const float* depth, void* host_rgba, float* host_distance);
 
 /* skyr_cloud_render that also accumulates work counters into device memory
- * `counters` (2 x uint64, not cleared): [0] raymarch samples taken,
- * [1] SampleSigmaT evaluations (raymarch + light march).  Same outputs as
- * skyr_cloud_render; the counting costs one atomic per warp and sample kind.
+ * `counters` (3 x uint64, not cleared): [0] raymarch samples taken,
+ * [1] SampleSigmaT evaluations (raymarch + light march), [2] those of them
+ * that sampled the detail texture (Material1: past the coverage test;
+ * Material0: all).  Same outputs as skyr_cloud_render, bit for bit; the
+ * instrumented kernel runs one lane per ray whatever the tuning says.
  * (No reference counterpart: instrumentation.) */
 int skyr_cloud_render_counted(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
                               const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
@@ -233,8 +235,9 @@ int skyr_cloud_render_counted(skyr_ctx* ctx, const skyr_atmosphere_parameters* a
                               unsigned long long* counters);
 
 /* Seeded 64x64 blue-noise tile (void-and-cluster ranks, value = (rank+0.5)/4096)
- * written to host memory `out` (4096 floats).  Stands in for
- * data/BlueNoise/64_64/HDR_L_0.png of the reference. */
+ * written to host memory `out` (4096 floats), for callers without the
+ * reference's data/BlueNoise/64_64/HDR_L_0.png (which the caller may upload
+ * instead: GL_R16 values / 65535, row y of the file = texel row y). */
 int skyr_blue_noise_generate(uint32_t seed, float* out);
 
 #ifdef __cplusplus

@@ -317,6 +317,15 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
     const int occ = ctx->tuning.cloud_blocks_per_sm;
     auto* out = reinterpret_cast<__half2*>(out_rgba);
     const int tlw = sizes->transmittance_width, tlh = sizes->transmittance_height;
+    if (counters) {  // the instrumented launch: one lane per ray (the frame does not depend on it)
+        const int tw1 = std::min(tile_w, 32);
+        dim3 grid1((C.width + tw1 * warps_x - 1) / (tw1 * warps_x),
+                   (C.height + (32 / tw1) * (4 / warps_x) - 1) / ((32 / tw1) * (4 / warps_x)));
+        launch_cloud_render_counted(half, grid1, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
+                                    aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,
+                                    tile_w, warps_x);
+        return check_cuda(cudaGetLastError(), "cloud raymarch kernel (counted)");
+    }
     if (G == 8)
         launch_cloud_render<8>(half, occ, grid, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
                                aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,

@@ -31,8 +31,9 @@ __device__ __forceinline__ float one_minus_exp(float x, float& e) {
 // accumulates in FP32 exactly as the reference's `t += inv_shadow_steps`.
 // Sample heights come from rho2(d) = rho2_p + d (2 q + d) with
 // q = sun . (p + R z^), exact relative to the primary sample.
+template <bool COUNT = false>
 __device__ __forceinline__ float sample_shadow(const CloudConsts& C, const MaterialConsts& M, float3 pos,
-                                               float rho2_p) {
+                                               float rho2_p, unsigned* n_detail = nullptr) {
     float od = 0.f;
     float inv = 1.f / C.shadow_steps;
     float3 sv = C.sun * C.shadow_distance;
@@ -46,7 +47,7 @@ __device__ __forceinline__ float sample_shadow(const CloudConsts& C, const Mater
         float d = C.shadow_distance * f;
         float h = height01_rho2(C, fmaf(d, q2 + d, rho2_p));
         float3 dc = sp - C.cam;
-        od += sigma_t(C, M, sp, h, sqrtf(dot3(dc, dc))) * C.shadow_distance * dt;
+        od += sigma_t<COUNT>(C, M, sp, h, sqrtf(dot3(dc, dc)), n_detail) * C.shadow_distance * dt;
         prev = cur;
     }
     return __expf(-od);
@@ -62,13 +63,16 @@ __device__ __forceinline__ unsigned shadow_sample_count(float steps) {
 
 struct March {
     float trans, trans_sum, wsum, sun, env;
-    unsigned samples, evals;  // work counters (instrumented launches only)
+    // work counters of instrumented launches (COUNT): raymarch samples, density
+    // evaluations, evaluations that sampled the detail texture
+    unsigned samples, evals, detail;
 };
 
 // One shell segment [t0, t1] of the raymarch loop (VolumetricCloudRender.comp:160-187).
 // Sample heights are taken relative to the segment entry, whose
 // rho2_e = R_e^2 - R^2 is exact: rho2(t0 + e) = rho2_e + e (k_e + e) with
-// k_e = 2 (r mu + t0) = 2 R_e mu_e.
+// k_e = 2 (r mu + t0) = 2 R_e mu_e.  COUNT: fill S's work counters.
+template <bool COUNT>
 __device__ __forceinline__ void march_segment(const CloudConsts& C, const MaterialConsts& M, float3 view,
                                               float t0, float t1, float rho2_e, float k_e, float jitter,
                                               float ph_back, float ph_fwd, March& S) {
@@ -77,20 +81,23 @@ __device__ __forceinline__ void march_segment(const CloudConsts& C, const Materi
     float step = dist / (float)n;
     float e = step * jitter;
     float t = t0 + e;
-    const unsigned light_samples = shadow_sample_count(C.shadow_steps);  // work counter only
+    unsigned light_samples = 0;
+    if constexpr (COUNT) light_samples = shadow_sample_count(C.shadow_steps);
     for (unsigned k = n; k != 0; --k, t += step, e += step) {
         float3 pos = C.cam + view * t;
         float rho2 = fmaf(e, k_e + e, rho2_e);
         float h = height01_rho2(C, rho2);
         // RayMarchStep (VolumetricCloudRender.comp:116-137)
-        float sigma = sigma_t(C, M, pos, h, t);
-        S.samples++;
-        S.evals++;
+        float sigma = sigma_t<COUNT>(C, M, pos, h, t, &S.detail);
+        if constexpr (COUNT) {
+            S.samples++;
+            S.evals++;
+        }
         if (sigma >= 1e-5f) {
-            S.evals += light_samples;
+            if constexpr (COUNT) S.evals += light_samples;
             float tr;
             float one_m_tr = one_minus_exp(step * sigma, tr);
-            float tsun = sample_shadow(C, M, pos, rho2);
+            float tsun = sample_shadow<COUNT>(C, M, pos, rho2, &S.detail);
             float w = __expf(-C.sun_ms_sigma_scale * sigma);
             float phase = ph_back * (1.f - w) + ph_fwd * w;
             float e_dummy;
@@ -111,7 +118,8 @@ __device__ __forceinline__ void march_segment(const CloudConsts& C, const Materi
 // march, phase and extinction terms, which do not depend on the running
 // state), then every lane of the group folds the round's G steps into the
 // running state in step order with the same FP32 operations as march_segment,
-// stopping where it stops (T < 0.01).  The step positions are the same
+// stopping where it stops (T < 0.01).  It keeps no work counters: instrumented
+// launches use one lane per ray.  The step positions are the same
 // repeated FP32 sums `t += step`, so the result equals march_segment's; the
 // group only shortens the chain of dependent texture reads per ray, which
 // bounds launches with few rays per SM (the quarter-resolution pass).
@@ -125,7 +133,6 @@ __device__ __forceinline__ void march_segment_lanes(const CloudConsts& C, const 
     float step = dist / (float)n;
     float e = step * jitter;
     float t = t0 + e;
-    const unsigned light_samples = shadow_sample_count(C.shadow_steps);
     for (unsigned k0 = 0; k0 < n; k0 += G) {
         float tk = t, ek = e;
 #pragma unroll
@@ -159,10 +166,7 @@ __device__ __forceinline__ void march_segment_lanes(const CloudConsts& C, const 
             float omtj = __shfl_sync(gmask, omt, j, G), envj = __shfl_sync(gmask, env, j, G);
             float trj = __shfl_sync(gmask, tr, j, G), tj = __shfl_sync(gmask, tk, j, G);
             if (!stop && k0 + (unsigned)j < n) {
-                S.samples++;
-                S.evals++;
                 if (sj >= 1e-5f) {
-                    S.evals += light_samples;
                     S.sun += S.trans * tpj * omtj;
                     S.env += S.trans * envj * omtj;
                     S.trans_sum += S.trans;
@@ -225,11 +229,12 @@ __device__ __forceinline__ void shell_intersect(const CloudConsts& C, float mu, 
     }
 }
 
-// counters (optional): the frame's raymarch samples and density evaluations.
 // MINB: resident blocks per SM the register budget is cut for (a tuning
 // choice, skyr_tuning::cloud_blocks_per_sm).  G: lanes per ray
-// (skyr_tuning::cloud_ray_lanes); a warp then covers 32 / G rays.
-template <class S, int MINB, int G>
+// (skyr_tuning::cloud_ray_lanes); a warp then covers 32 / G rays.  COUNT (with
+// G = 1): the instrumented launch, which adds the frame's raymarch samples,
+// density evaluations and detail-texture evaluations to counters[0..2].
+template <class S, int MINB, int G, bool COUNT = false>
 __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
                                                            const float4* __restrict__ tlut, int tw, int th,
                                                            const S* __restrict__ ap_lum,
@@ -281,7 +286,7 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, 
     float noise = __ldg(blue_noise + (py & 63) * 64 + (px & 63));
     float j = noise + C.jitter_offset;
     float jitter = j - floorf(j);
-    March mk{1.f, 0.f, 0.f, 0.f, 0.f, 0u, 0u};
+    March mk{1.f, 0.f, 0.f, 0.f, 0.f, 0u, 0u, 0u};
     float rmu = (C.R + C.cam.z) * mu;
     // the (up to) two shell segments share one inlined copy of the march
 #pragma unroll 1
@@ -289,7 +294,8 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, 
         float t0 = sg ? it[2] : it[0], t1 = sg ? it[3] : it[1];
         if (sg && !(t1 - t0 > 0.f)) break;
         if constexpr (G == 1)
-            march_segment(C, M, view, t0, t1, sg ? ent[1] : ent[0], 2.f * (rmu + t0), jitter, ph_back, ph_fwd, mk);
+            march_segment<COUNT>(C, M, view, t0, t1, sg ? ent[1] : ent[0], 2.f * (rmu + t0), jitter, ph_back,
+                                 ph_fwd, mk);
         else
             march_segment_lanes<G>(C, M, view, t0, t1, sg ? ent[1] : ent[0], 2.f * (rmu + t0), jitter, ph_back,
                                    ph_fwd, mk, sub, gmask);
@@ -336,15 +342,18 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, 
         reinterpret_cast<uint2*>(out_rgba)[pix] = raw;
     }
     if (out_dist && sub == 0) out_dist[pix] = avg_t;
-    if (counters) {
-        unsigned long long a = sub == 0 ? mk.samples : 0u, b = sub == 0 ? mk.evals : 0u;
+    if constexpr (COUNT) {
+        static_assert(G == 1, "instrumented launches use one lane per ray");
+        unsigned long long a = mk.samples, b = mk.evals, c = mk.detail;
         for (int o = 16; o > 0; o >>= 1) {
             a += __shfl_xor_sync(__activemask(), a, o);
             b += __shfl_xor_sync(__activemask(), b, o);
+            c += __shfl_xor_sync(__activemask(), c, o);
         }
         if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) {
             atomicAdd(counters, a);
             atomicAdd(counters + 1, b);
+            atomicAdd(counters + 2, c);
         }
     }
 }
@@ -381,6 +390,14 @@ SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 1);
 SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 2);
 SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 4);
 SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 8);
+
+// The instrumented raymarch (one lane per ray, counters[0..2]); its own
+// translation unit (cloud_raymarch_counted.cu).
+void launch_cloud_render_counted(bool half, dim3 grid, cudaStream_t stream, const CloudConsts& C,
+                                 const MaterialConsts& M, const AtmoConsts& A, const float4* tlut, int tw, int th,
+                                 const void* ap_lum, const void* ap_trans, const float* blue_noise,
+                                 const float* depth, __half2* out_rgba, float* out_dist,
+                                 unsigned long long* counters, int tile_w, int warps_x);
 
 // The raymarch launch for G lanes per ray at the tuning's register cut.
 template <int G>

@@ -25,7 +25,11 @@ __device__ __forceinline__ float height01_rho2(const CloudConsts& C, float rho2)
     return clamp01((alt - C.bottom) * C.inv_layer);
 }
 
-__device__ __forceinline__ float sample_sigma_t(const MaterialConsts& M, float3 p, float h01, float dist_to_cam) {
+// COUNT: instrumented launches count the evaluations that sample the detail
+// texture (past Material1's coverage test) in *n_detail.
+template <bool COUNT = false>
+__device__ __forceinline__ float sample_sigma_t(const MaterialConsts& M, float3 p, float h01, float dist_to_cam,
+                                                unsigned* n_detail = nullptr) {
     switch (M.type) {
         case SKYR_MATERIAL_DEFAULT1: {
             // VolumetricCloudDefaultMaterial1.glsl:14-29
@@ -37,6 +41,7 @@ __device__ __forceinline__ float sample_sigma_t(const MaterialConsts& M, float3 
             float density = clamp01((cr - M.m1_threshold) * M.m1_edge_hardness);
             density *= clamp01((1.f - h01) * M.m1_height_hardness);
             if (density == 0.f) return 0.f;
+            if constexpr (COUNT) ++*n_detail;
             float du = fmaf(p.x, M.detail.frequency, M.detail.bias_x);
             float dv = fmaf(p.y, M.detail.frequency, M.detail.bias_y);
             float dw = p.z * M.detail.frequency;
@@ -94,11 +99,15 @@ static __device__ __noinline__ float sigma_t_voxel(const MaterialConsts& M, floa
     return dtex_sample(M.voxel_tex, 0, u, v, h01, lod, SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST) * M.density;
 }
 
+template <bool COUNT = false>
 __device__ __forceinline__ float sigma_t(const CloudConsts& C, const MaterialConsts& M, float3 p, float h01,
-                                         float dist_to_cam) {
+                                         float dist_to_cam, unsigned* n_detail = nullptr) {
     if (M.type == SKYR_MATERIAL_DEFAULT1 || M.type == SKYR_MATERIAL_MINIMAL)
-        return sample_sigma_t(M, p, h01, dist_to_cam);
-    if (M.type == SKYR_MATERIAL_DEFAULT0) return sigma_t_material0(C, M, p, h01, dist_to_cam);
+        return sample_sigma_t<COUNT>(M, p, h01, dist_to_cam, n_detail);
+    if (M.type == SKYR_MATERIAL_DEFAULT0) {
+        if constexpr (COUNT) ++*n_detail;  // Material0 samples the detail texture at every evaluation
+        return sigma_t_material0(C, M, p, h01, dist_to_cam);
+    }
     if (M.type == SKYR_MATERIAL_VOXEL) return sigma_t_voxel(M, p, h01, dist_to_cam);
     return 0.f;
 }

@@ -2,9 +2,11 @@
 called through the C ABI (libskyr.so).
 
 Tolerance: <= 1e-3 maximum relative error per LUT texel and channel
-(|gpu - oracle| / |oracle|, no absolute floor) for FP32 storage; FP16 storage
-adds its rounding (2^-11 relative), so FP16 outputs are held to 1.5e-3 in the
-FP16 normal range and to the FP16 subnormal spacing (2^-24) below it.
+(|gpu - oracle| / |oracle|, no absolute floor) for FP32 storage.  FP16 storage
+adds its rounding (at most 2^-11 = 4.9e-4 relative) to the FP32 error (at most
+1.4e-4 measured), so FP16 outputs are held to the same 1e-3 in the FP16 normal
+range, and to the FP16 subnormal spacing (2^-24) below it, where the storage
+can only hold multiples of that spacing.
 """
 import ctypes as C
 import math
@@ -20,7 +22,7 @@ from skyrendering_gb300.atmosphere import Atmosphere, AtmosphereRenderer, LutSet
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-3
-TOL_FP16 = 1.5e-3
+TOL_FP16 = 1e-3
 FP16_MIN_NORMAL = 2.0 ** -14
 FP16_SUBNORMAL_STEP = 2.0 ** -24
 NAMES = ("transmittance", "multiscattering", "sky_view_luminance", "sky_view_transmittance",
@@ -51,9 +53,10 @@ def test_plain_lut_set_matches_fp64_oracle(ctx, zenith):
     assert np.all(as_np(luts, "sky_view_luminance")[..., 3] == 0.0)
 
 
-def test_fp16_storage(ctx):
+@pytest.mark.parametrize("zenith", W.SUN_ZENITHS_DEG)
+def test_fp16_storage(ctx, zenith):
     p, s = W.earth_like_atmosphere(), W.plain_lut_sizes(_abi.SKYR_FORMAT_RGBA16F)
-    r = W.render_parameters(W.frame_camera(), 45.0)
+    r = W.render_parameters(W.frame_camera(), zenith)
     luts = update_lut_set(ctx, p, r, s)
     ctx.synchronize()
     assert luts.multiscattering.dtype.itemsize == 2
@@ -64,7 +67,9 @@ def test_fp16_storage(ctx):
         normal = np.abs(want) >= FP16_MIN_NORMAL
         # relative bound in the FP16 normal range; below it the storage can
         # only hold multiples of the subnormal spacing
-        assert (np.abs(got - want)[normal] / np.abs(want)[normal]).max() <= TOL_FP16, n
+        rel = (np.abs(got - want)[normal] / np.abs(want)[normal]).max()
+        print(f"fp16 zenith {zenith} {n}: max rel {rel:.2e} over {int(normal.sum())} normal values")
+        assert rel <= TOL_FP16, n
         assert np.abs(got - want)[~normal].max(initial=0.0) <= FP16_SUBNORMAL_STEP, n
 
 
