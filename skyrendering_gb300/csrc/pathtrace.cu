@@ -465,6 +465,245 @@ __global__ void __launch_bounds__(128, 6) pathtrace_kernel(CloudConsts C, Materi
 }
 
 // ---------------------------------------------------------------------------
+// The same estimator over the dense grid with brick majorants, as one flat
+// loop per lane.  The kernel above runs a path's walks as nested loops (a free
+// flight, then the ratio-tracking walk toward the sun at each event), so the
+// lanes of a warp spread over different loops and wait for one another.  Here
+// a lane's state says which walk it is in (free flight, or next-event ratio
+// tracking with a copy of the RNG state) and every iteration advances each
+// active lane's walk by one tentative collision: the brick steps up to it,
+// then one trilinear density fetch at one shared call site for both kinds of
+// walk.  Scattering, escape, the ground and path ends are handled where a walk
+// ends.  Every walk draws the same random numbers in the same order as the
+// nested form (the copied RNG state of next-event estimation is taken before
+// the path's own state samples the new direction, which next-event estimation
+// never reads), so the estimator and the oracle's RNG-matched paths are
+// unchanged.
+// ---------------------------------------------------------------------------
+enum : int { kIdle = 0, kFlight = 1, kSunWalk = 2 };
+
+struct FlatLane {
+    PathState ps;
+    Walk w;
+    float t, t_end, tau;
+    int it, mode;
+    // next-event estimation in flight: RNG copy, transmittance so far, and the
+    // contribution it scales, L += thr * (k * (ph * tr)); then go on (cont) or end
+    uint32_t nseed;
+    float tr, ph;
+    float3 thr, k;
+    bool cont;
+};
+
+// Begin the free flight of the next bounce from ps.o along ps.d; false when
+// the ray leaves the region at once (the path ends: Trace's loop exit).
+__device__ __forceinline__ bool begin_flight(const PtConsts& P, FlatLane& s) {
+    float t0, t1;
+    region(P, s.ps.o, s.ps.d, t0, t1);
+    if (t0 >= t1) return false;
+    s.t = t0;
+    s.t_end = t1;
+    walk_init(P, s.w, s.ps.o, s.ps.d, t0);
+    s.tau = sample_tau(P, s.ps.seed);
+    s.it = 0;
+    s.mode = kFlight;
+    return true;
+}
+
+// Begin next-event estimation from ps.o toward the sun with the RNG copy
+// s.nseed (TransmittanceEstimation, PathTracing.comp:135-151); a ray that
+// leaves the region at once has transmittance 1.
+__device__ __forceinline__ bool begin_sun_walk(const CloudConsts& C, const PtConsts& P, FlatLane& s) {
+    s.tr = 1.f;
+    float t0, t1;
+    region(P, s.ps.o, C.sun, t0, t1);
+    if (t0 >= t1) return false;
+    s.t = t0;
+    s.t_end = t1;
+    walk_init(P, s.w, s.ps.o, C.sun, t0);
+    s.tau = sample_tau(P, s.nseed);
+    s.it = 0;
+    s.mode = kSunWalk;
+    return true;
+}
+
+// The end of a next-event walk: its contribution, then the next bounce or the
+// end of the path.  Returns whether the path goes on.
+__device__ __forceinline__ bool finish_sun_walk(const PtConsts& P, FlatLane& s) {
+    s.ps.L += s.thr * (s.k * (s.ph * clamp01(s.tr)));
+    return s.cont && begin_flight(P, s);
+}
+
+// A free flight ended: a collision at s.t (scatter) or none (escape, the
+// environment and the ground).  Returns whether the path goes on.
+template <class S>
+__device__ __forceinline__ bool flight_event(const CloudConsts& C, const AtmoConsts& A, const PtConsts& P,
+                                             const ViewConsts& E, const float4* tlut, int tw, int th, const S* svl,
+                                             const S* svt, FlatLane& s, bool collided) {
+    PathState& ps = s.ps;
+    if (collided) {
+        if (!ps.scattered) {
+            float3 dc = C.cam - ps.o;
+            ps.scattered_t = sqrtf(dot3(dc, dc));
+        }
+        ps.scattered = true;
+        ps.o = ps.o + ps.d * s.t;
+        float cs = dot3(ps.d, C.sun);
+        s.ph = hg_pt(cs, P.g_back) * (1.f - P.ratio) + hg_pt(cs, P.g_fwd) * P.ratio;
+        s.k = sun_illuminance(C, A, tlut, tw, th, ps.o);
+        s.thr = ps.thr;
+        s.nseed = ps.seed;  // the copy next-event estimation draws from
+        sample_scatter(P, ps);
+        ++ps.istep;
+        s.cont = ps.istep < P.max_bounces && fmaxf(ps.thr.x, fmaxf(ps.thr.y, ps.thr.z)) > 0.f;
+        return begin_sun_walk(C, P, s) || finish_sun_walk(P, s);
+    }
+    if (P.env == SKYR_ENV_OFF || !ps.scattered) return false;
+    auto env = [&](float3 wd) { return environment(A, E, tlut, tw, th, svl, svt, P.sv_w, P.sv_h, wd); };
+    if (P.env == SKYR_ENV_CONST_ENVIRONMENT_MAP) {
+        ps.L += ps.thr * env(P.m_front * ps.d.x + P.m_right * ps.d.y + P.m_up * ps.d.z);
+        return false;
+    }
+    float3 o = ps.o, d = ps.d;
+    float rho2 = fmaf(o.x, o.x, fmaf(o.y, o.y, o.z * (o.z + 2.f * C.R)));
+    float r = sqrtf(fmaf(C.R, C.R, rho2));
+    float mu = fmaf(d.x, o.x, fmaf(d.y, o.y, d.z * (o.z + C.R))) / r;
+    if (!ray_hits_ground(r, rho2, mu)) {
+        ps.L += ps.thr * env(P.m_front * d.x + P.m_right * d.y + P.m_up * d.z);
+        return false;
+    }
+    o = o + d * dist_to_bottom(r, rho2, mu);
+    float3 n = f3(o.x, o.y, o.z + C.R);
+    n = n * rsqrtf(dot3(n, n));
+    float ndl = dot3(n, C.sun);
+    float3 bsdf = A.ground_albedo * (1.f / SKYR_PI);
+    s.k = sun_illuminance(C, A, tlut, tw, th, o) * (bsdf * ndl);
+    s.ph = 1.f;
+    s.thr = ps.thr;
+    s.nseed = ps.seed;
+    ps.o = o;
+    if (P.env == SKYR_ENV_GROUND_SINGLE_BOUNCE) {
+        s.cont = false;
+    } else {
+        // GenerateLambertSample (PathTracing.comp:119-129)
+        float st = sqrtf(rand01(P, ps.seed));
+        float ct = sqrtf(clamp01(1.f - st * st));
+        float3 b0, b1;
+        onb(n, b0, b1);
+        float sp, cp;
+        sincosf(2.f * SKYR_PI * rand01(P, ps.seed), &sp, &cp);
+        ps.d = b0 * (st * sp) + b1 * (st * cp) + n * ct;
+        ps.thr *= A.ground_albedo;
+        ++ps.istep;
+        s.cont = ps.istep < P.max_bounces && fmaxf(ps.thr.x, fmaxf(ps.thr.y, ps.thr.z)) > 0.f;
+    }
+    return begin_sun_walk(C, P, s) || finish_sun_walk(P, s);
+}
+
+template <class S>
+__global__ void __launch_bounds__(128, 6) pathtrace_flat_kernel(const __grid_constant__ CloudConsts C,
+                                                                const __grid_constant__ MaterialConsts M,
+                                                                const __grid_constant__ AtmoConsts A,
+                                                                const __grid_constant__ PtConsts P,
+                                                                const __grid_constant__ ViewConsts E,
+                                                                const float4* __restrict__ tlut, int tw, int th,
+                                                                const S* __restrict__ svl, const S* __restrict__ svt,
+                                                                const S* __restrict__ apl, const S* __restrict__ apt,
+                                                                unsigned frame_begin, int n_frames,
+                                                                int* __restrict__ counter, float4* __restrict__ acc,
+                                                                float4* __restrict__ acc_sq) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int n_total = P.n_items * n_frames;
+    int chunk_next = 0, chunk_end = 0;  // warp-uniform
+    bool exhausted = false;             // warp-uniform
+    FlatLane s;
+    s.mode = kIdle;
+    s.ps.px = s.ps.py = 0;
+    for (;;) {
+        // hand the warp's next items to idle lanes (as pathtrace_kernel)
+        unsigned idle = __ballot_sync(full, s.mode == kIdle);
+        while (idle && !exhausted) {
+            if (chunk_next >= chunk_end) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(counter, kWarpChunk);
+                base = __shfl_sync(full, base, 0);
+                if (base >= n_total) {
+                    exhausted = true;
+                    break;
+                }
+                chunk_next = base;
+                chunk_end = min(base + kWarpChunk, n_total);
+            }
+            int take = min(__popc(idle), chunk_end - chunk_next);
+            int rank = __popc(idle & ((1u << lane) - 1u));
+            if (s.mode == kIdle && rank < take) {
+                int item = chunk_next + rank;
+                int f = item / P.n_items;
+                bool live = false;
+                if (P.points) {
+                    live = start_point_path(P, frame_begin + (unsigned)f, item - f * P.n_items, s.ps) &&
+                           begin_flight(P, s);
+                    if (!live) deposit(C, A, P, apl, apt, s.ps, acc, acc_sq);
+                } else if (item_pixel(P, item - f * P.n_items, s.ps.px, s.ps.py)) {
+                    live = start_path(C, P, frame_begin + (unsigned)f, s.ps) && begin_flight(P, s);
+                    if (!live) deposit(C, A, P, apl, apt, s.ps, acc, acc_sq);
+                }
+                if (!live) s.mode = kIdle;
+            }
+            chunk_next += take;
+            idle = __ballot_sync(full, s.mode == kIdle);
+        }
+        if (!__any_sync(full, s.mode != kIdle)) break;
+        if (s.mode == kIdle) continue;
+        // one tentative collision of the lane's walk: brick steps up to it
+        const float3 d = s.mode == kFlight ? s.ps.d : C.sun;
+        bool ended = false, overrun = false;
+        float m;
+        for (;;) {
+            if (++s.it > P.tracking_steps) {
+                overrun = true;
+                break;
+            }
+            float te = fminf(walk_exit(s.w), s.t_end);
+            m = walk_majorant(P, s.w);
+            float seg = (te - s.t) * m;
+            if (s.tau < seg) break;
+            s.tau -= seg;
+            s.t = te;
+            if (!(s.t < s.t_end)) {
+                ended = true;
+                break;
+            }
+            walk_step(s.w);
+        }
+        bool collided = false;
+        if (overrun) {  // as the nested walks: a free flight counts as an escape, a sun walk keeps tr
+            flag_overrun(P);
+            ended = true;
+        } else if (!ended) {
+            // the density fetch both kinds of walk share
+            s.t += s.tau / m;
+            float sig = grid_sigma(P, s.ps.o + d * s.t);
+            if (s.mode == kFlight) {
+                if (rand01(P, s.ps.seed) < sig / m) collided = true;
+                else s.tau = sample_tau(P, s.ps.seed);
+            } else {
+                s.tr *= 1.f - fmaxf(0.f, sig / m);
+                s.tau = sample_tau(P, s.nseed);
+            }
+        }
+        if (!ended && !collided) continue;
+        bool live = s.mode == kFlight ? flight_event(C, A, P, E, tlut, tw, th, svl, svt, s, collided)
+                                      : finish_sun_walk(P, s);
+        if (!live) {
+            deposit(C, A, P, apl, apt, s.ps, acc, acc_sq);
+            s.mode = kIdle;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Synthetic grid and brick majorants
 // ---------------------------------------------------------------------------
 // voxels [first, end) of the grid (the host splits the grid into short launches)
@@ -747,7 +986,8 @@ int pathtrace_launch(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere
     float4* acc2 = reinterpret_cast<float4*>(accumulation_sq);
     auto launch = [&](auto tag) -> int {
         using S = decltype(tag);
-        auto kernel = pathtrace_kernel<S>;
+        // the flat form for the dense grid with brick majorants, the nested form otherwise
+        auto kernel = P.grid && P.use_bricks ? pathtrace_flat_kernel<S> : pathtrace_kernel<S>;
         int per_sm = 0, sms = 0;
         if (int e = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0), "occupancy"))
             return e;
