@@ -73,6 +73,15 @@ int skyr_mlp_trainer_destroy(skyr_mlp_trainer* tr);
 /* One Adam step on the batch x[n] / t[n] (device); adds the batch loss to
  * *loss_accum (device float) when not NULL. n <= 65536. */
 int skyr_mlp_train_step(skyr_mlp_trainer* tr, const uint16_t* x, const float* t, int n, float* loss_accum);
+/* The full batches of one epoch without a host round trip per step: for
+ * b = 0, batch, 2 batch, ... while b + batch <= n_idx, one Adam step on the
+ * samples idx[b .. b + batch) of x[n_all] / t[n_all] (device; idx device
+ * int32, e.g. a random permutation; the gradient kernel reads the records
+ * through it, so no gathered copy is made).  An index outside [0, n_all)
+ * counts as an empty sample.  Adds each step's loss to *loss_accum (device
+ * float) when not NULL. */
+int skyr_mlp_train_epoch(skyr_mlp_trainer* tr, const uint16_t* x, const float* t, int n_all, const int* idx,
+                         int n_idx, int batch, float* loss_accum);
 /* Current parameters (device FP32[SKYR_MLP_PARAMS]) and packed network. */
 const float* skyr_mlp_trainer_params(const skyr_mlp_trainer* tr);
 const void* skyr_mlp_trainer_packed(const skyr_mlp_trainer* tr);

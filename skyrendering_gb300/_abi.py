@@ -456,6 +456,7 @@ _SIGNATURES.update({
     "skyr_mlp_trainer_steps": (C.c_int, [P]),
     "skyr_mlp_trainer_copy_params": (C.c_int, [P, P]),
     "skyr_mlp_trainer_copy_packed": (C.c_int, [P, P]),
+    "skyr_mlp_train_epoch": (C.c_int, [P, P, P, C.c_int, P, C.c_int, C.c_int, P]),
     "skyr_mlp_trainer_save_state": (C.c_int, [P, P, P, P, C.POINTER(C.c_int)]),
     "skyr_mlp_trainer_load_state": (C.c_int, [P, P, P, P, C.c_int]),
     "skyr_mlp_trainer_set_learning_rate": (C.c_int, [P, C.c_float]),

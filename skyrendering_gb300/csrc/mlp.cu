@@ -1,15 +1,15 @@
-// mlp.cu — the surrogate network's kernels: packing, batched inference, the
-// tensor-core gradient of the relative-L2 loss and the Adam update.
+// mlp.cu — the surrogate network's training step and its C ABI: packing, the
+// fixed-order reduction of the per-tile gradients with the Adam update, and
+// the trainer (the tensor-core kernels of the gradient and of batched
+// inference are in mlp_tc.cu).
 //
 // Training step = two launches:
-//  1. mlp_grad_kernel: one block of 4 warps per 128 samples.  The forward pass
-//     stores every hidden activation (BF16) in shared memory; the backward pass
-//     forms dZ per layer (BF16, shared memory) and computes the block's weight
-//     gradient dW = dZ^T H as a 64x64x128 tensor-core product split over the
-//     warps (ldmatrix.trans supplies the transposed operands), and dX = dZ W
-//     with W read transposed.  Each block writes its partial gradient vector.
-//  2. mlp_adam_kernel: sums the block partials in a fixed order (deterministic),
-//     applies Adam to the FP32 master parameters and re-packs the BF16 weights.
+//  1. mlp_grad_tc_kernel: one 4-warp CTA per 128 samples computes the tile's
+//     loss and its partial gradient vector (forward and dZ W on tcgen05, dW on
+//     the warp-level tensor path);
+//  2. mlp_reduce_kernel: sums the tile partials in a fixed order
+//     (deterministic), applies Adam to the FP32 master parameters and re-packs
+//     the BF16 weights.
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -21,29 +21,11 @@ namespace skyr {
 namespace mlp {
 
 constexpr int kWarps = 4;
-constexpr int kTile = 32 * kWarps;  // samples per gradient block
+constexpr int kTile = 32 * kWarps;  // samples per gradient CTA (one tcgen05 M = 128 tile)
 constexpr int kMaxBatch = 65536;
 constexpr int kMaxBlocks = kMaxBatch / kTile;
 
-// shared memory of the gradient kernel
-constexpr int kSmX = kPackedBytes;                   // X0 [128][kXS] bf16
-constexpr int kSmH = kSmX + kTile * kXS * 2;         // H1..H4 [4][128][kSH] bf16
-constexpr int kSmD = kSmH + 4 * kTile * kSH * 2;     // D0, D1 [2][128][kSH] bf16 (dZ)
-constexpr int kBiasSlots = 4 * kW + 8;                        // bias gradients of one warp (f32)
-constexpr int kSmBias = kSmD + 2 * kTile * kSH * 2;           // [kWarps][kBiasSlots] f32
-constexpr int kSmLoss = kSmBias + kWarps * kBiasSlots * 4;    // [kWarps] f32
-constexpr int kSmGrad = kSmLoss + 16;                         // 166208 bytes
-
-// shared memory of the inference kernel: packed network + per warp a record
-// tile [32][kXS] bf16 and its outputs [32][4] f32
-constexpr int kSmInferWarp = 32 * kXS * 2 + 32 * 4 * 4;
-constexpr int kSmInfer = kPackedBytes + kWarps * kSmInferWarp;
-
-__device__ __forceinline__ float bias_at(const unsigned char* sw, int l, int j) {
-    return reinterpret_cast<const float*>(sw + kOffB)[l * kW + j];
-}
-
-// byte address of parameter i in the packed network (bf16 weight or f32 bias)
+// parameter i into the packed network (bf16 weight or f32 bias)
 __device__ __forceinline__ void pack_one(unsigned char* packed, int i, float val) {
     int l = 0;
 #pragma unroll 1
@@ -62,297 +44,6 @@ __global__ void __launch_bounds__(256) mlp_pack_kernel(const float* __restrict__
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < SKYR_MLP_PARAMS) pack_one(packed, i, params[i]);
     if (i == 0) *reinterpret_cast<float*>(packed + kOffScale) = out_scale;
-}
-
-__global__ void __launch_bounds__(128) mlp_infer_kernel(const unsigned char* __restrict__ packed,
-                                                        const uint4* __restrict__ x, int n,
-                                                        float* __restrict__ y) {
-    extern __shared__ __align__(16) unsigned char sm[];
-    load_packed(sm, packed);
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __nv_bfloat16* xt = reinterpret_cast<__nv_bfloat16*>(sm + kPackedBytes + warp * kSmInferWarp);
-    float* yt = reinterpret_cast<float*>(sm + kPackedBytes + warp * kSmInferWarp + 32 * kXS * 2);
-    int tiles = (n + 31) / 32;
-    for (int tile = blockIdx.x * kWarps + warp; tile < tiles; tile += gridDim.x * kWarps) {
-        int s = tile * 32 + lane;
-        // one record (6 x 16 B) per lane
-#pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            uint4 v = s < n ? __ldg(x + (size_t)s * 6 + q) : make_uint4(0, 0, 0, 0);
-            *reinterpret_cast<uint4*>(xt + lane * kXS + q * 8) = v;
-        }
-        __syncwarp();
-        forward_warp(sm, xt, yt);
-        __syncwarp();
-        if (s < n) {
-            y[(size_t)s * 3 + 0] = yt[lane * 4 + 0];
-            y[(size_t)s * 3 + 1] = yt[lane * 4 + 1];
-            y[(size_t)s * 3 + 2] = yt[lane * 4 + 2];
-        }
-        __syncwarp();
-    }
-}
-
-// Reduce a per-thread FP32 value over the 8 lanes sharing lane % 4.
-__device__ __forceinline__ float sum_over_rows(float v) {
-    v += __shfl_xor_sync(0xffffffffu, v, 4);
-    v += __shfl_xor_sync(0xffffffffu, v, 8);
-    v += __shfl_xor_sync(0xffffffffu, v, 16);
-    return v;
-}
-
-__global__ void __launch_bounds__(128) mlp_grad_kernel(const unsigned char* __restrict__ packed,
-                                                       const uint4* __restrict__ x, const float* __restrict__ tgt,
-                                                       int n, float inv_scale, float loss_eps, float inv_count,
-                                                       float* __restrict__ partial,
-                                                       float* __restrict__ loss_partial) {
-    extern __shared__ __align__(16) unsigned char sm[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int base = blockIdx.x * kTile;
-    __nv_bfloat16* X0 = reinterpret_cast<__nv_bfloat16*>(sm + kSmX);
-    __nv_bfloat16* H = reinterpret_cast<__nv_bfloat16*>(sm + kSmH);  // H[l] at H + l * kTile * kSH
-    __nv_bfloat16* D = reinterpret_cast<__nv_bfloat16*>(sm + kSmD);  // D[b] at D + b * kTile * kSH
-    // per-warp bias-gradient and loss slots, summed over the warps in a fixed
-    // order at the end (no float atomics: the gradient is deterministic)
-    float* sbias = reinterpret_cast<float*>(sm + kSmBias) + warp * kBiasSlots;
-    float* sloss = reinterpret_cast<float*>(sm + kSmLoss);
-    auto Hl = [&](int l) { return H + l * kTile * kSH; };
-    auto Db = [&](int b) { return D + b * kTile * kSH; };
-    auto W = [&](int l) { return reinterpret_cast<const __nv_bfloat16*>(sm + packed_w_offset(l)); };
-
-    load_packed(sm, packed);
-    for (int i = threadIdx.x; i < kTile * 6; i += blockDim.x) {
-        int r = i / 6, q = i % 6, s = base + r;
-        uint4 v = s < n ? __ldg(x + (size_t)s * 6 + q) : make_uint4(0, 0, 0, 0);
-        *reinterpret_cast<uint4*>(X0 + r * kXS + q * 8) = v;
-    }
-    for (int i = threadIdx.x; i < kWarps * kBiasSlots; i += blockDim.x)
-        reinterpret_cast<float*>(sm + kSmBias)[i] = 0.f;
-    if (threadIdx.x < kWarps) sloss[threadIdx.x] = 0.f;
-    __syncthreads();
-
-    const int row_w = warp * 32;
-    // ---- forward: hidden layers, activations to shared memory ----
-#pragma unroll 1
-    for (int l = 0; l < 4; ++l) {
-        const __nv_bfloat16* in = l == 0 ? X0 : Hl(l - 1);
-        const int in_stride = l == 0 ? kXS : kSH, kts = l == 0 ? 3 : 4;
-#pragma unroll 1
-        for (int mt = 0; mt < 2; ++mt) {
-            float acc[8][4];
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                float b0 = bias_at(sm, l, nt * 8 + 2 * t), b1 = bias_at(sm, l, nt * 8 + 2 * t + 1);
-                acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
-            }
-#pragma unroll 1
-            for (int kt = 0; kt < kts; ++kt) {
-                uint32_t a[4];
-                load_a(a, in, in_stride, row_w + mt * 16, kt * 16);
-#pragma unroll
-                for (int np = 0; np < 4; ++np) {
-                    uint32_t b[4];
-                    load_b_pair(b, W(l), packed_stride(l), np * 16, kt * 16);
-                    mma(acc[2 * np], a, b[0], b[1]);
-                    mma(acc[2 * np + 1], a, b[2], b[3]);
-                }
-            }
-            __nv_bfloat16* out = Hl(l);
-            int r = row_w + mt * 16 + g;
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                int c = nt * 8 + 2 * t;
-                *reinterpret_cast<uint32_t*>(out + r * kSH + c) =
-                    pack_bf16(fmaxf(acc[nt][0], 0.f), fmaxf(acc[nt][1], 0.f));
-                *reinterpret_cast<uint32_t*>(out + (r + 8) * kSH + c) =
-                    pack_bf16(fmaxf(acc[nt][2], 0.f), fmaxf(acc[nt][3], 0.f));
-            }
-        }
-        __syncwarp();
-    }
-    // ---- output layer, loss and dY ----
-    {
-        const __nv_bfloat16* w5 = W(4);
-        float db0 = 0.f, db1 = 0.f, loss = 0.f;
-#pragma unroll 1
-        for (int mt = 0; mt < 2; ++mt) {
-            float o[4];
-            o[0] = bias_at(sm, 4, 2 * t); o[1] = bias_at(sm, 4, 2 * t + 1); o[2] = o[0]; o[3] = o[1];
-#pragma unroll
-            for (int kp = 0; kp < 2; ++kp) {
-                uint32_t a0[4], a1[4], b[4];
-                load_a(a0, Hl(3), kSH, row_w + mt * 16, kp * 32);
-                load_a(a1, Hl(3), kSH, row_w + mt * 16, kp * 32 + 16);
-                ldsm_x4(b, smem_u32(w5 + (lane & 7) * kSH + kp * 32 + (lane >> 3) * 8));
-                mma(o, a0, b[0], b[1]);
-                mma(o, a1, b[2], b[3]);
-            }
-            float dy[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                int r = row_w + mt * 16 + g + (e >> 1) * 8, c = 2 * t + (e & 1), s = base + r;
-                dy[e] = 0.f;
-                if (c < kOut && s < n) {
-                    float d = o[e] - __ldg(tgt + (size_t)s * 3 + c) * inv_scale;
-                    float w = 1.f / (o[e] * o[e] + loss_eps);
-                    loss += d * d * w * inv_count;
-                    dy[e] = 2.f * d * w * inv_count;
-                }
-            }
-            db0 += dy[0] + dy[2];
-            db1 += dy[1] + dy[3];
-            int r = row_w + mt * 16 + g;
-            *reinterpret_cast<uint32_t*>(Db(0) + r * kSH + 2 * t) = pack_bf16(dy[0], dy[1]);
-            *reinterpret_cast<uint32_t*>(Db(0) + (r + 8) * kSH + 2 * t) = pack_bf16(dy[2], dy[3]);
-        }
-        db0 = sum_over_rows(db0);
-        db1 = sum_over_rows(db1);
-        if (g == 0 && t < 2) {
-            sbias[4 * kW + 2 * t] = db0;
-            sbias[4 * kW + 2 * t + 1] = db1;
-        }
-        for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
-        if (lane == 0) sloss[warp] = loss;
-    }
-    __syncthreads();
-
-    float* pg = partial + (size_t)blockIdx.x * SKYR_MLP_PARAMS;
-    // ---- backward ----
-#pragma unroll 1
-    for (int l = 4; l >= 0; --l) {
-        const __nv_bfloat16* dz = Db(l & 1);
-        const __nv_bfloat16* hin = l == 0 ? X0 : Hl(l - 1);
-        const int hin_stride = l == 0 ? kXS : kSH;
-        // (a) dW_l = dZ_l^T H_{l-1} over the block's 128 samples
-        if (l == 4) {
-            // rows = the 3 (of 8) outputs, warp w takes input columns 16w .. 16w + 15
-            float acc[2][4] = {};
-            const int n0 = warp * 16;
-#pragma unroll 1
-            for (int kt = 0; kt < 8; ++kt) {
-                uint32_t a[4], b[4];
-                ldsm_x4_t(a, smem_u32(dz + (kt * 16 + (lane & 7) + ((lane >> 4) << 3)) * kSH + ((lane >> 3) & 1) * 8));
-                a[1] = 0u;
-                a[3] = 0u;
-                ldsm_x4_t(b, smem_u32(hin + (kt * 16 + (lane & 7) + ((lane >> 3) & 1) * 8) * hin_stride + n0 +
-                                      (lane >> 4) * 8));
-                mma(acc[0], a, b[0], b[1]);
-                mma(acc[1], a, b[2], b[3]);
-            }
-            if (g < kOut) {
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    int c = n0 + h * 8 + 2 * t;
-                    pg[w_offset(4) + g * kW + c] = acc[h][0];
-                    pg[w_offset(4) + g * kW + c + 1] = acc[h][1];
-                }
-            }
-        } else {
-            // rows n_out 16w .. 16w + 15, all input columns
-            const int fi = fan_in(l), nps = l == 0 ? 3 : 4;
-            float acc[8][4] = {};
-#pragma unroll 1
-            for (int kt = 0; kt < 8; ++kt) {
-                uint32_t a[4];
-                ldsm_x4_t(a, smem_u32(dz + (kt * 16 + (lane & 7) + ((lane >> 4) << 3)) * kSH + warp * 16 +
-                                      ((lane >> 3) & 1) * 8));
-#pragma unroll
-                for (int np = 0; np < 4; ++np) {
-                    if (np < nps) {
-                        uint32_t b[4];
-                        ldsm_x4_t(b, smem_u32(hin + (kt * 16 + (lane & 7) + ((lane >> 3) & 1) * 8) * hin_stride +
-                                              np * 16 + (lane >> 4) * 8));
-                        mma(acc[2 * np], a, b[0], b[1]);
-                        mma(acc[2 * np + 1], a, b[2], b[3]);
-                    }
-                }
-            }
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                int c = nt * 8 + 2 * t, r = warp * 16 + g;
-                if (c < fi) {
-                    pg[w_offset(l) + r * fi + c] = acc[nt][0];
-                    pg[w_offset(l) + (r + 8) * fi + c] = acc[nt][2];
-                }
-                if (c + 1 < fi) {
-                    pg[w_offset(l) + r * fi + c + 1] = acc[nt][1];
-                    pg[w_offset(l) + (r + 8) * fi + c + 1] = acc[nt][3];
-                }
-            }
-        }
-        // (b) dZ_{l-1} = (dZ_l W_l) * (H_{l-1} > 0) for the warp's own rows
-        if (l > 0) {
-            const __nv_bfloat16* w = W(l);
-            const int ws = packed_stride(l);
-            __nv_bfloat16* dzo = Db((l - 1) & 1);
-            const __nv_bfloat16* hp = Hl(l - 1);
-            float db[8][2] = {};
-#pragma unroll 1
-            for (int mt = 0; mt < 2; ++mt) {
-                const int r0 = row_w + mt * 16;
-                float acc[8][4] = {};
-                if (l == 4) {
-                    uint32_t a[4];
-                    load_a(a, dz, kSH, r0, 0);
-                    a[2] = 0u;
-                    a[3] = 0u;
-#pragma unroll
-                    for (int np = 0; np < 4; ++np) {
-                        uint32_t b[4];
-                        ldsm_x4_t(b, smem_u32(w + (lane & 7) * ws + np * 16 + (lane >> 4) * 8));
-                        mma(acc[2 * np], a, b[0], 0u);
-                        mma(acc[2 * np + 1], a, b[2], 0u);
-                    }
-                } else {
-#pragma unroll 1
-                    for (int kt = 0; kt < 4; ++kt) {
-                        uint32_t a[4];
-                        load_a(a, dz, kSH, r0, kt * 16);
-#pragma unroll
-                        for (int np = 0; np < 4; ++np) {
-                            uint32_t b[4];
-                            ldsm_x4_t(b, smem_u32(w + (kt * 16 + (lane & 7) + ((lane >> 3) & 1) * 8) * ws +
-                                                  np * 16 + (lane >> 4) * 8));
-                            mma(acc[2 * np], a, b[0], b[1]);
-                            mma(acc[2 * np + 1], a, b[2], b[3]);
-                        }
-                    }
-                }
-#pragma unroll
-                for (int nt = 0; nt < 8; ++nt) {
-                    int c = nt * 8 + 2 * t;
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        int r = r0 + g + h * 8;
-                        __nv_bfloat162 hv = *reinterpret_cast<const __nv_bfloat162*>(hp + r * kSH + c);
-                        float z0 = __low2float(hv) > 0.f ? acc[nt][2 * h] : 0.f;
-                        float z1 = __high2float(hv) > 0.f ? acc[nt][2 * h + 1] : 0.f;
-                        db[nt][0] += z0;
-                        db[nt][1] += z1;
-                        *reinterpret_cast<uint32_t*>(dzo + r * kSH + c) = pack_bf16(z0, z1);
-                    }
-                }
-            }
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                float s0 = sum_over_rows(db[nt][0]), s1 = sum_over_rows(db[nt][1]);
-                if (g == 0) {
-                    sbias[(l - 1) * kW + nt * 8 + 2 * t] = s0;
-                    sbias[(l - 1) * kW + nt * 8 + 2 * t + 1] = s1;
-                }
-            }
-        }
-        __syncthreads();
-    }
-    const float* sb = reinterpret_cast<const float*>(sm + kSmBias);
-    for (int l = 0; l < kLayers; ++l)
-        for (int j = threadIdx.x; j < fan_out(l); j += blockDim.x) {
-            float v = 0.f;
-            for (int w = 0; w < kWarps; ++w) v += sb[w * kBiasSlots + l * kW + j];
-            pg[b_offset(l) + j] = v;
-        }
-    if (threadIdx.x == 0) loss_partial[blockIdx.x] = ((sloss[0] + sloss[1]) + sloss[2]) + sloss[3];
 }
 
 // grad[i] = sum over blocks of partial[b][i] (fixed order); optional Adam
@@ -385,21 +76,8 @@ __global__ void __launch_bounds__(256) mlp_reduce_kernel(const float* __restrict
     }
 }
 
-// The dynamic shared-memory opt-in of both kernels, once per device.
-int ensure_grad_attr() {
-    static bool done[64] = {};
-    int dev = 0;
-    if (int e = check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return e;
-    if (dev >= 0 && dev < 64 && done[dev]) return SKYR_OK;
-    if (int e = check_cuda(cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmGrad),
-                           "mlp gradient smem attribute"))
-        return e;
-    if (int e = check_cuda(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmInfer),
-                           "mlp inference smem attribute"))
-        return e;
-    if (dev >= 0 && dev < 64) done[dev] = true;
-    return SKYR_OK;
-}
+// Batched inference on the tensor cores (mlp_tc.cu).
+int launch_infer_tc(skyr_ctx* ctx, const void* packed, const uint16_t* x, int n, float* y);
 
 int validate_hparams(const skyr_mlp_hparams* h) {
     if (!h) return set_error(SKYR_EINVAL, "null hyper-parameters");
@@ -410,14 +88,15 @@ int validate_hparams(const skyr_mlp_hparams* h) {
     return SKYR_OK;
 }
 
+// The gradient of one training step on the tensor cores (mlp_tc.cu).
+int launch_grad_tc(skyr_ctx* ctx, const void* packed, const uint16_t* x, const float* t, const int* idx, int n_all,
+                   int n, float inv_scale, float loss_eps, float* partial, float* loss_partial);
+
+// The batch is x[idx[i]], t[idx[i]] for i < n (x[i], t[i] without idx).
 int launch_grad(skyr_ctx* ctx, const void* packed, const skyr_mlp_hparams* h, const uint16_t* x, const float* t,
-                int n, float* partial, float* loss_partial) {
-    if (int e = ensure_grad_attr()) return e;
-    int nblk = (n + kTile - 1) / kTile;
-    mlp_grad_kernel<<<nblk, kTile, kSmGrad, ctx->stream>>>(
-        reinterpret_cast<const unsigned char*>(packed), reinterpret_cast<const uint4*>(x), t, n, 1.f / h->label_scale,
-        h->loss_epsilon, 1.f / (3.f * (float)n), partial, loss_partial);
-    return check_cuda(cudaGetLastError(), "mlp gradient kernel");
+                const int* idx, int n_all, int n, float* partial, float* loss_partial) {
+    return launch_grad_tc(ctx, packed, x, t, idx, n_all, n, 1.f / h->label_scale, h->loss_epsilon, partial,
+                          loss_partial);
 }
 
 }  // namespace mlp
@@ -491,16 +170,7 @@ int skyr_mlp_infer(skyr_ctx* ctx, const void* packed, const uint16_t* x, int n, 
     if ((reinterpret_cast<uintptr_t>(x) & 15) || (reinterpret_cast<uintptr_t>(packed) & 15))
         return set_error(SKYR_EINVAL, "records and packed network must be 16-byte aligned");
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
-    if (int e = mlp::ensure_grad_attr()) return e;
-    int sms = 0;
-    if (int e = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device),
-                           "multiprocessor count"))
-        return e;
-    int tiles = (n + 31) / 32;
-    int blocks = std::min((tiles + mlp::kWarps - 1) / mlp::kWarps, sms * 8);
-    mlp::mlp_infer_kernel<<<blocks, 32 * mlp::kWarps, mlp::kSmInfer, ctx->stream>>>(
-        reinterpret_cast<const unsigned char*>(packed), reinterpret_cast<const uint4*>(x), n, y);
-    return check_cuda(cudaGetLastError(), "mlp inference kernel");
+    return mlp::launch_infer_tc(ctx, packed, x, n, y);
 }
 
 int skyr_mlp_gradient(skyr_ctx* ctx, const void* packed, const skyr_mlp_hparams* h, const uint16_t* x,
@@ -516,7 +186,7 @@ int skyr_mlp_gradient(skyr_ctx* ctx, const void* packed, const skyr_mlp_hparams*
     if (int e = ensure_pt_scratch(ctx, need)) return e;  // shared per-context scratch
     float* partial = reinterpret_cast<float*>(ctx->pt_scratch);
     float* lp = partial + (size_t)nblk * SKYR_MLP_PARAMS;
-    if (int e = mlp::launch_grad(ctx, packed, h, x, t, n, partial, lp)) return e;
+    if (int e = mlp::launch_grad(ctx, packed, h, x, t, nullptr, n, n, partial, lp)) return e;
     mlp::mlp_reduce_kernel<<<(SKYR_MLP_PARAMS + 255) / 256, 256, 0, ctx->stream>>>(
         partial, nblk, lp, grad, loss, 0, nullptr, nullptr, nullptr, 0.f, 0.f, 0.f, 0.f, 1.f, 1.f, nullptr);
     return check_cuda(cudaGetLastError(), "mlp reduce kernel");
@@ -566,13 +236,12 @@ int skyr_mlp_trainer_destroy(skyr_mlp_trainer* tr) {
     return SKYR_OK;
 }
 
-int skyr_mlp_train_step(skyr_mlp_trainer* tr, const uint16_t* x, const float* t, int n, float* loss_accum) {
-    if (!tr || !x || !t) return set_error(SKYR_EINVAL, "null argument");
-    if (n < 1 || n > mlp::kMaxBatch) return set_error(SKYR_EINVAL, "batch size must be in [1, 65536]");
-    if (reinterpret_cast<uintptr_t>(x) & 15) return set_error(SKYR_EINVAL, "records must be 16-byte aligned");
+namespace {
+int train_step(skyr_mlp_trainer* tr, const uint16_t* x, const float* t, const int* idx, int n_all, int n,
+               float* loss_accum) {
     skyr_ctx* ctx = tr->ctx;
-    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
-    if (int e = mlp::launch_grad(ctx, tr->packed, &tr->h, x, t, n, tr->partial, tr->loss_partial)) return e;
+    if (int e = mlp::launch_grad(ctx, tr->packed, &tr->h, x, t, idx, n_all, n, tr->partial, tr->loss_partial))
+        return e;
     int step = tr->steps + 1;
     double c1 = 1.0 - std::pow((double)tr->h.beta1, step), c2 = 1.0 - std::pow((double)tr->h.beta2, step);
     int nblk = (n + mlp::kTile - 1) / mlp::kTile;
@@ -583,7 +252,27 @@ int skyr_mlp_train_step(skyr_mlp_trainer* tr, const uint16_t* x, const float* t,
     tr->steps = step;
     return SKYR_OK;
 }
+}  // namespace
 
+int skyr_mlp_train_step(skyr_mlp_trainer* tr, const uint16_t* x, const float* t, int n, float* loss_accum) {
+    if (!tr || !x || !t) return set_error(SKYR_EINVAL, "null argument");
+    if (n < 1 || n > mlp::kMaxBatch) return set_error(SKYR_EINVAL, "batch size must be in [1, 65536]");
+    if (reinterpret_cast<uintptr_t>(x) & 15) return set_error(SKYR_EINVAL, "records must be 16-byte aligned");
+    if (int e = check_cuda(cudaSetDevice(tr->ctx->device), "cudaSetDevice")) return e;
+    return train_step(tr, x, t, nullptr, n, n, loss_accum);
+}
+
+int skyr_mlp_train_epoch(skyr_mlp_trainer* tr, const uint16_t* x, const float* t, int n_all, const int* idx,
+                         int n_idx, int batch, float* loss_accum) {
+    if (!tr || !x || !t || !idx) return set_error(SKYR_EINVAL, "null argument");
+    if (batch < 1 || batch > mlp::kMaxBatch) return set_error(SKYR_EINVAL, "batch size must be in [1, 65536]");
+    if (n_all < 1 || n_idx < 0) return set_error(SKYR_EINVAL, "bad sample counts");
+    if (reinterpret_cast<uintptr_t>(x) & 15) return set_error(SKYR_EINVAL, "records must be 16-byte aligned");
+    if (int e = check_cuda(cudaSetDevice(tr->ctx->device), "cudaSetDevice")) return e;
+    for (int b = 0; b + batch <= n_idx; b += batch)
+        if (int e = train_step(tr, x, t, idx + b, n_all, batch, loss_accum)) return e;
+    return SKYR_OK;
+}
 const float* skyr_mlp_trainer_params(const skyr_mlp_trainer* tr) { return tr ? tr->params : nullptr; }
 const void* skyr_mlp_trainer_packed(const skyr_mlp_trainer* tr) { return tr ? tr->packed : nullptr; }
 int skyr_mlp_trainer_steps(const skyr_mlp_trainer* tr) { return tr ? tr->steps : -1; }

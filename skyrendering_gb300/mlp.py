@@ -103,6 +103,16 @@ class Trainer:
         _check_records(rec)
         _abi.call("skyr_mlp_train_step", self._tr, _ptr(rec), _ptr(targets), rec.shape[0], _ptr(loss_accum))
 
+    def epoch(self, rec: torch.Tensor, targets: torch.Tensor, perm: torch.Tensor, batch: int,
+              loss_accum: torch.Tensor | None = None):
+        """The full batches of one epoch over the permutation `perm` (device int32 / int64
+        indices into rec / targets), gathered by the gradient kernel itself."""
+        _check_records(rec)
+        idx = perm.to(torch.int32).contiguous()
+        t = targets.contiguous().float()
+        _abi.call("skyr_mlp_train_epoch", self._tr, _ptr(rec), _ptr(t), rec.shape[0], _ptr(idx), idx.shape[0], batch,
+                  _ptr(loss_accum))
+
     def set_learning_rate(self, lr: float):
         _abi.call("skyr_mlp_trainer_set_learning_rate", self._tr, C.c_float(lr))
 

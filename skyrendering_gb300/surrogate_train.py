@@ -103,11 +103,8 @@ def train(ctx: Context, rec: torch.Tensor, lab: torch.Tensor, val_rec: torch.Ten
             tr.set_learning_rate(lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * ep / max(epochs, 1)))))
         perm = torch.randperm(n, device="cuda", generator=gen)
         loss.zero_()
-        steps = 0
-        for b in range(0, n - batch + 1, batch):
-            idx = perm[b:b + batch]
-            tr.step(rec[idx].contiguous(), lab[idx].contiguous(), loss)
-            steps += 1
+        steps = n // batch
+        tr.epoch(rec, lab, perm, batch, loss)  # the batches gathered inside the gradient kernel
         ve = validation_error(tr.packed(), val_rec, val_lab)
         curve.append((ep, float(loss.item()) / max(steps, 1), ve))
         log(f"epoch {ep}: train loss {curve[-1][1]:.5f}  validation rel L1 {ve:.4f}")

@@ -136,6 +136,38 @@ def test_trainer_checkpoint_resumes_bit_for_bit(ctx):
     b.close()
 
 
+def test_epoch_gathers_batches_in_the_kernel(ctx):
+    """skyr_mlp_train_epoch over a permutation equals one skyr_mlp_train_step per
+    gathered batch, bit for bit; indices outside the data count as empty samples."""
+    p = _params(51)
+    rec, _, t = _data(3 * 2048 + 100, 52)
+    tt = torch.from_numpy(t).cuda()
+    perm = torch.randperm(rec.shape[0], device="cuda", generator=torch.Generator(device="cuda").manual_seed(3))
+    h = mlp.hparams(learning_rate=2e-3)
+    a, b = mlp.Trainer(ctx, p, h), mlp.Trainer(ctx, p, h)
+    la, lb = torch.zeros(1, device="cuda"), torch.zeros(1, device="cuda")
+    a.epoch(rec, tt, perm, 2048, la)
+    for k in range(3):
+        idx = perm[k * 2048:(k + 1) * 2048]
+        b.step(rec[idx].contiguous(), tt[idx].contiguous(), lb)
+    sa, sb = a.state(), b.state()
+    ctx.synchronize()
+    assert sa["steps"] == sb["steps"] == 3
+    for k in ("params", "m", "v"):
+        assert torch.equal(sa[k], sb[k]), k
+    assert torch.equal(la, lb)
+    # out-of-range indices are empty samples: the gradient equals the one of the valid samples alone
+    c = mlp.Trainer(ctx, p, h)
+    bad = perm[:2048].clone()
+    bad[1000:] = -5
+    c.epoch(rec, tt, bad, 2048)
+    ctx.synchronize()
+    assert torch.isfinite(c.params()).all()
+    a.close()
+    b.close()
+    c.close()
+
+
 def test_adam_step_matches_oracle(ctx):
     p = _params(41)
     rec, _, t = _data(2048, 42)
