@@ -118,6 +118,56 @@ int fill_tex(DTex& t, const void* p, const skyr_noise_texture_desc& d, bool bord
 }
 }  // namespace
 
+// The constants of the specialised density evaluation (cloud_fast.cuh), and
+// whether it applies: Material1, NEAREST_MIPMAP_NEAREST minification on both
+// textures, REPEAT, expanded level 0 present, a square cloud map and a cubic
+// detail texture.
+static void derive_fast_consts(const skyr_cloud_material& m, const skyr_cloud_textures& tex, MaterialConsts& mc,
+                               double tan_half, double vmin) {
+    mc.fast_ok = 0;
+    const skyr_noise_texture_desc &cd = tex.cloud_map_desc, &dd = tex.detail_desc;
+    if (m.type != SKYR_MATERIAL_DEFAULT1 || m.minfilter2d != SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST ||
+        m.minfilter3d != SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST || !mc.cloud_map_tex.ex || !mc.detail_tex.ex ||
+        mc.cloud_map_tex.border || mc.detail_tex.border || cd.width != cd.height || cd.depth != 1 ||
+        dd.width != dd.height || dd.width != dd.depth || dd.depth < 2)
+        return;
+    auto fill = [&](FastTex& t, const DTex& d, const skyr_noise_texture_desc& desc, double repeat) {
+        t.base = d.base;
+        t.ex = d.ex;
+        t.w = desc.width;
+        t.h = desc.height;
+        t.d = desc.depth;
+        t.last = d.levels - 1;
+        t.fw = (float)desc.width;
+        t.fh = (float)desc.height;
+        t.fd = (float)desc.depth;
+        // CalKLod (VolumetricCloudDefaultMaterial.cpp:24-28) in double
+        double maxw = std::max(desc.width, std::max(desc.height, desc.depth));
+        double lod_k = std::log2(maxw * tan_half / (repeat * vmin)) + (double)m.lod_bias;
+        t.lod_k = (float)lod_k;
+        // lambda = 0.5 log2 d2 + lod_k <= 1/2  <=>  d2 <= 2^(1 - 2 lod_k)
+        t.mag_d2 = (float)std::exp2(1.0 - 2.0 * lod_k);
+        for (int l = 0; l < kMaxLevels; ++l)
+            t.off[l] = l < d.levels ? (unsigned)noise_level_offset(&desc, l) : 0u;
+    };
+    FastConsts& f = mc.fast;
+    fill(f.cm, mc.cloud_map_tex, cd, m.cloud_map_repeat_size);
+    fill(f.dt, mc.detail_tex, dd, m.detail_repeat_size);
+    // Material1's terms in 0..255 texel units (VolumetricCloudDefaultMaterial1.glsl:18-28)
+    const double e = m.base_edge_hardness, hh = m.base_height_hardness;
+    f.cov_a = (float)(e / 255.0);
+    f.cov_b = (float)(-(double)m.base_density_threshold * e);
+    f.hh_a = (float)-hh;
+    f.hh_b = (float)hh;
+    f.det_a = (float)((double)m.detail_scale / 255.0);
+    f.det_b = (float)((double)m.detail_base * m.detail_scale);
+    f.height_cut = mc.m1_height_cut;
+    f.ec_a = (float)(-1.0 / 255.0);
+    f.ec_b = m.edge_cut;
+    f.density = m.density;
+    mc.fast_ok = 1;
+}
+
 // VolumetricCloud::Update (VolumetricCloud.cpp:168-280), the material Update
 // (VolumetricCloudDefaultMaterial.cpp:84-101,451-463; VolumetricCloudVoxelMaterial.cpp:93-105)
 // and CalKLod (VolumetricCloudDefaultMaterial.cpp:24-28).
@@ -266,6 +316,7 @@ int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud
         return st;
     if (d0 && tex.displacement_desc.channels < 4) return set_error(SKYR_EINVAL, "displacement texture needs 4 channels");
     if ((d0 || d1) && tex.cloud_map_desc.channels < 2) return set_error(SKYR_EINVAL, "cloud map needs 2 channels");
+    derive_fast_consts(m, tex, mc, tan_half, vmin);
     return SKYR_OK;
 }
 

@@ -138,6 +138,29 @@ struct SampleInfoD {
     float bias_x, bias_y, frequency, k_lod;
 };
 
+// Constants of the specialised density evaluation (cloud_fast.cuh): Material1
+// with NEAREST_MIPMAP_NEAREST minification, REPEAT and expanded level 0.
+struct FastTex {
+    const uint8_t* base;  // channel 0 of level l at base + off[l]
+    const void* ex;       // expanded level 0 of channel 0 (uint32 per 2D texel, uint64 per 3D texel)
+    int w, h, d;          // level-0 size (powers of two; d = 1 for a 2D texture)
+    int last;             // index of the last mip level
+    float fw, fh, fd;     // level-0 size as floats
+    float mag_d2;         // GL magnifies (lambda <= 1/2) while |p - cam|^2 <= mag_d2
+    float lod_k;          // lambda = 0.5 log2 |p - cam|^2 + lod_k  (lod_k = log2 k_lod + lod_bias)
+    unsigned off[kMaxLevels];
+};
+
+struct FastConsts {
+    FastTex cm, dt;          // cloud map (2D, channel R), detail texture (3D, channel R)
+    float cov_a, cov_b;      // clamp01((cr - threshold) * edge_hardness) = sat(cr255 cov_a + cov_b)
+    float hh_a, hh_b;        // clamp01((1 - h) * height_hardness)         = sat(h hh_a + hh_b)
+    float det_a, det_b;      // (detail + detail_base) * detail_scale      = dt255 det_a + det_b
+    float height_cut;        // clamp01(h - height_cut)
+    float ec_a, ec_b;        // clamp01(edge_cut - cr)                     = sat(cr255 ec_a + ec_b)
+    float density;           // uDensity
+};
+
 // Material constants (the material's Update + VolumetricCloudDefaultMaterialCommon)
 struct MaterialConsts {
     int type;
@@ -149,6 +172,8 @@ struct MaterialConsts {
     float m0_detail_x, m0_detail_y, m0_disp_scale;
     float vx_freq_x, vx_freq_y, vx_bias_x, vx_bias_y, vx_k_lod;
     DTex cloud_map_tex, detail_tex, displacement_tex, voxel_tex;
+    int fast_ok;      // the configuration cloud_fast.cuh specialises (set by derive_cloud_consts)
+    FastConsts fast;  // its constants, when fast_ok
 };
 
 // Frame constants (VolumetricCloud::Update, VolumetricCloud.cpp:168-280)

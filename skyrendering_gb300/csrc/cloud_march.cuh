@@ -7,6 +7,7 @@
 #include <type_traits>
 
 #include "atmosphere_kernels.cuh"
+#include "cloud_fast.cuh"
 #include "cloud_internal.cuh"
 #include "cloud_material.cuh"
 #include "lut_access.cuh"
@@ -30,24 +31,31 @@ __device__ __forceinline__ float one_minus_exp(float x, float& e) {
 // SampleShadow (VolumetricCloudRender.comp:98-114).  The loop variable
 // accumulates in FP32 exactly as the reference's `t += inv_shadow_steps`.
 // Sample heights come from rho2(d) = rho2_p + d (2 q + d) with
-// q = sun . (p + R z^), exact relative to the primary sample.
-template <bool COUNT = false>
+// q = sun . (p + R z^), exact relative to the primary sample.  FAST: the
+// density of cloud_fast.cuh (MaterialConsts::fast_ok).
+template <bool FAST, bool COUNT = false>
 __device__ __forceinline__ float sample_shadow(const CloudConsts& C, const MaterialConsts& M, float3 pos,
                                                float rho2_p, unsigned* n_detail = nullptr) {
+    // Products whose results have several uses are rounded explicitly (_rn), so
+    // that no later pass may fuse them into a neighbouring add: every launch
+    // shape (register cut, lanes per ray) then gives the same bits.
     float od = 0.f;
     float inv = 1.f / C.shadow_steps;
     float3 sv = C.sun * C.shadow_distance;
     float q2 = 2.f * fmaf(C.sun.x, pos.x, fmaf(C.sun.y, pos.y, C.sun.z * (pos.z + C.R)));
     float prev = 0.f;
     for (float t = inv; t <= 1.f; t += inv) {
-        float cur = t * t;
-        float dt = cur - prev;
+        float cur = __fmul_rn(t, t);
+        float dt = __fsub_rn(cur, prev);
         float f = fmaf(0.5f, dt, prev);
-        float3 sp = pos + sv * f;
-        float d = C.shadow_distance * f;
-        float h = height01_rho2(C, fmaf(d, q2 + d, rho2_p));
+        float3 sp = make_float3(fmaf(sv.x, f, pos.x), fmaf(sv.y, f, pos.y), fmaf(sv.z, f, pos.z));
+        float d = __fmul_rn(C.shadow_distance, f);
+        float h = height01_rho2(C, fmaf(d, __fadd_rn(q2, d), rho2_p));
         float3 dc = sp - C.cam;
-        od += sigma_t<COUNT>(C, M, sp, h, sqrtf(dot3(dc, dc)), n_detail) * C.shadow_distance * dt;
+        float sigma;
+        if constexpr (FAST) sigma = fast_sigma_m1<COUNT>(M, sp, h, dot3(dc, dc), n_detail);
+        else sigma = sigma_t<COUNT>(C, M, sp, h, sqrtf(dot3(dc, dc)), n_detail);
+        od = fmaf(__fmul_rn(sigma, C.shadow_distance), dt, od);
         prev = cur;
     }
     return __expf(-od);
@@ -71,24 +79,27 @@ struct March {
 // One shell segment [t0, t1] of the raymarch loop (VolumetricCloudRender.comp:160-187).
 // Sample heights are taken relative to the segment entry, whose
 // rho2_e = R_e^2 - R^2 is exact: rho2(t0 + e) = rho2_e + e (k_e + e) with
-// k_e = 2 (r mu + t0) = 2 R_e mu_e.  COUNT: fill S's work counters.
-template <bool COUNT>
+// k_e = 2 (r mu + t0) = 2 R_e mu_e.  COUNT: fill S's work counters; FAST: the
+// density of cloud_fast.cuh.
+template <bool FAST, bool COUNT>
 __device__ __forceinline__ void march_segment(const CloudConsts& C, const MaterialConsts& M, float3 view,
                                               float t0, float t1, float rho2_e, float k_e, float jitter,
                                               float ph_back, float ph_fwd, March& S) {
     float dist = fminf(t1 - t0, C.max_raymarch_distance);
     unsigned n = (unsigned)fmaxf(C.max_raymarch_steps * (dist / C.max_raymarch_distance), 1.f);
     float step = dist / (float)n;
-    float e = step * jitter;
-    float t = t0 + e;
+    float e = __fmul_rn(step, jitter);
+    float t = __fadd_rn(t0, e);
     unsigned light_samples = 0;
     if constexpr (COUNT) light_samples = shadow_sample_count(C.shadow_steps);
     for (unsigned k = n; k != 0; --k, t += step, e += step) {
-        float3 pos = C.cam + view * t;
+        float3 pos = make_float3(fmaf(view.x, t, C.cam.x), fmaf(view.y, t, C.cam.y), fmaf(view.z, t, C.cam.z));
         float rho2 = fmaf(e, k_e + e, rho2_e);
         float h = height01_rho2(C, rho2);
         // RayMarchStep (VolumetricCloudRender.comp:116-137)
-        float sigma = sigma_t<COUNT>(C, M, pos, h, t, &S.detail);
+        float sigma;
+        if constexpr (FAST) sigma = fast_sigma_m1<COUNT>(M, pos, h, t * t, &S.detail);
+        else sigma = sigma_t<COUNT>(C, M, pos, h, t, &S.detail);
         if constexpr (COUNT) {
             S.samples++;
             S.evals++;
@@ -97,7 +108,7 @@ __device__ __forceinline__ void march_segment(const CloudConsts& C, const Materi
             if constexpr (COUNT) S.evals += light_samples;
             float tr;
             float one_m_tr = one_minus_exp(step * sigma, tr);
-            float tsun = sample_shadow<COUNT>(C, M, pos, rho2, &S.detail);
+            float tsun = sample_shadow<FAST, COUNT>(C, M, pos, rho2, &S.detail);
             float w = __expf(-C.sun_ms_sigma_scale * sigma);
             float phase = ph_back * (1.f - w) + ph_fwd * w;
             float e_dummy;
@@ -123,7 +134,7 @@ __device__ __forceinline__ void march_segment(const CloudConsts& C, const Materi
 // repeated FP32 sums `t += step`, so the result equals march_segment's; the
 // group only shortens the chain of dependent texture reads per ray, which
 // bounds launches with few rays per SM (the quarter-resolution pass).
-template <int G>
+template <int G, bool FAST>
 __device__ __forceinline__ void march_segment_lanes(const CloudConsts& C, const MaterialConsts& M, float3 view,
                                                     float t0, float t1, float rho2_e, float k_e, float jitter,
                                                     float ph_back, float ph_fwd, March& S, int sub,
@@ -131,8 +142,8 @@ __device__ __forceinline__ void march_segment_lanes(const CloudConsts& C, const 
     float dist = fminf(t1 - t0, C.max_raymarch_distance);
     unsigned n = (unsigned)fmaxf(C.max_raymarch_steps * (dist / C.max_raymarch_distance), 1.f);
     float step = dist / (float)n;
-    float e = step * jitter;
-    float t = t0 + e;
+    float e = __fmul_rn(step, jitter);
+    float t = __fadd_rn(t0, e);
     for (unsigned k0 = 0; k0 < n; k0 += G) {
         float tk = t, ek = e;
 #pragma unroll
@@ -144,13 +155,14 @@ __device__ __forceinline__ void march_segment_lanes(const CloudConsts& C, const 
         }
         float sigma = 0.f, tp = 0.f, omt = 0.f, env = 0.f, tr = 1.f;
         if (k0 + (unsigned)sub < n) {
-            float3 pos = C.cam + view * tk;
+            float3 pos = make_float3(fmaf(view.x, tk, C.cam.x), fmaf(view.y, tk, C.cam.y), fmaf(view.z, tk, C.cam.z));
             float rho2 = fmaf(ek, k_e + ek, rho2_e);
             float h = height01_rho2(C, rho2);
-            sigma = sigma_t(C, M, pos, h, tk);
+            if constexpr (FAST) sigma = fast_sigma_m1(M, pos, h, tk * tk);
+            else sigma = sigma_t(C, M, pos, h, tk);
             if (sigma >= 1e-5f) {
                 omt = one_minus_exp(step * sigma, tr);
-                float tsun = sample_shadow(C, M, pos, rho2);
+                float tsun = sample_shadow<FAST>(C, M, pos, rho2);
                 float w = __expf(-C.sun_ms_sigma_scale * sigma);
                 float phase = ph_back * (1.f - w) + ph_fwd * w;
                 float e_dummy;
@@ -234,8 +246,12 @@ __device__ __forceinline__ void shell_intersect(const CloudConsts& C, float mu, 
 // (skyr_tuning::cloud_ray_lanes); a warp then covers 32 / G rays.  COUNT (with
 // G = 1): the instrumented launch, which adds the frame's raymarch samples,
 // density evaluations and detail-texture evaluations to counters[0..2].
-template <class S, int MINB, int G, bool COUNT = false>
-__global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, MaterialConsts M, AtmoConsts A,
+// FAST: the density evaluation of cloud_fast.cuh (only when M.fast_ok).  The
+// parameter blocks are __grid_constant__: device code reads them in place
+// (a run-time index into them is a constant load, not a local copy).
+template <class S, int MINB, int G, bool COUNT, bool FAST>
+__global__ void __launch_bounds__(128, MINB) cloud_render_kernel(const __grid_constant__ CloudConsts C,
+                                                           const __grid_constant__ MaterialConsts M, AtmoConsts A,
                                                            const float4* __restrict__ tlut, int tw, int th,
                                                            const S* __restrict__ ap_lum,
                                                            const S* __restrict__ ap_trans,
@@ -294,11 +310,11 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, 
         float t0 = sg ? it[2] : it[0], t1 = sg ? it[3] : it[1];
         if (sg && !(t1 - t0 > 0.f)) break;
         if constexpr (G == 1)
-            march_segment<COUNT>(C, M, view, t0, t1, sg ? ent[1] : ent[0], 2.f * (rmu + t0), jitter, ph_back,
-                                 ph_fwd, mk);
+            march_segment<FAST, COUNT>(C, M, view, t0, t1, sg ? ent[1] : ent[0], 2.f * (rmu + t0), jitter, ph_back,
+                                       ph_fwd, mk);
         else
-            march_segment_lanes<G>(C, M, view, t0, t1, sg ? ent[1] : ent[0], 2.f * (rmu + t0), jitter, ph_back,
-                                   ph_fwd, mk, sub, gmask);
+            march_segment_lanes<G, FAST>(C, M, view, t0, t1, sg ? ent[1] : ent[0], 2.f * (rmu + t0), jitter,
+                                         ph_back, ph_fwd, mk, sub, gmask);
     }
 
     float avg_t = mk.wsum == 0.f ? frag_dist : mk.wsum / mk.trans_sum;
@@ -360,7 +376,7 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(CloudConsts C, 
 
 // Launches the raymarch kernel for G lanes per ray and the register cut MINB
 // (resident blocks per SM: 5, 6, 7 or 8) with the LUT storage type (half:
-// RGBA16F, else RGBA32F).  Every (G, MINB) pair is instantiated in one of the
+// RGBA16F, else RGBA32F) and the density evaluation M.fast_ok selects.  Every (G, MINB) pair is instantiated in one of the
 // cloud_raymarch_l<G>_c<cuts>.cu translation units, two cuts per unit, so the
 // kernel variants compile in parallel.
 template <int G, int MINB>
@@ -369,14 +385,21 @@ void launch_cloud_render_cut(bool half, dim3 grid, cudaStream_t stream, const Cl
                              const void* ap_lum, const void* ap_trans, const float* blue_noise, const float* depth,
                              __half2* out_rgba, float* out_dist, unsigned long long* counters, int tile_w,
                              int warps_x) {
-    auto go = [&](auto tag) {
+    auto go = [&](auto tag, auto fast) {
         using S = decltype(tag);
-        cloud_render_kernel<S, MINB, G><<<grid, 128, 0, stream>>>(
+        cloud_render_kernel<S, MINB, G, false, decltype(fast)::value><<<grid, 128, 0, stream>>>(
             C, M, A, tlut, tw, th, reinterpret_cast<const S*>(ap_lum), reinterpret_cast<const S*>(ap_trans),
             blue_noise, depth, out_rgba, out_dist, counters, tile_w, warps_x);
     };
-    if (half) go(__half2{});
-    else go(float4{});
+    using Fast = std::true_type;
+    using General = std::false_type;
+    if (half) {
+        if (M.fast_ok) go(__half2{}, Fast{});
+        else go(__half2{}, General{});
+    } else {
+        if (M.fast_ok) go(float4{}, Fast{});
+        else go(float4{}, General{});
+    }
 }
 
 #define SKYR_CLOUD_CUT_SIGNATURE(G, B)                                                                          \

@@ -22,7 +22,7 @@ __device__ __forceinline__ float height01(const CloudConsts& C, float3 p) {
 __device__ __forceinline__ float height01_rho2(const CloudConsts& C, float rho2) {
     float r = sqrtf(fmaf(C.R, C.R, rho2));
     float alt = __fdividef(rho2, r + C.R);
-    return clamp01((alt - C.bottom) * C.inv_layer);
+    return clamp01(__fsub_rn(alt, C.bottom) * C.inv_layer);
 }
 
 // COUNT: instrumented launches count the evaluations that sample the detail
