@@ -85,11 +85,14 @@ typedef struct skyr_device_limits {
      * 2^20, range [1, 2^30] */
     int32_t tracking_steps;
     int32_t reserved; /* 0 */
-    /* SM clock cycles a block of the surrogate raymarch waits for the bulk
-     * copy of the network into its shared memory before it gives up (the
-     * block then waits for the copy in flight with the default bound and
-     * leaves without rendering); default 2^31 (about a second), range
-     * [0, 2^40] (0: no block waits, every block gives up at once) */
+    /* SM clock cycles a block waits for an asynchronous unit of its own
+     * before it gives up: the bulk copy of the network into the shared memory
+     * of a surrogate-raymarch block, and the tensor-core products of the
+     * network's inference and training kernels.  A block that gives up
+     * waits for the work in flight with the default bound, frees its tensor
+     * memory and leaves without writing its outputs.  Default 2^31 (about a
+     * second), range [0, 2^40] (0: no block waits, every block gives up at
+     * once) */
     int64_t copy_wait_cycles;
 } skyr_device_limits;
 int skyr_device_limits_default(skyr_device_limits* out);

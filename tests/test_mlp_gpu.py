@@ -168,6 +168,30 @@ def test_epoch_gathers_batches_in_the_kernel(ctx):
     c.close()
 
 
+def test_tensor_core_wait_bound_reports_timeout(ctx):
+    """With a wait bound of 0 every CTA of the tcgen05 inference gives up on its
+    first product: it lets the product land (bounded), frees its tensor memory
+    and leaves without writing; the call reads SKYR_ETIMEOUT, the output stays
+    untouched, and the default bound then infers normally."""
+    p = _params(61)
+    rec, _, _ = _data(1000, 62)
+    net = mlp.PackedMLP.from_params(ctx, p)
+    default = ctx.limits
+    tight = _abi.DeviceLimits.from_buffer_copy(default)
+    tight.copy_wait_cycles = 0
+    y = torch.full((1000, 3), float("nan"), device="cuda")
+    ctx.limits = tight
+    net.infer(rec, out=y)
+    with pytest.raises(_abi.SkyrError) as exc:
+        ctx.check_status()
+    assert exc.value.status == _abi.SKYR_ETIMEOUT
+    assert bool(torch.isnan(y).all())
+    ctx.limits = default
+    net.infer(rec, out=y)
+    ctx.check_status()
+    assert bool(torch.isfinite(y).all())
+
+
 def test_adam_step_matches_oracle(ctx):
     p = _params(41)
     rec, _, t = _data(2048, 42)
