@@ -68,6 +68,25 @@ size_t skyr_noise_expanded_bytes(const skyr_noise_texture_desc* desc, int channe
 int skyr_noise_expand(skyr_ctx* ctx, const skyr_noise_texture_desc* desc, const void* tex, int channels,
                       void* out);
 
+/* A hardware sampler of level 0 of one channel of a generated texture: the
+ * bytes are copied (ordered on the context's stream) into a CUDA array that the
+ * texture units filter as the GL texture of the reference does -- LINEAR,
+ * REPEAT, UNORM8 -- with its 8-bit fixed-point filter weights (1/256), the
+ * precision GL drivers filter the reference's textures with.  The cloud
+ * raymarch takes its magnified Material1 fetches from it when
+ * skyr_cloud_textures names one; minified fetches (NEAREST_MIPMAP_NEAREST at
+ * the levels above 0) still read `tex`.  The library allocates the array; the
+ * sampler keeps no pointer to `tex`.  skyr_noise_sampler_handle gives the
+ * cudaTextureObject_t as a 64-bit value.  (Counterpart: the texture objects the
+ * reference binds, VolumetricCloudDefaultMaterial.cpp:40-72.) */
+typedef struct skyr_noise_sampler skyr_noise_sampler;
+int skyr_noise_sampler_create(skyr_ctx* ctx, const skyr_noise_texture_desc* desc, const void* tex, int channel,
+                              skyr_noise_sampler** out);
+/* Copy a regenerated texture (same description) into the sampler; the handle stays valid. */
+int skyr_noise_sampler_update(skyr_ctx* ctx, skyr_noise_sampler* sampler, const void* tex);
+int skyr_noise_sampler_destroy(skyr_noise_sampler* sampler);
+uint64_t skyr_noise_sampler_handle(const skyr_noise_sampler* sampler);
+
 /* ---- material plug-ins (IVolumetricCloudMaterial) --------------------- */
 #define SKYR_MATERIAL_DEFAULT0 0 /* VolumetricCloudDefaultMaterial0 (VolumetricCloudDefaultMaterial0.glsl) */
 #define SKYR_MATERIAL_DEFAULT1 1 /* VolumetricCloudDefaultMaterial1 (VolumetricCloudDefaultMaterial1.glsl) */
@@ -127,6 +146,9 @@ typedef struct skyr_cloud_textures {
     const void* voxel_expanded;
     int cloud_map_expanded_channels, detail_expanded_channels;
     int displacement_expanded_channels, voxel_expanded_channels;
+    /* optional hardware samplers (skyr_noise_sampler_handle, 0 = none) of
+     * channel 0 of the cloud map and of the detail texture */
+    uint64_t cloud_map_sampler, detail_sampler;
 } skyr_cloud_textures;
 
 /* ---- volumetric cloud (VolumetricCloud) ------------------------------ */

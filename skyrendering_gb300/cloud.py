@@ -33,6 +33,8 @@ class NoiseTexture:
         self.data = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
         self.expanded = None
         self.expanded_channels = 0
+        self._sampler = C.c_void_p()
+        self._sampler_ctx = None
         self._generated = None
 
     def level_offset(self, level: int) -> int:
@@ -50,7 +52,36 @@ class NoiseTexture:
         self._generated = bytes(self.desc)
         if self.expanded is not None:
             self.expand(ctx, self.expanded_channels)
+        if self._sampler:  # the same handle, refreshed: textures structs that hold it stay valid
+            _abi.call("skyr_noise_sampler_update", ctx.handle, self._sampler, _ptr(self.data))
         return self
+
+    def make_sampler(self, ctx: Context) -> "NoiseTexture":
+        """(Re)build the hardware sampler of channel 0 of level 0 (skyr_noise_sampler):
+        GL LINEAR / REPEAT / UNORM8 filtering in the texture units."""
+        self.close_sampler()
+        _abi.call("skyr_noise_sampler_create", ctx.handle, C.byref(self.desc), _ptr(self.data), 0,
+                  C.byref(self._sampler))
+        self._sampler_ctx = ctx
+        return self
+
+    @property
+    def sampler(self) -> int:
+        """The sampler's texture-object handle, 0 without one."""
+        return int(_abi.lib().skyr_noise_sampler_handle(self._sampler)) if self._sampler else 0
+
+    def close_sampler(self) -> None:
+        if self._sampler:
+            if self._sampler_ctx is not None:
+                self._sampler_ctx.synchronize()  # no launch in flight may still read it
+            _abi.call("skyr_noise_sampler_destroy", self._sampler)
+            self._sampler = C.c_void_p()
+
+    def __del__(self):  # best effort
+        try:
+            self.close_sampler()
+        except Exception:
+            pass
 
     def expand(self, ctx: Context, channels: int) -> "NoiseTexture":
         """Build the filtering layout of level 0 for the first `channels` channels."""
@@ -74,6 +105,10 @@ class NoiseTexture:
 def textures_struct(cloud_map: NoiseTexture | None = None, detail: NoiseTexture | None = None,
                     displacement: NoiseTexture | None = None, voxel: NoiseTexture | None = None):
     t = _abi.CloudTextures()
+    # The struct holds raw device pointers and sampler handles: it keeps the
+    # textures alive, so a sampler is not destroyed (nor a buffer reused) while
+    # a renderer that holds the struct can still launch with it.
+    t._owners = [x for x in (cloud_map, detail, displacement, voxel) if x is not None]
     for name, tex in (("cloud_map", cloud_map), ("detail", detail), ("displacement", displacement),
                       ("voxel", voxel)):
         if tex is not None:
@@ -82,6 +117,8 @@ def textures_struct(cloud_map: NoiseTexture | None = None, detail: NoiseTexture 
             if tex.expanded is not None:
                 setattr(t, name + "_expanded", tex.expanded.data_ptr())
                 setattr(t, name + "_expanded_channels", tex.expanded_channels)
+            if name in ("cloud_map", "detail") and tex.sampler:
+                setattr(t, name + "_sampler", tex.sampler)
     return t
 
 
@@ -94,11 +131,15 @@ MATERIAL_CHANNELS = {
 }
 
 
-def prepare_textures(ctx: Context, material_type: int, textures: dict) -> dict:
-    """Expand the level-0 channels that `material_type` filters (exact re-layout)."""
+def prepare_textures(ctx: Context, material_type: int, textures: dict, samplers: bool = True) -> dict:
+    """Expand the level-0 channels that `material_type` filters (exact re-layout) and,
+    for Material1 with `samplers`, build the hardware samplers of its two textures."""
     for name, ch in MATERIAL_CHANNELS[material_type].items():
         if name in textures and textures[name].expanded_channels < ch:
             textures[name].expand(ctx, ch)
+        if samplers and material_type == _abi.SKYR_MATERIAL_DEFAULT1 and name in textures and \
+                not textures[name].sampler:
+            textures[name].make_sampler(ctx)
     return textures
 
 

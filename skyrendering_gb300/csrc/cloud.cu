@@ -120,20 +120,29 @@ int fill_tex(DTex& t, const void* p, const skyr_noise_texture_desc& d, bool bord
 
 // The constants of the specialised density evaluation (cloud_fast.cuh), and
 // whether it applies: Material1, NEAREST_MIPMAP_NEAREST minification on both
-// textures, REPEAT, expanded level 0 present, a square cloud map and a cubic
-// detail texture.
-static void derive_fast_consts(const skyr_cloud_material& m, const skyr_cloud_textures& tex, MaterialConsts& mc,
-                               double tan_half, double vmin) {
+// textures, REPEAT, for each texture a hardware sampler or the expanded level 0,
+// a square cloud map and a cubic detail texture.
+static void derive_fast_consts(const skyr_cloud_material& m, const skyr_cloud_textures& tex,
+                               const skyr_cloud_parameters& cp, double R, MaterialConsts& mc, double tan_half,
+                               double vmin) {
     mc.fast_ok = 0;
+    // the height series holds while |rho2| / R^2 <= 0.02 for every sample: the primary samples lie in the
+    // layer, the light-march samples within shadow_distance of it
+    const double h_hi = (double)cp.bottom_altitude + cp.thickness + cp.shadow_distance,
+                 h_lo = (double)cp.bottom_altitude - cp.shadow_distance;
+    const double x_max = std::max(std::fabs(h_hi * (2.0 * R + h_hi)), std::fabs(h_lo * (2.0 * R + h_lo))) / (R * R);
+    if (!(x_max <= 0.02)) return;
     const skyr_noise_texture_desc &cd = tex.cloud_map_desc, &dd = tex.detail_desc;
     if (m.type != SKYR_MATERIAL_DEFAULT1 || m.minfilter2d != SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST ||
-        m.minfilter3d != SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST || !mc.cloud_map_tex.ex || !mc.detail_tex.ex ||
-        mc.cloud_map_tex.border || mc.detail_tex.border || cd.width != cd.height || cd.depth != 1 ||
-        dd.width != dd.height || dd.width != dd.depth || dd.depth < 2)
+        m.minfilter3d != SKYR_MIPMAP_NEAREST_MIPMAP_NEAREST || !(mc.cloud_map_tex.ex || tex.cloud_map_sampler) ||
+        !(mc.detail_tex.ex || tex.detail_sampler) || mc.cloud_map_tex.border || mc.detail_tex.border ||
+        cd.width != cd.height || cd.depth != 1 || dd.width != dd.height || dd.width != dd.depth || dd.depth < 2)
         return;
-    auto fill = [&](FastTex& t, const DTex& d, const skyr_noise_texture_desc& desc, double repeat) {
+    auto fill = [&](FastTex& t, const DTex& d, const skyr_noise_texture_desc& desc, double repeat,
+                    uint64_t sampler) {
         t.base = d.base;
         t.ex = d.ex;
+        t.tex = sampler;
         t.w = desc.width;
         t.h = desc.height;
         t.d = desc.depth;
@@ -151,8 +160,8 @@ static void derive_fast_consts(const skyr_cloud_material& m, const skyr_cloud_te
             t.off[l] = l < d.levels ? (unsigned)noise_level_offset(&desc, l) : 0u;
     };
     FastConsts& f = mc.fast;
-    fill(f.cm, mc.cloud_map_tex, cd, m.cloud_map_repeat_size);
-    fill(f.dt, mc.detail_tex, dd, m.detail_repeat_size);
+    fill(f.cm, mc.cloud_map_tex, cd, m.cloud_map_repeat_size, tex.cloud_map_sampler);
+    fill(f.dt, mc.detail_tex, dd, m.detail_repeat_size, tex.detail_sampler);
     // Material1's terms in 0..255 texel units (VolumetricCloudDefaultMaterial1.glsl:18-28)
     const double e = m.base_edge_hardness, hh = m.base_height_hardness;
     f.cov_a = (float)(e / 255.0);
@@ -165,6 +174,10 @@ static void derive_fast_consts(const skyr_cloud_material& m, const skyr_cloud_te
     f.ec_a = (float)(-1.0 / 255.0);
     f.ec_b = m.edge_cut;
     f.density = m.density;
+    const double inv_layer = 1.0 / cp.thickness;
+    f.h_ir2 = (float)(1.0 / (R * R));
+    f.h_k1 = (float)(inv_layer / (2.0 * R));
+    f.h_k0 = (float)(-(double)cp.bottom_altitude * inv_layer);
     mc.fast_ok = 1;
 }
 
@@ -316,7 +329,7 @@ int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud
         return st;
     if (d0 && tex.displacement_desc.channels < 4) return set_error(SKYR_EINVAL, "displacement texture needs 4 channels");
     if ((d0 || d1) && tex.cloud_map_desc.channels < 2) return set_error(SKYR_EINVAL, "cloud map needs 2 channels");
-    derive_fast_consts(m, tex, mc, tan_half, vmin);
+    derive_fast_consts(m, tex, cp, R, mc, tan_half, vmin);
     return SKYR_OK;
 }
 

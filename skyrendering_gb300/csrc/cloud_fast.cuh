@@ -14,7 +14,12 @@
 //     into the material's constants, each clamp01(a x + b) being one fused
 //     multiply-add with saturation;
 //   * a level's byte offset is one constant load (kernel parameters are
-//     __grid_constant__), not a loop over the levels above it.
+//     __grid_constant__), not a loop over the levels above it;
+//   * where the caller gives a hardware sampler of level 0
+//     (skyr_noise_sampler), the magnified LINEAR fetch is one texture
+//     instruction: the texture unit filters UNORM8 texels with 8-bit
+//     fixed-point weights, as GL does for the reference's textures, and the
+//     filter arithmetic leaves the SM's pipes.
 // The host picks this path (MaterialConsts::fast_ok) only when every
 // condition holds, square / cubic textures included; anything else runs the
 // general sample_sigma_t.
@@ -76,6 +81,16 @@ __device__ __forceinline__ float fast_nearest(const FastTex& T, float u, float v
     return __uint_as_float(0x4B000000u | (unsigned)__ldg(T.base + T.off[l] + i)) - 8388608.f;
 }
 
+// CalHeight01 (VolumetricCloudCommon.glsl:36-39) of a point with
+// rho2 = |p + R z^|^2 - R^2, by the series of FastConsts (no square root, no
+// division).  Products of several uses are rounded explicitly (see
+// sample_shadow).
+__device__ __forceinline__ float fast_height01(const FastConsts& F, float rho2) {
+    float x = __fmul_rn(rho2, F.h_ir2);
+    float poly = fmaf(x, fmaf(x, 0.125f, -0.25f), 1.f);
+    return sat(fmaf(__fmul_rn(rho2, poly), F.h_k1, F.h_k0));
+}
+
 // Material1's SampleSigmaT at p with height fraction h and squared camera
 // distance d2 (VolumetricCloudDefaultMaterial1.glsl:14-29).  n_detail
 // (COUNT): evaluations past the coverage test.
@@ -85,14 +100,23 @@ __device__ __forceinline__ float fast_sigma_m1(const MaterialConsts& M, float3 p
     const FastConsts& F = M.fast;
     float u = fmaf(p.x, M.cloud_map.frequency, M.cloud_map.bias_x);
     float v = fmaf(p.y, M.cloud_map.frequency, M.cloud_map.bias_y);
-    float cr = d2 <= F.cm.mag_d2 ? fast_bilinear(F.cm, u, v) : fast_nearest<false>(F.cm, u, v, 0.f, d2);
+    float cr;
+    if (d2 <= F.cm.mag_d2)
+        cr = F.cm.tex ? 255.f * tex2D<float>((cudaTextureObject_t)F.cm.tex, u, v) : fast_bilinear(F.cm, u, v);
+    else
+        cr = fast_nearest<false>(F.cm, u, v, 0.f, d2);
     float density = sat(fmaf(cr, F.cov_a, F.cov_b)) * sat(fmaf(h, F.hh_a, F.hh_b));
     if (density == 0.f) return 0.f;
     if constexpr (COUNT) ++*n_detail;
     float du = fmaf(p.x, M.detail.frequency, M.detail.bias_x);
     float dv = fmaf(p.y, M.detail.frequency, M.detail.bias_y);
     float dw = p.z * M.detail.frequency;
-    float dt = d2 <= F.dt.mag_d2 ? fast_trilinear(F.dt, du, dv, dw) : fast_nearest<true>(F.dt, du, dv, dw, d2);
+    float dt;
+    if (d2 <= F.dt.mag_d2)
+        dt = F.dt.tex ? 255.f * tex3D<float>((cudaTextureObject_t)F.dt.tex, du, dv, dw)
+                      : fast_trilinear(F.dt, du, dv, dw);
+    else
+        dt = fast_nearest<true>(F.dt, du, dv, dw, d2);
     float erode = fmaxf(sat(h - F.height_cut), sat(fmaf(cr, F.ec_a, F.ec_b)));
     return sat(fmaf(-fmaf(dt, F.det_a, F.det_b), erode, density)) * F.density * h;
 }

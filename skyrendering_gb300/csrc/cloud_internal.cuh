@@ -143,6 +143,7 @@ struct SampleInfoD {
 struct FastTex {
     const uint8_t* base;  // channel 0 of level l at base + off[l]
     const void* ex;       // expanded level 0 of channel 0 (uint32 per 2D texel, uint64 per 3D texel)
+    unsigned long long tex;  // hardware sampler of level 0, channel 0 (cudaTextureObject_t), or 0
     int w, h, d;          // level-0 size (powers of two; d = 1 for a 2D texture)
     int last;             // index of the last mip level
     float fw, fh, fd;     // level-0 size as floats
@@ -159,6 +160,11 @@ struct FastConsts {
     float height_cut;        // clamp01(h - height_cut)
     float ec_a, ec_b;        // clamp01(edge_cut - cr)                     = sat(cr255 ec_a + ec_b)
     float density;           // uDensity
+    // CalHeight01 from rho2 = |p + R z|^2 - R^2 by its series in x = rho2 / R^2:
+    // altitude = rho2 / (2R) (1 - x/4 + x^2/8 - 5x^3/64 ...); the host admits the
+    // path only while |x| <= 0.02 for every sample (the cubic term < 2e-7)
+    float h_ir2;             // 1 / R^2
+    float h_k1, h_k0;        // height01 = sat(altitude h_k1 + h_k0): inv_layer, -bottom inv_layer, with 1/(2R)
 };
 
 // Material constants (the material's Update + VolumetricCloudDefaultMaterialCommon)

@@ -50,7 +50,8 @@ __device__ __forceinline__ float sample_shadow(const CloudConsts& C, const Mater
         float f = fmaf(0.5f, dt, prev);
         float3 sp = make_float3(fmaf(sv.x, f, pos.x), fmaf(sv.y, f, pos.y), fmaf(sv.z, f, pos.z));
         float d = __fmul_rn(C.shadow_distance, f);
-        float h = height01_rho2(C, fmaf(d, __fadd_rn(q2, d), rho2_p));
+        float rho2 = fmaf(d, __fadd_rn(q2, d), rho2_p);
+        float h = FAST ? fast_height01(M.fast, rho2) : height01_rho2(C, rho2);
         float3 dc = sp - C.cam;
         float sigma;
         if constexpr (FAST) sigma = fast_sigma_m1<COUNT>(M, sp, h, dot3(dc, dc), n_detail);
@@ -95,7 +96,7 @@ __device__ __forceinline__ void march_segment(const CloudConsts& C, const Materi
     for (unsigned k = n; k != 0; --k, t += step, e += step) {
         float3 pos = make_float3(fmaf(view.x, t, C.cam.x), fmaf(view.y, t, C.cam.y), fmaf(view.z, t, C.cam.z));
         float rho2 = fmaf(e, k_e + e, rho2_e);
-        float h = height01_rho2(C, rho2);
+        float h = FAST ? fast_height01(M.fast, rho2) : height01_rho2(C, rho2);
         // RayMarchStep (VolumetricCloudRender.comp:116-137)
         float sigma;
         if constexpr (FAST) sigma = fast_sigma_m1<COUNT>(M, pos, h, t * t, &S.detail);
@@ -157,7 +158,7 @@ __device__ __forceinline__ void march_segment_lanes(const CloudConsts& C, const 
         if (k0 + (unsigned)sub < n) {
             float3 pos = make_float3(fmaf(view.x, tk, C.cam.x), fmaf(view.y, tk, C.cam.y), fmaf(view.z, tk, C.cam.z));
             float rho2 = fmaf(ek, k_e + ek, rho2_e);
-            float h = height01_rho2(C, rho2);
+            float h = FAST ? fast_height01(M.fast, rho2) : height01_rho2(C, rho2);
             if constexpr (FAST) sigma = fast_sigma_m1(M, pos, h, tk * tk);
             else sigma = sigma_t(C, M, pos, h, tk);
             if (sigma >= 1e-5f) {

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <new>
 #include <random>
 #include <vector>
 
@@ -233,6 +234,95 @@ int skyr_noise_expand(skyr_ctx* ctx, const skyr_noise_texture_desc* desc, const 
         expand2d_kernel<<<blocks, 256, 0, ctx->stream>>>(t, desc->width, desc->height, channels,
                                                          reinterpret_cast<uint32_t*>(out));
     return check_cuda(cudaGetLastError(), "texture expansion kernel");
+}
+
+}  // extern "C"
+
+struct skyr_noise_sampler {
+    int device = 0;
+    cudaArray_t array = nullptr;
+    cudaTextureObject_t tex = 0;
+    skyr_noise_texture_desc desc{};
+    int channel = 0;
+};
+
+namespace {
+// Channel `channel` of level 0 of `tex` (channel-planar layout) into the sampler's array.
+int sampler_copy(skyr_ctx* ctx, skyr_noise_sampler* smp, const void* tex) {
+    const skyr_noise_texture_desc& d = smp->desc;
+    const bool d3 = d.depth > 1;
+    const size_t plane = (size_t)d.width * d.height * d.depth;
+    cudaMemcpy3DParms cp{};
+    cp.srcPtr = make_cudaPitchedPtr(const_cast<uint8_t*>(reinterpret_cast<const uint8_t*>(tex)) + smp->channel * plane,
+                                    (size_t)d.width, (size_t)d.width, (size_t)d.height);
+    cp.dstArray = smp->array;
+    cp.extent = make_cudaExtent((size_t)d.width, (size_t)d.height, d3 ? (size_t)d.depth : 1);
+    cp.kind = cudaMemcpyDeviceToDevice;
+    return check_cuda(cudaMemcpy3DAsync(&cp, ctx->stream), "copy into the noise sampler");
+}
+}  // namespace
+
+extern "C" {
+
+int skyr_noise_sampler_destroy(skyr_noise_sampler* sampler) {
+    if (!sampler) return SKYR_OK;
+    cudaSetDevice(sampler->device);
+    int st = SKYR_OK;
+    if (sampler->tex) st = check_cuda(cudaDestroyTextureObject(sampler->tex), "cudaDestroyTextureObject");
+    if (sampler->array) {
+        int e = check_cuda(cudaFreeArray(sampler->array), "cudaFreeArray");
+        if (!st) st = e;
+    }
+    delete sampler;
+    return st;
+}
+
+int skyr_noise_sampler_create(skyr_ctx* ctx, const skyr_noise_texture_desc* desc, const void* tex, int channel,
+                              skyr_noise_sampler** out) {
+    if (!ctx || !out) return set_error(SKYR_EINVAL, "null argument");
+    *out = nullptr;
+    if (int st = validate_noise_desc(desc, false)) return st;
+    if (!tex) return set_error(SKYR_EINVAL, "null texture");
+    if (channel < 0 || channel >= desc->channels) return set_error(SKYR_EINVAL, "bad channel %d", channel);
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    auto* smp = new (std::nothrow) skyr_noise_sampler;
+    if (!smp) return set_error(SKYR_ENOMEM, "out of host memory");
+    smp->device = ctx->device;
+    smp->desc = *desc;
+    smp->channel = channel;
+    const bool d3 = desc->depth > 1;
+    cudaChannelFormatDesc fmt = cudaCreateChannelDesc<unsigned char>();
+    cudaExtent ext = make_cudaExtent((size_t)desc->width, (size_t)desc->height, d3 ? (size_t)desc->depth : 0);
+    int e = check_cuda(cudaMalloc3DArray(&smp->array, &fmt, ext, 0), "cudaMalloc3DArray(noise sampler)");
+    if (!e) e = sampler_copy(ctx, smp, tex);
+    if (!e) {
+        cudaResourceDesc rd{};
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = smp->array;
+        cudaTextureDesc td{};
+        td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeWrap;  // GL REPEAT
+        td.filterMode = cudaFilterModeLinear;                                              // GL LINEAR
+        td.readMode = cudaReadModeNormalizedFloat;                                         // UNORM8
+        td.normalizedCoords = 1;
+        e = check_cuda(cudaCreateTextureObject(&smp->tex, &rd, &td, nullptr), "cudaCreateTextureObject");
+    }
+    if (e) {
+        skyr_noise_sampler_destroy(smp);
+        return e;
+    }
+    *out = smp;
+    return SKYR_OK;
+}
+
+int skyr_noise_sampler_update(skyr_ctx* ctx, skyr_noise_sampler* sampler, const void* tex) {
+    if (!ctx || !sampler || !tex) return set_error(SKYR_EINVAL, "null argument");
+    if (sampler->device != ctx->device) return set_error(SKYR_EINVAL, "sampler of another device");
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    return sampler_copy(ctx, sampler, tex);
+}
+
+uint64_t skyr_noise_sampler_handle(const skyr_noise_sampler* sampler) {
+    return sampler ? (uint64_t)sampler->tex : 0;
 }
 
 int skyr_blue_noise_generate(uint32_t seed, float* out) {

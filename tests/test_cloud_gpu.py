@@ -49,7 +49,7 @@ class Frame:
     """One frame's inputs on the device and on the host."""
 
     def __init__(self, ctx, cam, zenith, material_kind=_abi.SKYR_MATERIAL_DEFAULT1, cloud=None, fmt=0,
-                 size=None, expand=True, blue_noise=None):
+                 size=None, expand=True, blue_noise=None, samplers=True):
         self.atmo = W.earth_like_atmosphere()
         self.sizes = W.plain_lut_sizes(fmt)
         self.render = W.render_parameters(cam, zenith)
@@ -61,7 +61,7 @@ class Frame:
         self.tex["detail"] = NoiseTexture(W.base_noise_desc()).generate(ctx)
         self.tex["displacement"] = NoiseTexture(W.displacement_desc()).generate(ctx)
         if expand:
-            prepare_textures(ctx, material_kind, self.tex)
+            prepare_textures(ctx, material_kind, self.tex, samplers=samplers)
         self.bn = (blue_noise_tile() if blue_noise is None else torch.from_numpy(blue_noise)).cuda()
         self.view = W.frame_view(cam, zenith, width=size[0] if size else None, height=size[1] if size else None)
         self.vc = VolumetricCloud(ctx, self.cloud, self.material, textures_struct(**self.tex))
@@ -209,10 +209,39 @@ def test_expanded_layout_bytes(ctx):
 
 def test_expanded_layout_renders_like_plain_layout(ctx):
     cam = W.Camera(width=480, height=270)
-    a = Frame(ctx, cam, 45.0, expand=True)
+    a = Frame(ctx, cam, 45.0, expand=True, samplers=False)
     b = Frame(ctx, cam, 45.0, expand=False)
     ga, gb = a.rgba.float().cpu().numpy(), b.rgba.float().cpu().numpy()
     assert mean_rel(ga, gb) <= 1e-5
+
+
+def test_hardware_samplers_filter_like_gl(ctx):
+    """The Material1 frame with hardware samplers (the texture units' LINEAR filter,
+    8-bit fixed-point weights, as GL filters the reference's textures) against the
+    exact-weight software filter: the weights' rounding moves the frame by about
+    1e-4 (an FP64 experiment with weights rounded to 1/256 gave 0.8-3.2e-4 over sun
+    zeniths 45-95 deg), well inside the 1e-3 bound the frames keep against the oracle.
+    At the frame's 1920x1080 the textures are magnified (LINEAR at level 0) out to
+    about 15 km, so the sampler path covers the near clouds; at 480x270 that range
+    shrinks to about 4 km, and there the two frames came out identical."""
+    cam = W.frame_camera()
+    a = Frame(ctx, cam, 45.0, samplers=True)
+    b = Frame(ctx, cam, 45.0, samplers=False)
+    assert a.tex["cloud_map"].sampler and a.tex["detail"].sampler
+    assert a.vc.textures.detail_sampler and not b.vc.textures.detail_sampler
+    ga, gb = a.rgba.float().cpu().numpy().reshape(-1, 4), b.rgba.float().cpu().numpy().reshape(-1, 4)
+    err = mean_rel(ga[:, :3], gb[:, :3])
+    changed = int((ga[:, :3] != gb[:, :3]).any(axis=1).sum())
+    print(f"hardware samplers against the exact filter: mean rel {err:.2e}, {changed} pixels differ")
+    assert 0.0 < err <= 5e-4 and changed > 0
+    # regenerating the textures refreshes their samplers in place: the same handles render the same frame
+    handles = (a.tex["cloud_map"].sampler, a.tex["detail"].sampler)
+    for t in a.tex.values():
+        t.generate(ctx)
+    assert (a.tex["cloud_map"].sampler, a.tex["detail"].sampler) == handles
+    again, _ = a.vc.render(a.atmo, a.view, a.sizes, a.luts, a.bn)
+    ctx.synchronize()
+    assert torch.equal(again, a.rgba)
 
 
 def test_cloud_invalid_arguments(ctx):
