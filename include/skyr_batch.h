@@ -22,7 +22,7 @@ typedef struct skyr_tuning {
     int view_lanes;          /* lanes sharing one sky-view / aerial-perspective ray: 4, 8, 16 */
     int cloud_tile_width;    /* pixels across one warp's tile (height 32 / width): 4, 8, 16, 32 */
     int cloud_block_warps_x; /* warps side by side in a 4-warp block: 1, 2, 4 */
-    int cloud_blocks_per_sm; /* resident blocks per SM the raymarch's registers are cut for: 5, 6, 7, 8 */
+    int cloud_blocks_per_sm; /* resident blocks per SM the raymarch's registers are cut for: 5 .. 10 */
     int cloud_ray_lanes;     /* lanes sharing one ray's steps: 1, 2, 4, 8 (a warp's tile is then at most
                                 32 / lanes pixels wide) */
 } skyr_tuning;
@@ -38,12 +38,12 @@ int skyr_ctx_get_tuning(const skyr_ctx* ctx, skyr_tuning* t);
  *   LUTs:  [0..2] transmittance lanes 4, 8, 16; [3..5] view lanes 4, 8, 16
  *          (the LUT set of skyr_update_lut_set; the outputs are overwritten);
  *   cloud: SKYR_CLOUD_TUNE_CANDIDATES = ray lanes {1, 2, 4, 8} x blocks per SM
- *          {5, 6, 7, 8} x the 12 (tile width, block warps x) pairs (4,1) (4,2) (4,4)
+ *          {5, 6, 7, 8, 9, 10} x the 12 (tile width, block warps x) pairs (4,1) (4,2) (4,4)
  *          (8,1) (8,2) (8,4) (16,1) (16,2) (16,4) (32,1) (32,2) (32,4), index =
- *          (lanes index * 4 + occupancy index) * 12 + pair index
+ *          (lanes index * 6 + occupancy index) * 12 + pair index
  *          (skyr_cloud_render's outputs are overwritten). */
 #define SKYR_CLOUD_TILE_CANDIDATES 12
-#define SKYR_CLOUD_TUNE_CANDIDATES 192
+#define SKYR_CLOUD_TUNE_CANDIDATES 288
 int skyr_autotune_luts(skyr_ctx* ctx, const skyr_atmosphere_parameters* params,
                        const skyr_atmosphere_render_parameters* render, int n_sets, const skyr_lut_sizes* sizes,
                        void* transmittance, void* multiscattering, void* sky_view_luminance,

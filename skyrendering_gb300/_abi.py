@@ -505,7 +505,7 @@ _SIGNATURES.update({
 # skyr_batch.h
 # ---------------------------------------------------------------------------
 SKYR_CLOUD_TILE_CANDIDATES = 12
-SKYR_CLOUD_TUNE_CANDIDATES = 192
+SKYR_CLOUD_TUNE_CANDIDATES = 288
 
 
 class Tuning(C.Structure):

@@ -17,7 +17,7 @@ from .atmosphere import Context, LutSet, _ptr
 
 TILE_CANDIDATES = ((4, 1), (4, 2), (4, 4), (8, 1), (8, 2), (8, 4), (16, 1), (16, 2), (16, 4), (32, 1), (32, 2),
                    (32, 4))
-OCCUPANCY_CANDIDATES = (5, 6, 7, 8)
+OCCUPANCY_CANDIDATES = (5, 6, 7, 8, 9, 10)
 RAY_LANE_CANDIDATES = (1, 2, 4, 8)
 # (tile width, block warps x, blocks per SM, ray lanes) in the order of skyr_autotune_cloud's times
 CLOUD_CANDIDATES = tuple((w, bx, occ, g) for g in RAY_LANE_CANDIDATES for occ in OCCUPANCY_CANDIDATES

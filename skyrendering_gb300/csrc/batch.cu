@@ -49,7 +49,8 @@ constexpr int kTileCandidates[SKYR_CLOUD_TILE_CANDIDATES][2] = {
     {4, 1}, {4, 2}, {4, 4}, {8, 1}, {8, 2}, {8, 4}, {16, 1}, {16, 2}, {16, 4}, {32, 1}, {32, 2}, {32, 4}};
 constexpr int kLaneCandidates[3] = {4, 8, 16};
 
-constexpr int kOccupancyCandidates[4] = {5, 6, 7, 8};
+constexpr int kOccupancyCandidates[6] = {5, 6, 7, 8, 9, 10};
+constexpr int kOccupancies = 6;
 constexpr int kRayLaneCandidates[4] = {1, 2, 4, 8};
 
 bool valid_lanes(int l) { return l == 4 || l == 8 || l == 16; }
@@ -77,7 +78,7 @@ int time_launches(skyr_ctx* ctx, int reps, F&& fn, float* ms) {
 
 // Times `run` for every cloud candidate (ray lanes x blocks per SM x tile
 // shapes, the order of skyr_autotune_cloud's times) and keeps the fastest.
-static_assert(SKYR_CLOUD_TUNE_CANDIDATES == 4 * 4 * SKYR_CLOUD_TILE_CANDIDATES, "cloud candidate table");
+static_assert(SKYR_CLOUD_TUNE_CANDIDATES == 4 * kOccupancies * SKYR_CLOUD_TILE_CANDIDATES, "cloud candidate table");
 
 template <class F>
 int autotune_cloud_candidates(skyr_ctx* ctx, int reps, skyr_tuning* best, float* times_ms, F&& run) {
@@ -90,8 +91,8 @@ int autotune_cloud_candidates(skyr_ctx* ctx, int reps, skyr_tuning* best, float*
         const int* tile = kTileCandidates[i % SKYR_CLOUD_TILE_CANDIDATES];
         ctx->tuning.cloud_tile_width = tile[0];
         ctx->tuning.cloud_block_warps_x = tile[1];
-        ctx->tuning.cloud_blocks_per_sm = kOccupancyCandidates[(i / SKYR_CLOUD_TILE_CANDIDATES) % 4];
-        ctx->tuning.cloud_ray_lanes = kRayLaneCandidates[i / (4 * SKYR_CLOUD_TILE_CANDIDATES)];
+        ctx->tuning.cloud_blocks_per_sm = kOccupancyCandidates[(i / SKYR_CLOUD_TILE_CANDIDATES) % kOccupancies];
+        ctx->tuning.cloud_ray_lanes = kRayLaneCandidates[i / (kOccupancies * SKYR_CLOUD_TILE_CANDIDATES)];
     };
     for (int i = 0; i < SKYR_CLOUD_TUNE_CANDIDATES && !st; ++i) {
         apply(i);
@@ -122,8 +123,8 @@ int skyr_ctx_set_tuning(skyr_ctx* ctx, const skyr_tuning* t) {
         return set_error(SKYR_EINVAL, "lanes must be 4, 8 or 16");
     if (!valid_tile(t->cloud_tile_width, t->cloud_block_warps_x))
         return set_error(SKYR_EINVAL, "cloud tile width must be 4, 8, 16 or 32 and block warps 1, 2 or 4");
-    if (t->cloud_blocks_per_sm < 5 || t->cloud_blocks_per_sm > 8)
-        return set_error(SKYR_EINVAL, "cloud blocks per SM must be 5, 6, 7 or 8");
+    if (t->cloud_blocks_per_sm < 5 || t->cloud_blocks_per_sm > 10)
+        return set_error(SKYR_EINVAL, "cloud blocks per SM must be 5 .. 10");
     if (t->cloud_ray_lanes != 1 && t->cloud_ray_lanes != 2 && t->cloud_ray_lanes != 4 && t->cloud_ray_lanes != 8)
         return set_error(SKYR_EINVAL, "cloud ray lanes must be 1, 2, 4 or 8");
     ctx->tuning = *t;

@@ -408,7 +408,7 @@ void launch_cloud_render_cut(bool half, dim3 grid, cudaStream_t stream, const Cl
                                        const AtmoConsts&, const float4*, int, int, const void*, const void*,   \
                                        const float*, const float*, __half2*, float*, unsigned long long*, int, \
                                        int)
-#define SKYR_CLOUD_CUTS(X, G) X(G, 5); X(G, 6); X(G, 7); X(G, 8)
+#define SKYR_CLOUD_CUTS(X, G) X(G, 5); X(G, 6); X(G, 7); X(G, 8); X(G, 9); X(G, 10)
 #define SKYR_CLOUD_CUT_EXTERN(G, B) extern template SKYR_CLOUD_CUT_SIGNATURE(G, B)
 SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 1);
 SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 2);
@@ -436,6 +436,8 @@ void launch_cloud_render(bool half, int blocks_per_sm, dim3 grid, cudaStream_t s
                                                           counters, tile_w, warps_x);
     };
     switch (blocks_per_sm) {
+        case 10: cut(std::integral_constant<int, 10>{}); break;
+        case 9: cut(std::integral_constant<int, 9>{}); break;
         case 8: cut(std::integral_constant<int, 8>{}); break;
         case 7: cut(std::integral_constant<int, 7>{}); break;
         case 6: cut(std::integral_constant<int, 6>{}); break;

@@ -8,7 +8,7 @@ launch-shape tuning, the autotuners, multi-view raymarches and CUDA graphs.
 * the raymarch's warp-tile shape, register budget and lanes per ray change
   only which lane computes a step and how it is scheduled (with 2 or 4 lanes
   per ray the steps are folded in step order with the same FP32 operations):
-  the 192 shapes give bit-identical frames;
+  the 288 shapes give bit-identical frames;
 * views rendered together (forked streams) or replayed from a CUDA graph are
   bit-identical to one skyr_cloud_render per view;
 * a seeded subset of the batched workload (perturbed atmospheres, altitudes up
@@ -172,7 +172,7 @@ def test_autotuners(sctx):
     best, times = B.autotune_cloud(sctx, atmo, cl.cloud, cl.material, cl.textures, view, sizes, l1, cl.bn, rgba,
                                    dist, reps=2)
     key = B.cloud_tuning_key(best)
-    assert key in B.CLOUD_CANDIDATES and len(times) == len(B.CLOUD_CANDIDATES) == 192
+    assert key in B.CLOUD_CANDIDATES and len(times) == len(B.CLOUD_CANDIDATES) == 288
     assert min(times) == pytest.approx(times[B.CLOUD_CANDIDATES.index(key)])
 
 

@@ -16,7 +16,7 @@ and as a whole chain.
   the depth-aware paths; viewport 480x270 gives odd half / quarter sizes;
 * graph replay is bit-identical, and so is the raymarch with 2, 4 or 8 lanes
   per ray; bad arguments are refused;
-* the quarter-pass autotuner times all 192 launch shapes on the pass itself and
+* the quarter-pass autotuner times all 288 launch shapes on the pass itself and
   keeps the fastest, which renders the same texels as the default shape.
 """
 import numpy as np
