@@ -17,12 +17,25 @@
  *           corner j is +-1/sqrt(3) along v, u, w by bits 0, 1, 2 of j
  *   41      height of the point within the grid box, 0 (bottom) .. 1 (top)
  *   42      cos(view direction, sun direction)
- *   43..47  zero
+ *   43      transmittance from the point along the view direction to where the
+ *           view ray leaves the volume (training points: a midpoint march at
+ *           half-voxel steps to the grid box's exit; the raymarch: what remains
+ *           of the ray's optical depth at its own samples past the point)
+ *   44..78  the density stencil: mean extinction / sigma_ref from mip levels
+ *           l = 2..6 of the grid (level l averages 2^l-voxel cubes), at the
+ *           point and +-2^(l+1) voxels along the sun, the sun's horizontal
+ *           perpendicular (sun x z; sun x x with the sun at the zenith) and
+ *           their cross product; feature 44 + 7 (l - 2) + j, j = 0 the centre,
+ *           j = 1, 2 +- the sun axis, 3, 4 the second axis, 5, 6 the third
+ *   79      zero
  * span = the grid's longest edge; extinctions are divided by sigma_ref.
- * Features 0..32 and 41 depend on the position only: they are taken at the
- * nodes of a coarse lattice (every `stride` voxels, where 33..40 are zero) and
- * interpolated trilinearly; 33..40 are looked up in the grid per sample.  Both
- * are done the same way for training points and for the raymarch.
+ * Features 0..32, 41 and 44..78 depend on the position only: they are taken at
+ * the nodes of a coarse lattice (every `stride` voxels, where the other slots
+ * are zero) and interpolated trilinearly; 33..40, 42 and 43 are computed per
+ * sample.  Both are done the same way for training points and for the
+ * raymarch.  Features 0..42 are the configured inputs; 43..78 (the view ray's
+ * far side and the stencil) halve the network's error against path-traced
+ * labels.
  */
 #ifndef SKYR_SURROGATE_H_
 #define SKYR_SURROGATE_H_
@@ -36,7 +49,8 @@ extern "C" {
 
 /* Feature lattice of one (grid, sun direction) pair (struct id 12). */
 typedef struct skyr_feature_volume {
-    void* data;        /* device: records [nodes][48] bf16, then sun optical depth [nodes] f32 */
+    void* data;        /* device: records [nodes][80] bf16, sun optical depth [nodes] f32, then the
+                        * grid's mip levels 1..6 (FP16, each 256-byte aligned) */
     int stride;        /* voxels between lattice nodes */
     int nx, ny, nz;    /* nodes per axis: (grid n + stride - 1) / stride + 1 */
     float sigma_ref;   /* extinctions are divided by this */
@@ -63,8 +77,9 @@ int skyr_surrogate_parameters_default(skyr_surrogate_parameters* p);
 size_t skyr_feature_volume_bytes(const skyr_density_grid* grid, int stride, skyr_feature_volume* fv);
 
 /* Build the lattice of `grid` for the sun of `view` (angles, and the frame of
- * `atmosphere` / `cloud`): features 0..41 per node and the optical depth to
- * the sun (a midpoint march at half the voxel edge to the grid box's exit).
+ * `atmosphere` / `cloud`): the grid's mip chain, the position features per node
+ * and the optical depth to the sun (a midpoint march at half the voxel edge to
+ * the grid box's exit).
  * fv->data (skyr_feature_volume_bytes), fv->stride and fv->sigma_ref are the
  * caller's; the node counts and fv->sun are filled in. */
 int skyr_feature_volume_build(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,

@@ -343,7 +343,7 @@ def _fp(a: np.ndarray):
 
 
 def mlp_predict(params: np.ndarray, x: np.ndarray, mirror: bool = True, nthreads: int | None = None) -> np.ndarray:
-    """FP64 forward of the surrogate network: x[n][43] -> y[n][3]."""
+    """FP64 forward of the surrogate network: x[n][79] -> y[n][3]."""
     p = np.ascontiguousarray(params, dtype=np.float32)
     xx = np.ascontiguousarray(x, dtype=np.float32)
     y = np.zeros((len(xx), 3))
@@ -353,7 +353,7 @@ def mlp_predict(params: np.ndarray, x: np.ndarray, mirror: bool = True, nthreads
 
 def mlp_gradient(params: np.ndarray, x: np.ndarray, t: np.ndarray, label_scale: float = 1.0,
                  loss_eps: float = 1e-2, mirror: bool = True):
-    """(loss, gradient[15491]) of the mean relative-L2 loss, FP64."""
+    """(loss, gradient[17795]) of the mean relative-L2 loss, FP64."""
     p = np.ascontiguousarray(params, dtype=np.float32)
     xx = np.ascontiguousarray(x, dtype=np.float32)
     tt = np.ascontiguousarray(t, dtype=np.float32)
@@ -442,8 +442,8 @@ def surrogate_render(atmo, cloud, grid_struct, data_half, pt, view, sizes, luts:
     arrs = _lut_arrays(luts, ("transmittance", "aerial_perspective_luminance", "aerial_perspective_transmittance"))
     nodes = fv.nx * fv.ny * fv.nz
     raw = np.ascontiguousarray(lattice, dtype=np.uint8)
-    rec = np.ascontiguousarray(raw[: nodes * 96].view(np.uint16))
-    tau = np.ascontiguousarray(raw[nodes * 96: nodes * 100].view(np.float32))
+    rec = np.ascontiguousarray(raw[: nodes * 160].view(np.uint16))
+    tau = np.ascontiguousarray(raw[nodes * 160: nodes * 164].view(np.float32))
     p = np.ascontiguousarray(params, dtype=np.float32)
     px = np.ascontiguousarray(pixels, dtype=np.int32)
     out, err = np.zeros((len(px), 4)), np.zeros(len(px))

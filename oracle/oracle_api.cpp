@@ -452,7 +452,7 @@ int oracle_pathtrace(const skyr_atmosphere_parameters* atmo, const skyr_cloud_pa
 
 extern "C" {
 
-// y[n][3] = MLP(x[n][43]) in FP64 (BF16 rounding points mirrored when `mirror`)
+// y[n][3] = MLP(x[n][79]) in FP64 (BF16 rounding points mirrored when `mirror`)
 int oracle_mlp_predict(const float* params, const float* x, int n, int mirror, int threads, double* y) {
     orc::MlpOracle net(params, mirror != 0);
     parallel_for(n, threads, [&](int s) {
@@ -463,7 +463,7 @@ int oracle_mlp_predict(const float* params, const float* x, int n, int mirror, i
     return 0;
 }
 
-// gradient of the mean relative-L2 loss (grad[15491] overwritten); returns the loss
+// gradient of the mean relative-L2 loss (grad[17795] overwritten); returns the loss
 double oracle_mlp_gradient(const float* params, const float* x, const float* t, int n, double label_scale,
                            double loss_eps, int mirror, double* grad) {
     orc::MlpOracle net(params, mirror != 0);
@@ -545,9 +545,11 @@ int oracle_point_radiance(const skyr_atmosphere_parameters* atmo, const skyr_clo
 }
 
 // The surrogate raymarch of skyr_surrogate_render for listed pixels, in FP64
-// over the GPU-built feature lattice (records bf16 [nodes][48] then sun
+// over the GPU-built feature lattice (records bf16 [nodes][80] then sun
 // optical depth f32 [nodes]); the network is oracle_mlp.hpp with the BF16
-// rounding points mirrored.  out[n][4] = (luminance rgb, transmittance),
+// rounding points mirrored.  The far-side feature (43) of sample k is the
+// transmittance of what remains of the ray's optical depth at the march's
+// samples past it: exp(-(sum_j>k sigma_j dt + sigma_k dt / 2)).  out[n][4] = (luminance rgb, transmittance),
 // err[n] = the error estimate with a single relative error `rel_err`.
 int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
                             const skyr_density_grid* gd, const skyr_pathtrace_parameters* pt,
@@ -573,7 +575,8 @@ int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_c
     const double cell = (double)gd->voxel_size * fv->stride;
     const orc::V3<double> og(gd->origin[0], gd->origin[1], gd->origin[2]);
     const orc::V3<double> sun(fv->sun[0], fv->sun[1], fv->sun[2]);
-    auto lattice = [&](orc::V3<double> x, double f[42], double& tau) {
+    constexpr int kRec = 80, kIn = orc::kMlpIn;
+    auto lattice = [&](orc::V3<double> x, double f[kIn], double& tau) {
         orc::V3<double> g = (x - og) / cell;
         int i0[3];
         double fr[3];
@@ -582,7 +585,7 @@ int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_c
             i0[a] = std::min(std::max((int)std::floor(g[a]), 0), nn[a] - 2);
             fr[a] = std::min(std::max(g[a] - i0[a], 0.0), 1.0);
         }
-        for (int k = 0; k < 42; ++k) f[k] = 0.0;
+        for (int k = 0; k < kIn; ++k) f[k] = 0.0;
         tau = 0.0;
         for (int c = 0; c < 8; ++c) {
             int d[3] = {c & 1, (c >> 1) & 1, c >> 2};
@@ -590,13 +593,13 @@ int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_c
             for (int a = 0; a < 3; ++a) w *= d[a] ? fr[a] : 1.0 - fr[a];
             size_t node = ((size_t)(i0[2] + d[2]) * fv->ny + (i0[1] + d[1])) * fv->nx + (i0[0] + d[0]);
             tau += w * lattice_tau[node];
-            for (int k = 0; k < 42; ++k) f[k] += w * orc::bf16_to_float(lattice_rec[node * 48 + k]);
+            for (int k = 0; k < kIn; ++k) f[k] += w * orc::bf16_to_float(lattice_rec[node * kRec + k]);
         }
     };
     // features 33..40: the view-oriented cube corners (skyr_surrogate.h)
     const double span = (double)gd->voxel_size * std::max(gd->nx, std::max(gd->ny, gd->nz));
     const double nbr = 0.1 * span / std::sqrt(3.0), inv_ref = 1.0 / fv->sigma_ref;
-    auto view_neighbours = [&](orc::V3<double> x, orc::V3<double> v, double f[42]) {
+    auto view_neighbours = [&](orc::V3<double> x, orc::V3<double> v, double f[kIn]) {
         orc::V3<double> u = sun - v * orc::dot(v, sun);
         double l2 = orc::dot(u, u);
         if (l2 < 1e-8) {
@@ -629,19 +632,23 @@ int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_c
             double jitter = (double)(js >> 8) / 16777216.0;
             double mu = orc::dot(dir, sun);
             double ph = hg(mu, gb) * (1 - ratio) + hg(mu, gf) * ratio;
+            double tau_total = 0, run = 0;
+            for (int k = 0; k < steps; ++k) tau_total += PT.grid_sigma(F.cam + dir * (t0 + (k + jitter) * dt)) * dt;
             for (int k = 0; k < steps && T > min_t; ++k) {
                 double t = t0 + (k + jitter) * dt;
                 orc::V3<double> x = F.cam + dir * t;
                 double sigma = PT.grid_sigma(x);
+                run += sigma * dt;
                 if (!(sigma > 0)) continue;
-                double f[42], tau;
+                double f[kIn], tau;
                 lattice(x, f, tau);
                 view_neighbours(x, dir, f);
+                f[42] = mu;
+                f[43] = std::exp(-std::max(tau_total - run + 0.5 * sigma * dt, 0.0));
                 orc::V3<double> ms(0.0);
                 if (use_network) {
-                    double rec[43], y[3];
-                    for (int q = 0; q < 42; ++q) rec[q] = bf16_of(f[q]);
-                    rec[42] = bf16_of(mu);
+                    double rec[kIn], y[3];
+                    for (int q = 0; q < kIn; ++q) rec[q] = bf16_of(f[q]);
                     net.predict(rec, y);
                     for (int c = 0; c < 3; ++c) ms[c] = std::max(y[c] * (double)(float)out_scale, 0.0);
                 }

@@ -17,28 +17,31 @@
 namespace skyr {
 namespace mlp {
 
-constexpr int kIn = SKYR_MLP_INPUTS;    // 43
-constexpr int kRec = SKYR_MLP_RECORD;   // 48 (3 k-tiles)
+constexpr int kIn = SKYR_MLP_INPUTS;    // 79
+constexpr int kRec = SKYR_MLP_RECORD;   // 80
+constexpr int kKT = kRec / 16;          // k-tiles of the first layer (5)
 constexpr int kW = SKYR_MLP_WIDTH;      // 64
 constexpr int kOut = SKYR_MLP_OUTPUTS;  // 3
 constexpr int kLayers = 5;
+static_assert(kRec % 16 == 0 && kIn < kRec && kRec <= 128, "record: whole k-tiles, at most two 64-column tiles");
 
-// Row strides (bf16) of the packed weight matrices: 112 B and 144 B rows put
-// the 8 rows an ldmatrix phase reads in 8 different 16-byte bank groups.
-constexpr int kS1 = 56;  // W1 [64][kS1], columns 43..55 zero
-constexpr int kSH = 72;  // W2..W4 [64][kSH], W5 [8][kSH] (rows 3..7 zero)
+// Row strides (bf16) of the packed weight matrices: rows of an odd number of
+// 16-byte units (176 B, 144 B) put the 8 rows an ldmatrix phase reads in 8
+// different 16-byte bank groups.
+constexpr int kS1 = kRec + 8;  // W1 [64][kS1], columns kIn.. zero
+constexpr int kSH = 72;        // W2..W4 [64][kSH], W5 [8][kSH] (rows 3..7 zero)
 // Byte offsets in the packed network
 constexpr int kOffW1 = 0;
-constexpr int kOffW2 = kOffW1 + kW * kS1 * 2;   // 7168
-constexpr int kOffW3 = kOffW2 + kW * kSH * 2;   // 16384
-constexpr int kOffW4 = kOffW3 + kW * kSH * 2;   // 25600
-constexpr int kOffW5 = kOffW4 + kW * kSH * 2;   // 34816
-constexpr int kOffB = kOffW5 + 8 * kSH * 2;     // 35968: b1..b4 [4][64] f32, b5 [8] f32
-constexpr int kOffScale = kOffB + (4 * kW + 8) * 4;  // 37024
-constexpr int kPackedBytes = kOffScale + 16;         // 37040
+constexpr int kOffW2 = kOffW1 + kW * kS1 * 2;
+constexpr int kOffW3 = kOffW2 + kW * kSH * 2;
+constexpr int kOffW4 = kOffW3 + kW * kSH * 2;
+constexpr int kOffW5 = kOffW4 + kW * kSH * 2;
+constexpr int kOffB = kOffW5 + 8 * kSH * 2;          // b1..b4 [4][64] f32, b5 [8] f32
+constexpr int kOffScale = kOffB + (4 * kW + 8) * 4;
+constexpr int kPackedBytes = kOffScale + 16;
 
-// Row stride (bf16) of a feature-record tile in shared memory (112 B rows)
-constexpr int kXS = 56;
+// Row stride (bf16) of a feature-record tile in shared memory (176 B rows)
+constexpr int kXS = kRec + 8;
 
 __host__ __device__ constexpr int fan_in(int l) { return l == 0 ? kIn : kW; }
 __host__ __device__ constexpr int fan_out(int l) { return l == kLayers - 1 ? kOut : kW; }
@@ -161,15 +164,15 @@ struct OutTile {
     float c[4];
 };
 
-// Forward of one 16-row slab: A fragments of the input (3 k-tiles of the
-// 48-wide record) already loaded.  Returns the FP32 output fragment of the
-// final layer (columns 0..2 valid, before the output scale).
-__device__ __forceinline__ OutTile forward_slab(const unsigned char* sw, const uint32_t (&x)[3][4]) {
+// Forward of one 16-row slab: rows row0.. of the record tile x (stride kXS),
+// its kKT k-tiles loaded one at a time.  Returns the FP32 output fragment of
+// the final layer (columns 0..2 valid, before the output scale).
+__device__ __forceinline__ OutTile forward_slab(const unsigned char* sw, const __nv_bfloat16* x, int row0) {
     const int lane = threadIdx.x & 31, t = lane & 3;
     const float* bias = reinterpret_cast<const float*>(sw + kOffB);
     uint32_t a[4][4];
     float acc[8][4];
-    // layer 1: K = 48
+    // layer 1: K = kRec
     {
         const __nv_bfloat16* w = reinterpret_cast<const __nv_bfloat16*>(sw + kOffW1);
 #pragma unroll
@@ -178,14 +181,17 @@ __device__ __forceinline__ OutTile forward_slab(const unsigned char* sw, const u
             acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
         }
 #pragma unroll
-        for (int kt = 0; kt < 3; ++kt)
+        for (int kt = 0; kt < kKT; ++kt) {
+            uint32_t xa[4];
+            load_a(xa, x, kXS, row0, kt * 16);
 #pragma unroll
             for (int np = 0; np < 4; ++np) {
                 uint32_t b[4];
                 load_b_pair(b, w, kS1, np * 16, kt * 16);
-                mma(acc[2 * np], x[kt], b[0], b[1]);
-                mma(acc[2 * np + 1], x[kt], b[2], b[3]);
+                mma(acc[2 * np], xa, b[0], b[1]);
+                mma(acc[2 * np + 1], xa, b[2], b[3]);
             }
+        }
     }
     // layers 2..4: K = 64, A from the previous accumulators
 #pragma unroll 1
@@ -246,10 +252,7 @@ __device__ __forceinline__ void forward_warp(const unsigned char* sw, const __nv
     const float scale = *reinterpret_cast<const float*>(sw + kOffScale);
 #pragma unroll 1
     for (int mt = 0; mt < 2; ++mt) {
-        uint32_t xa[3][4];
-#pragma unroll
-        for (int kt = 0; kt < 3; ++kt) load_a(xa[kt], x, kXS, mt * 16, kt * 16);
-        OutTile o = forward_slab(sw, xa);
+        OutTile o = forward_slab(sw, x, mt * 16);
         if (t < 2) {
             int r = mt * 16 + g;
             int c = 2 * t;

@@ -35,10 +35,10 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const unsigned char* 
     const int tiles = (n + 127) / 128;
     for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
         const int smp = tile * 128 + tid;
-        // the record of sample tid: 48 bf16 = 6 chunks of the A row
+        // the record of sample tid: kRec bf16 = kRec / 8 chunks of the A row
 #pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            uint4 v = smp < n ? __ldg(x + (size_t)smp * 6 + q) : make_uint4(0, 0, 0, 0);
+        for (int q = 0; q < kRec / 8; ++q) {
+            uint4 v = smp < n ? __ldg(x + (size_t)smp * (kRec / 8) + q) : make_uint4(0, 0, 0, 0);
             *reinterpret_cast<uint4*>(s + kTcA + tc05::sw128_offset(tid, q * 8, 128)) = v;
         }
 #pragma unroll 1
@@ -83,8 +83,8 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const unsigned char* 
 // X0, the hidden activations H1..H4 (A operands forward, ReLU masks and dW
 // operands backward), two dZ tiles used in turn, biases and reduction slots.
 constexpr int kGWT = kTcNet;                      // W2^T, W3^T, W4^T, W5^T: [64 in][64 out] each
-constexpr int kGX = kGWT + 4 * kTcWTile;          // X0 [128][64] (48 used)
-constexpr int kGH = kGX + 128 * 128;              // H1..H4 [128][64]
+constexpr int kGX = kGWT + 4 * kTcWTile;          // X0 [128][128] (two tiles, kRec columns used)
+constexpr int kGH = kGX + 2 * kTcABlock;          // H1..H4 [128][64]
 constexpr int kGD = kGH + 4 * 128 * 128;          // D0, D1 [128][64]
 constexpr int kGBias = kGD + 2 * 128 * 128;       // b1..b5 f32, then the output scale
 constexpr int kGSlot = kGBias + 1088;             // [4 warps][64] f32 column sums
@@ -144,8 +144,8 @@ __global__ void __launch_bounds__(128, 1) mlp_grad_tc_kernel(const unsigned char
         for (int i = tid; i < 4 * kW + 8 + 1; i += blockDim.x) sb[i] = __ldg(pb + i);
     }
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        uint4 v = q < 6 && smp >= 0 ? __ldg(x + (size_t)smp * 6 + q) : make_uint4(0, 0, 0, 0);
+    for (int q = 0; q < kRec / 8; ++q) {
+        uint4 v = smp >= 0 ? __ldg(x + (size_t)smp * (kRec / 8) + q) : make_uint4(0, 0, 0, 0);
         *reinterpret_cast<uint4*>(s + kGX + tc05::sw128_offset(tid, q * 8, 128)) = v;
     }
     if (tid == 0) tc05::mbar_init(bar, 1);
@@ -241,8 +241,8 @@ __global__ void __launch_bounds__(128, 1) mlp_grad_tc_kernel(const unsigned char
         sync_for_mma();
         const uint32_t dz = gd(l & 1), hin = gh(l);
         if (l > 0 && tid == 0)
-            tc_mma(tc05::smem_addr(s + dz), tc05::smem_addr(s + kGWT + (l - 1) * kTcWTile), l == 4 ? 1 : 4, 64, tmem,
-                   bar);
+            tc_mma(tc05::smem_addr(s + dz), 0, tc05::smem_addr(s + kGWT + (l - 1) * kTcWTile), 0, l == 4 ? 1 : 4, 64,
+                   tmem, bar);
         // dW[l] on the warp-level tensor path while the tcgen05 product runs
         if (l == 4) {
             float acc[2][4] = {};
@@ -268,15 +268,15 @@ __global__ void __launch_bounds__(128, 1) mlp_grad_tc_kernel(const unsigned char
                 }
             }
         } else {
-            const int fi = fan_in(l), nps = l == 0 ? 3 : 4;
-            float acc[8][4] = {};
+            const int fi = fan_in(l), nps = l == 0 ? kKT : 4;  // 16-column pairs of dW's columns
+            float acc[2 * kKT > 8 ? 2 * kKT : 8][4] = {};
 #pragma unroll 1
             for (int kt = 0; kt < 8; ++kt) {
                 uint32_t a[4];
                 ldsm_x4_t(a, tc05::smem_addr(s + dz + tc05::sw128_offset(kt * 16 + (lane & 7) + ((lane >> 4) << 3),
                                                                          warp * 16 + ((lane >> 3) & 1) * 8, 128)));
 #pragma unroll
-                for (int np = 0; np < 4; ++np) {
+                for (int np = 0; np < (kKT > 4 ? kKT : 4); ++np) {
                     if (np < nps) {
                         uint32_t b[4];
                         ldsm_x4_t(b, tc05::smem_addr(
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(128, 1) mlp_grad_tc_kernel(const unsigned char
                 }
             }
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
+            for (int nt = 0; nt < 2 * (kKT > 4 ? kKT : 4); ++nt) {
                 int c = nt * 8 + 2 * t, r = warp * 16 + g;
                 if (c < fi) {
                     pg[w_offset(l) + r * fi + c] = acc[nt][0];

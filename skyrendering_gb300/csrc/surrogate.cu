@@ -18,17 +18,41 @@
 namespace skyr {
 namespace {
 
-constexpr int kFeat = 42;  // position features per lattice node
+// Feature record layout (skyr_surrogate.h): kRec bf16, kRec / 8 chunks of 16 bytes.
+constexpr int kRecQ = SKYR_MLP_RECORD / 8;  // chunks per record (10)
+constexpr int kSun = 32;                    // samples toward the sun (features 1..32)
+constexpr int kViewNbr = 33;                // features 33..40: view-oriented cube corners (per sample)
+constexpr int kHeight = 41;                 // height in the grid box (lattice)
+constexpr int kCos = 42;                    // cos(view, sun) (per sample)
+constexpr int kFar = 43;                    // transmittance along the view ray to the box's exit (per sample)
+constexpr int kStencil = 44;                // features 44..78: the density stencil (lattice)
+constexpr int kStencilLevels = 5;           // mip levels 2..6
+constexpr int kStencilFirst = 2;
+constexpr int kStencilPoints = 7;           // centre and +-1 along the stencil's three axes
+constexpr int kMipLevels = 6;               // levels 1..6 of the grid, kept in the lattice's buffer
+static_assert(kStencil + kStencilLevels * kStencilPoints + 1 == SKYR_MLP_RECORD, "record layout");
+static_assert(kStencil + kStencilLevels * kStencilPoints == SKYR_MLP_INPUTS, "network inputs");
 constexpr int kMaxSampleTries = 64;
 constexpr int kMaxTrackSteps = 1 << 16;
 
 struct Lattice {
-    const uint4* rec;  // [nodes][6] (48 bf16)
+    const uint4* rec;  // [nodes][kRecQ] (kRec bf16, the per-sample slots zero)
     const float* tau;  // [nodes]
     int nx, ny, nz;
     float3 origin;
     float inv_cell;
     float3 sun;
+};
+
+// Level l (1..6) of the grid's mip chain: each texel the mean of the (up to)
+// 2 x 2 x 2 texels of level l - 1 that exist (ceil sizes), FP16.
+struct MipLevel {
+    const unsigned short* data;
+    int nx, ny, nz;
+    float inv_voxel;
+};
+struct Mips {
+    MipLevel level[kMipLevels + 1];  // [0] is the grid itself
 };
 
 __device__ __forceinline__ float u01(uint32_t& s) {
@@ -58,61 +82,75 @@ struct GridBox {
     float span;  // longest edge
 };
 
-// Trilinear interpolation of the lattice at x: the 42 features (when F) and
-// the optical depth to the sun.
-template <bool FEATURES>
-__device__ __forceinline__ float lattice_at(const Lattice& L, float3 x, float (&f)[kFeat]) {
+// Trilinear between texel centres of a mip level, zero border (grid_sigma's
+// convention), in the grid's units (without the grid's density factor).
+__device__ __forceinline__ float mip_value(const MipLevel& M, float3 origin, float3 p) {
+    float gx = (p.x - origin.x) * M.inv_voxel - 0.5f, gy = (p.y - origin.y) * M.inv_voxel - 0.5f,
+          gz = (p.z - origin.z) * M.inv_voxel - 0.5f;
+    float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
+    float a = gx - fx, b = gy - fy, c = gz - fz;
+    int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
+    auto at = [&](int x, int y, int z) -> float {
+        if ((unsigned)x >= (unsigned)M.nx || (unsigned)y >= (unsigned)M.ny || (unsigned)z >= (unsigned)M.nz)
+            return 0.f;
+        return __half2float(__ushort_as_half(__ldg(M.data + ((size_t)z * M.ny + y) * M.nx + x)));
+    };
+    float r[2];
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz) {
+        float t00 = at(x0, y0, z0 + dz), t10 = at(x0 + 1, y0, z0 + dz);
+        float t01 = at(x0, y0 + 1, z0 + dz), t11 = at(x0 + 1, y0 + 1, z0 + dz);
+        float top = fmaf(a, t10 - t00, t00), bot = fmaf(a, t11 - t01, t01);
+        r[dz] = fmaf(b, bot - top, top);
+    }
+    return fmaf(c, r[1] - r[0], r[0]);
+}
+
+// Level l + 1 texel (x, y, z) from level l: the mean of the texels that exist.
+__global__ void __launch_bounds__(256) mip_reduce_kernel(MipLevel src, MipLevel dst, unsigned short* __restrict__ out) {
+    size_t n = (size_t)dst.nx * dst.ny * dst.nz;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int x = (int)(i % dst.nx), y = (int)((i / dst.nx) % dst.ny), z = (int)(i / ((size_t)dst.nx * dst.ny));
+    float sum = 0.f;
+    int cnt = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        int sx = 2 * x + (c & 1), sy = 2 * y + ((c >> 1) & 1), sz = 2 * z + (c >> 2);
+        if (sx < src.nx && sy < src.ny && sz < src.nz) {
+            sum += __half2float(__ushort_as_half(__ldg(src.data + ((size_t)sz * src.ny + sy) * src.nx + sx)));
+            ++cnt;
+        }
+    }
+    out[i] = __half_as_ushort(__float2half_rn(sum / (float)cnt));
+}
+
+// The lattice's trilinear cell at x: the 8 node indices and weights.
+struct LatticeCell {
+    size_t node[8];
+    float w[8];
+};
+__device__ __forceinline__ void lattice_cell(const Lattice& L, float3 x, LatticeCell& c) {
     float gx = (x.x - L.origin.x) * L.inv_cell, gy = (x.y - L.origin.y) * L.inv_cell,
           gz = (x.z - L.origin.z) * L.inv_cell;
     int ix = min(max((int)floorf(gx), 0), L.nx - 2), iy = min(max((int)floorf(gy), 0), L.ny - 2),
         iz = min(max((int)floorf(gz), 0), L.nz - 2);
     float fx = fminf(fmaxf(gx - ix, 0.f), 1.f), fy = fminf(fmaxf(gy - iy, 0.f), 1.f),
           fz = fminf(fmaxf(gz - iz, 0.f), 1.f);
-    if (FEATURES) {
 #pragma unroll
-        for (int i = 0; i < kFeat; ++i) f[i] = 0.f;
+    for (int k = 0; k < 8; ++k) {
+        int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+        c.w[k] = (dx ? fx : 1.f - fx) * (dy ? fy : 1.f - fy) * (dz ? fz : 1.f - fz);
+        c.node[k] = ((size_t)(iz + dz) * L.ny + (iy + dy)) * L.nx + (ix + dx);
     }
-    float tau = 0.f;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
-        float w = (dx ? fx : 1.f - fx) * (dy ? fy : 1.f - fy) * (dz ? fz : 1.f - fz);
-        size_t node = ((size_t)(iz + dz) * L.ny + (iy + dy)) * L.nx + (ix + dx);
-        tau = fmaf(w, __ldg(L.tau + node), tau);
-        if (FEATURES) {
-#pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                uint4 v = __ldg(L.rec + node * 6 + q);
-                uint32_t u[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    int i = q * 8 + h * 2;
-                    if (i < kFeat) {
-                        __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&u[h]);
-                        f[i] = fmaf(w, __low2float(b), f[i]);
-                        if (i + 1 < kFeat) f[i + 1] = fmaf(w, __high2float(b), f[i + 1]);
-                    }
-                }
-            }
-        }
-    }
-    return tau;
 }
 
-// record of a sample (features + cos(view, sun)) as 6 x 16 bytes
-__device__ __forceinline__ void store_record(uint4* dst, const float (&f)[kFeat], float mu) {
+// The optical depth to the sun at x, interpolated from the lattice.
+__device__ __forceinline__ float lattice_tau(const Lattice& L, const LatticeCell& c) {
+    float tau = 0.f;
 #pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        uint32_t u[4];
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-            int i = q * 8 + h * 2;
-            float a = i < kFeat ? f[i] : (i == kFeat ? mu : 0.f);
-            float b = i + 1 < kFeat ? f[i + 1] : (i + 1 == kFeat ? mu : 0.f);
-            u[h] = mlp::pack_bf16(a, b);
-        }
-        dst[q] = make_uint4(u[0], u[1], u[2], u[3]);
-    }
+    for (int k = 0; k < 8; ++k) tau = fmaf(c.w[k], __ldg(L.tau + c.node[k]), tau);
+    return tau;
 }
 
 // Features 33..40: extinction / sigma_ref at the 8 corners of a cube whose
@@ -121,7 +159,7 @@ __device__ __forceinline__ void store_record(uint4* dst, const float (&f)[kFeat]
 // parallel), w = v x u.  Corner j takes +dist/sqrt(3) along v, u, w where bit
 // 0, 1, 2 of j is set, -dist/sqrt(3) where it is not.
 __device__ __forceinline__ void view_neighbours(const PtConsts& P, float3 x, float3 v, float3 sun, float dist,
-                                                float inv_ref, float (&f)[kFeat]) {
+                                                float inv_ref, float (&nb)[8]) {
     float3 u = sun - v * dot3(v, sun);
     float l2 = dot3(u, u);
     if (l2 < 1e-8f) {
@@ -135,19 +173,68 @@ __device__ __forceinline__ void view_neighbours(const PtConsts& P, float3 x, flo
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         float3 o = v * ((j & 1) ? r : -r) + u * ((j & 2) ? r : -r) + w * ((j & 4) ? r : -r);
-        f[33 + j] = grid_sigma(P, x + o) * inv_ref;
+        nb[j] = grid_sigma(P, x + o) * inv_ref;
     }
 }
 
+// The feature record of a sample at x seen along v: the lattice's features
+// interpolated trilinearly chunk by chunk, with the per-sample slots filled in
+// (the view neighbours, cos(v, sun), the far-side transmittance `far_t`),
+// written as kRecQ 16-byte chunks to `row`.  Returns the sun optical depth;
+// f0 / near_sun receive feature 0 and the mean of features 1..8 (the error
+// table's bin).
+__device__ __forceinline__ float write_record(const Lattice& L, const PtConsts& P, float3 x, float3 v, float nbr,
+                                              float inv_ref, float far_t, uint4* row, float& f0, float& near_sun) {
+    LatticeCell c;
+    lattice_cell(L, x, c);
+    const float tau = lattice_tau(L, c);
+    float nb[8];
+    view_neighbours(P, x, v, L.sun, nbr, inv_ref, nb);
+    const float mu = dot3(v, L.sun);
+    float near = 0.f;
+#pragma unroll
+    for (int q = 0; q < kRecQ; ++q) {
+        float a[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) a[e] = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            uint4 u = __ldg(L.rec + c.node[k] * kRecQ + q);
+            uint32_t w4[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&w4[h]);
+                a[2 * h] = fmaf(c.w[k], __low2float(b), a[2 * h]);
+                a[2 * h + 1] = fmaf(c.w[k], __high2float(b), a[2 * h + 1]);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int i = q * 8 + e;
+            if (i >= kViewNbr && i < kViewNbr + 8) a[e] = nb[i - kViewNbr];
+            if (i == kCos) a[e] = mu;
+            if (i == kFar) a[e] = far_t;
+            if (i == 0) f0 = a[e];
+            if (i >= 1 && i <= 8) near += a[e];
+        }
+        row[q] = make_uint4(mlp::pack_bf16(a[0], a[1]), mlp::pack_bf16(a[2], a[3]), mlp::pack_bf16(a[4], a[5]),
+                            mlp::pack_bf16(a[6], a[7]));
+    }
+    near_sun = near * 0.125f;
+    return tau;
+}
+
 struct LatticeBuild {
-    float dist[32];  // sun sample distances
-    float nbr;       // neighbour radius
+    float dist[kSun];  // sun sample distances
+    float nbr;         // neighbour radius
     float inv_sigma_ref;
-    float step;      // sun optical-depth march step
+    float step;        // sun optical-depth march step
+    float3 axis[3];    // the stencil's axes: the sun, then two perpendiculars
+    float spacing[kStencilLevels];  // stencil step at each level: 2 texels of the level
 };
 
 __global__ void __launch_bounds__(128) feature_lattice_kernel(PtConsts P, GridBox B, Lattice L, LatticeBuild Q,
-                                                              int stride, uint4* __restrict__ rec,
+                                                              Mips M, int stride, uint4* __restrict__ rec,
                                                               float* __restrict__ tau) {
     size_t n = (size_t)L.nx * L.ny * L.nz;
     size_t node = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -155,15 +242,35 @@ __global__ void __launch_bounds__(128) feature_lattice_kernel(PtConsts P, GridBo
     int ix = (int)(node % L.nx), iy = (int)((node / L.nx) % L.ny), iz = (int)(node / ((size_t)L.nx * L.ny));
     float cell = 1.f / L.inv_cell;
     float3 x = f3(L.origin.x + ix * cell, L.origin.y + iy * cell, L.origin.z + iz * cell);
-    float f[kFeat];
-    f[0] = grid_sigma(P, x) * Q.inv_sigma_ref;
-#pragma unroll 4
-    for (int k = 0; k < 32; ++k) f[1 + k] = grid_sigma(P, x + L.sun * Q.dist[k]) * Q.inv_sigma_ref;
-    // features 33..40 depend on the view direction: filled per sample (view_neighbours)
+    // chunk by chunk: the features of positions q * 8 .. q * 8 + 7
+    const float k_ref = Q.inv_sigma_ref * P.density;
+#pragma unroll 1
+    for (int q = 0; q < kRecQ; ++q) {
+        float a[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) f[33 + j] = 0.f;
-    f[41] = fminf(fmaxf((x.z - B.lo.z) / (B.hi.z - B.lo.z), 0.f), 1.f);
-    store_record(rec + node * 6, f, 0.f);
+        for (int e = 0; e < 8; ++e) {
+            const int i = q * 8 + e;
+            float v = 0.f;  // the per-sample slots (view neighbours, cos, far side) and the pad stay zero
+            if (i == 0) {
+                v = grid_sigma(P, x) * Q.inv_sigma_ref;
+            } else if (i <= kSun) {
+                v = grid_sigma(P, x + L.sun * Q.dist[i - 1]) * Q.inv_sigma_ref;
+            } else if (i == kHeight) {
+                v = fminf(fmaxf((x.z - B.lo.z) / (B.hi.z - B.lo.z), 0.f), 1.f);
+            } else if (i >= kStencil && i < kStencil + kStencilLevels * kStencilPoints) {
+                const int s = i - kStencil, lv = s / kStencilPoints, j = s % kStencilPoints;
+                float3 p = x;
+                if (j > 0) {
+                    const float h = (j & 1) ? Q.spacing[lv] : -Q.spacing[lv];
+                    p = x + Q.axis[(j - 1) >> 1] * h;
+                }
+                v = mip_value(M.level[kStencilFirst + lv], P.origin, p) * k_ref;
+            }
+            a[e] = v;
+        }
+        rec[node * kRecQ + q] = make_uint4(mlp::pack_bf16(a[0], a[1]), mlp::pack_bf16(a[2], a[3]),
+                                           mlp::pack_bf16(a[4], a[5]), mlp::pack_bf16(a[6], a[7]));
+    }
     // optical depth to the sun: midpoint rule to the exit of the grid box
     float t0, t1;
     box_hit(B.lo, B.hi, x, L.sun, t0, t1);
@@ -175,6 +282,22 @@ __global__ void __launch_bounds__(128) feature_lattice_kernel(PtConsts P, GridBo
         od *= h;
     }
     tau[node] = od;
+}
+
+// Transmittance from x along d to the exit of the grid box: midpoint rule at
+// steps of at most `step` (the training records' far-side feature).
+__device__ __forceinline__ float far_transmittance(const PtConsts& P, const GridBox& B, float3 x, float3 d,
+                                                   float step) {
+    float t0, t1;
+    box_hit(B.lo, B.hi, x, d, t0, t1);
+    float od = 0.f;
+    if (t1 > 0.f) {
+        int steps = min((int)ceilf(t1 / step), kMaxTrackSteps);
+        float h = t1 / (float)max(steps, 1);
+        for (int s = 0; s < steps; ++s) od += grid_sigma(P, x + d * ((s + 0.5f) * h));
+        od *= h;
+    }
+    return __expf(-od);
 }
 
 __global__ void __launch_bounds__(128) sample_points_kernel(PtConsts P, GridBox B, float sigma_max, float sigma_min,
@@ -220,16 +343,23 @@ __global__ void __launch_bounds__(128) sample_points_kernel(PtConsts P, GridBox 
     o6[3] = d.x; o6[4] = d.y; o6[5] = d.z;
 }
 
-__global__ void __launch_bounds__(128) records_kernel(Lattice L, PtConsts P, float nbr, float inv_ref,
-                                                      const float* __restrict__ pts, int n, uint4* __restrict__ rec) {
+__global__ void __launch_bounds__(128) records_kernel(Lattice L, PtConsts P, GridBox B, float nbr, float inv_ref,
+                                                      float far_step, const float* __restrict__ pts, int n,
+                                                      uint4* __restrict__ rec) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* q = pts + 6 * (size_t)i;
     float3 x = f3(q[0], q[1], q[2]), d = f3(q[3], q[4], q[5]);
-    float f[kFeat];
-    lattice_at<true>(L, x, f);
-    view_neighbours(P, x, d, L.sun, nbr, inv_ref, f);
-    store_record(rec + (size_t)i * 6, f, dot3(d, L.sun));
+    float f0, near_sun;
+    write_record(L, P, x, d, nbr, inv_ref, far_transmittance(P, B, x, d, far_step), rec + (size_t)i * kRecQ, f0,
+                 near_sun);
+}
+
+// Sample s of the surrogate raymarch: t = t0 + (s + jitter) dt along dir from o
+// (explicit fused operations, so that both loops that visit it agree bit for bit).
+__device__ __forceinline__ float3 march_point(float3 o, float3 dir, float t0, float dt, float jitter, int s) {
+    const float t = fmaf((float)s + jitter, dt, t0);
+    return f3(fmaf(dir.x, t, o.x), fmaf(dir.y, t, o.y), fmaf(dir.z, t, o.z));
 }
 
 struct RenderConsts {
@@ -259,13 +389,13 @@ __global__ void __launch_bounds__(256) error_bins_kernel(const __nv_bfloat16* __
     bins[i] = error_bin(__bfloat162float(r[0]), s * 0.125f);
 }
 
-constexpr int kRenderWarps = 4;
+constexpr int kRenderWarps = 8;              // 2 blocks per SM: one network copy for 8 warps
 constexpr int kSmTile = 32 * mlp::kXS * 2;    // records of one warp
 constexpr int kSmOut = 32 * 4 * 4;            // network outputs of one warp
 constexpr int kSmRender = mlp::kPackedBytes + kRenderWarps * (kSmTile + kSmOut);
 
 template <class S>
-__global__ void __launch_bounds__(128, 4) surrogate_render_kernel(CloudConsts C, AtmoConsts A, PtConsts P, Lattice L,
+__global__ void __launch_bounds__(32 * kRenderWarps, 2) surrogate_render_kernel(CloudConsts C, AtmoConsts A, PtConsts P, Lattice L,
                                                                   RenderConsts R, const float4* __restrict__ tlut,
                                                                   int tw, int th, const S* __restrict__ apl,
                                                                   const S* __restrict__ apt,
@@ -296,31 +426,34 @@ __global__ void __launch_bounds__(128, 4) surrogate_render_kernel(CloudConsts C,
     float T = 1.f, err = 0.f, wsum = 0.f, wt = 0.f;
     float3 Lum = f3(0.f);
     uint4* row = reinterpret_cast<uint4*>(tile + lane * mlp::kXS);
+    // the ray's optical depth through the region at the march's own samples:
+    // the far-side feature of sample s is what remains of it past the sample
+    float tau_total = 0.f;
+    if (R.use_network && hit) {
+        for (int s = 0; s < R.steps; ++s) tau_total += grid_sigma(P, march_point(C.cam, dir, t0, dt, jitter, s));
+        tau_total *= dt;
+    }
+    float run = 0.f;  // optical depth up to and including the current sample
     for (int s = 0; s < R.steps; ++s) {
         bool live = hit && T > R.min_t;
         if (!__any_sync(full, live)) break;
-        float t = t0 + ((float)s + jitter) * dt;
-        float3 x = C.cam + dir * t;
+        float t = fmaf((float)s + jitter, dt, t0);
+        float3 x = march_point(C.cam, dir, t0, dt, jitter, s);
         float sigma = live ? grid_sigma(P, x) : 0.f;
+        run = fmaf(sigma, dt, run);
         bool need = live && sigma > 0.f;
         if (!__any_sync(full, need)) continue;
         float tau = 0.f, rel_err = R.network_error;
         float3 ms = f3(0.f);
         if (R.use_network) {
             if (need) {
-                float f[kFeat];
-                tau = lattice_at<true>(L, x, f);
-                view_neighbours(P, x, dir, C.sun, R.nbr, R.inv_ref, f);
-                store_record(row, f, mu);
-                if (R.error_table) {
-                    float near_sun = 0.f;
-#pragma unroll
-                    for (int k = 1; k <= 8; ++k) near_sun += f[k];
-                    rel_err = __ldg(R.error_table + error_bin(f[0], near_sun * 0.125f));
-                }
+                const float far_t = __expf(-fmaxf(tau_total - run + 0.5f * sigma * dt, 0.f));
+                float f0, near_sun;
+                tau = write_record(L, P, x, dir, R.nbr, R.inv_ref, far_t, row, f0, near_sun);
+                if (R.error_table) rel_err = __ldg(R.error_table + error_bin(f0, near_sun));
             } else {
 #pragma unroll
-                for (int q = 0; q < 6; ++q) row[q] = make_uint4(0, 0, 0, 0);
+                for (int q = 0; q < kRecQ; ++q) row[q] = make_uint4(0, 0, 0, 0);
             }
             __syncwarp();
             mlp::forward_warp(sm, tile, yout);
@@ -328,8 +461,9 @@ __global__ void __launch_bounds__(128, 4) surrogate_render_kernel(CloudConsts C,
             ms = f3(fmaxf(yout[lane * 4], 0.f), fmaxf(yout[lane * 4 + 1], 0.f), fmaxf(yout[lane * 4 + 2], 0.f));
             __syncwarp();
         } else if (need) {
-            float f[kFeat];
-            tau = lattice_at<false>(L, x, f);
+            LatticeCell c;
+            lattice_cell(L, x, c);
+            tau = lattice_tau(L, c);
         }
         if (need) {
             float3 ss = sun_illuminance(C, A, tlut, tw, th, x) * (ph * __expf(-tau));
@@ -388,6 +522,28 @@ int grid_setup(const skyr_density_grid* grid, PtConsts& P, GridBox& B) {
     return SKYR_OK;
 }
 
+// Bytes of a lattice of `nodes` nodes over `grid`: the records, the sun optical
+// depths, then the grid's mip levels 1..kMipLevels (each 256-byte aligned).
+// With M: the levels' sizes, texel sizes and byte offsets from the buffer's
+// start (in data), level 0 being the grid itself.
+size_t lattice_bytes(const skyr_density_grid* grid, size_t nodes, Mips* M) {
+    size_t off = nodes * (kRecQ * 16 + 4);
+    int nx = grid->nx, ny = grid->ny, nz = grid->nz;
+    if (M) {
+        M->level[0] = MipLevel{reinterpret_cast<const unsigned short*>(grid->data), nx, ny, nz,
+                               1.f / grid->voxel_size};
+    }
+    for (int l = 1; l <= kMipLevels; ++l) {
+        off = (off + 255) & ~(size_t)255;
+        nx = (nx + 1) / 2, ny = (ny + 1) / 2, nz = (nz + 1) / 2;
+        if (M)
+            M->level[l] = MipLevel{reinterpret_cast<const unsigned short*>(off), nx, ny, nz,
+                                   1.f / (grid->voxel_size * (float)(1 << l))};
+        off += (size_t)nx * ny * nz * 2;
+    }
+    return off;
+}
+
 int lattice_setup(const skyr_density_grid* grid, const skyr_feature_volume* fv, Lattice& L) {
     if (!fv || !fv->data) return set_error(SKYR_EINVAL, "null feature lattice");
     if (fv->stride < 1 || fv->nx < 2 || fv->ny < 2 || fv->nz < 2)
@@ -398,7 +554,7 @@ int lattice_setup(const skyr_density_grid* grid, const skyr_feature_volume* fv, 
     if (reinterpret_cast<uintptr_t>(fv->data) & 15) return set_error(SKYR_EINVAL, "feature lattice must be 16-byte aligned");
     size_t nodes = (size_t)fv->nx * fv->ny * fv->nz;
     L.rec = reinterpret_cast<const uint4*>(fv->data);
-    L.tau = reinterpret_cast<const float*>(reinterpret_cast<const unsigned char*>(fv->data) + nodes * 96);
+    L.tau = reinterpret_cast<const float*>(reinterpret_cast<const unsigned char*>(fv->data) + nodes * kRecQ * 16);
     L.nx = fv->nx;
     L.ny = fv->ny;
     L.nz = fv->nz;
@@ -446,7 +602,7 @@ size_t skyr_feature_volume_bytes(const skyr_density_grid* grid, int stride, skyr
         fv->ny = ny;
         fv->nz = nz;
     }
-    return (size_t)nx * ny * nz * (96 + 4);
+    return lattice_bytes(grid, (size_t)nx * ny * nz, nullptr);
 }
 
 int skyr_feature_volume_build(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
@@ -470,14 +626,45 @@ int skyr_feature_volume_build(skyr_ctx* ctx, const skyr_atmosphere_parameters* a
     Lattice L;
     if (int e = lattice_setup(grid, fv, L)) return e;
     LatticeBuild Q;
-    for (int k = 0; k < 32; ++k) Q.dist[k] = B.span * 0.01f * (float)std::pow(1000.0, k / 31.0);
+    for (int k = 0; k < kSun; ++k) Q.dist[k] = B.span * 0.01f * (float)std::pow(1000.0, k / 31.0);
     Q.nbr = 0.1f * B.span;
     Q.inv_sigma_ref = 1.f / fv->sigma_ref;
     Q.step = 0.5f * grid->voxel_size;
+    // the stencil's axes: the sun, its perpendicular in the horizontal plane
+    // (sun x z; sun x x when the sun is at the zenith), and their cross product
+    {
+        double e1[3] = {C.sun.x, C.sun.y, C.sun.z};
+        double n1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+        for (double& v : e1) v /= n1;
+        double e2[3] = {e1[1], -e1[0], 0.0};  // e1 x z
+        double n2 = std::sqrt(e2[0] * e2[0] + e2[1] * e2[1]);
+        if (n2 < 1e-3) {
+            e2[0] = 0.0, e2[1] = e1[2], e2[2] = -e1[1];  // e1 x x
+            n2 = std::sqrt(e2[1] * e2[1] + e2[2] * e2[2]);
+        }
+        for (double& v : e2) v /= n2;
+        double e3[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        Q.axis[0] = make_float3((float)e1[0], (float)e1[1], (float)e1[2]);
+        Q.axis[1] = make_float3((float)e2[0], (float)e2[1], (float)e2[2]);
+        Q.axis[2] = make_float3((float)e3[0], (float)e3[1], (float)e3[2]);
+    }
+    for (int l = 0; l < kStencilLevels; ++l)
+        Q.spacing[l] = grid->voxel_size * (float)(2 << (kStencilFirst + l));
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    // the mip chain of the grid, in the lattice's buffer after the optical depths
+    Mips M;
     size_t nodes = (size_t)L.nx * L.ny * L.nz;
+    lattice_bytes(grid, nodes, &M);
+    unsigned char* base = reinterpret_cast<unsigned char*>(fv->data);
+    for (int l = 1; l <= kMipLevels; ++l) {
+        M.level[l].data = reinterpret_cast<const unsigned short*>(base + reinterpret_cast<size_t>(M.level[l].data));
+        size_t n = (size_t)M.level[l].nx * M.level[l].ny * M.level[l].nz;
+        mip_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+            M.level[l - 1], M.level[l], const_cast<unsigned short*>(M.level[l].data));
+        if (int e = check_cuda(cudaGetLastError(), "mip reduce kernel")) return e;
+    }
     feature_lattice_kernel<<<(unsigned)((nodes + 127) / 128), 128, 0, ctx->stream>>>(
-        P, B, L, Q, fv->stride, reinterpret_cast<uint4*>(fv->data), const_cast<float*>(L.tau));
+        P, B, L, Q, M, fv->stride, reinterpret_cast<uint4*>(fv->data), const_cast<float*>(L.tau));
     return check_cuda(cudaGetLastError(), "feature lattice kernel");
 }
 
@@ -509,7 +696,8 @@ int skyr_surrogate_records(skyr_ctx* ctx, const skyr_density_grid* grid, const s
     if (int e = lattice_setup(grid, fv, L)) return e;
     if (n == 0) return SKYR_OK;
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
-    records_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(L, P, 0.1f * B.span, 1.f / fv->sigma_ref, points, n,
+    records_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(L, P, B, 0.1f * B.span, 1.f / fv->sigma_ref,
+                                                           0.5f * grid->voxel_size, points, n,
                                                            reinterpret_cast<uint4*>(records));
     return check_cuda(cudaGetLastError(), "records kernel");
 }

@@ -1,7 +1,7 @@
 """Host side of the surrogate network (include/skyr_mlp.h): parameter init,
 feature records, the packed network, inference, gradients and the trainer.
 
-The network (43 -> 64 -> 64 -> 64 -> 64 -> 3, ReLU, BF16 weights, FP32
+The network (79 -> 64 -> 64 -> 64 -> 64 -> 3, ReLU, BF16 weights, FP32
 accumulation) has no counterpart in the reference; it stands in for the
 multiple-scattering heuristic of VolumetricCloudRender.comp:125-130.
 """
@@ -40,7 +40,7 @@ def hparams(**kw) -> _abi.MlpHparams:
 
 
 def to_records(x: torch.Tensor) -> torch.Tensor:
-    """[n][43] features -> [n][48] bf16 records on the GPU (5 zero pads)."""
+    """[n][INPUTS] features -> [n][RECORD] bf16 records on the GPU (zero pads)."""
     n = x.shape[0]
     r = torch.zeros((n, RECORD), dtype=torch.bfloat16, device="cuda")
     r[:, :INPUTS] = x.to(device="cuda", dtype=torch.bfloat16)
@@ -48,13 +48,13 @@ def to_records(x: torch.Tensor) -> torch.Tensor:
 
 
 def records_to_numpy(rec: torch.Tensor) -> np.ndarray:
-    """bf16 records -> the float32 [n][43] features they hold exactly."""
+    """bf16 records -> the float32 [n][INPUTS] features they hold exactly."""
     return rec[:, :INPUTS].float().cpu().numpy()
 
 
 def _check_records(rec: torch.Tensor):
     if rec.dtype != torch.bfloat16 or rec.dim() != 2 or rec.shape[1] != RECORD or not rec.is_contiguous():
-        raise ValueError("records must be a contiguous [n][48] bfloat16 CUDA tensor")
+        raise ValueError(f"records must be a contiguous [n][{RECORD}] bfloat16 CUDA tensor")
 
 
 class PackedMLP:
@@ -68,6 +68,8 @@ class PackedMLP:
     def from_params(cls, ctx: Context, params, out_scale: float = 1.0) -> "PackedMLP":
         m = cls(ctx)
         p = torch.as_tensor(np.asarray(params, dtype=np.float32)).cuda() if not torch.is_tensor(params) else params
+        if p.dtype != torch.float32 or p.numel() != PARAMS or not p.is_cuda:
+            raise ValueError(f"parameters must be {PARAMS} FP32 values on the GPU (got {p.numel()} {p.dtype})")
         m._params = p.contiguous()
         _abi.call("skyr_mlp_pack", ctx.handle, _ptr(m._params), C.c_float(out_scale), _ptr(m.buf))
         return m
@@ -80,7 +82,7 @@ class PackedMLP:
 
 
 def gradient(ctx: Context, packed: PackedMLP, h: _abi.MlpHparams, rec: torch.Tensor, targets: torch.Tensor):
-    """(gradient[15491] FP32, loss) of the mean relative-L2 loss on one batch."""
+    """(gradient[PARAMS] FP32, loss) of the mean relative-L2 loss on one batch."""
     _check_records(rec)
     t = targets.contiguous().float()
     g = torch.empty(PARAMS, dtype=torch.float32, device="cuda")

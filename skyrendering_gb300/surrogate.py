@@ -16,7 +16,7 @@ from pathlib import Path
 import numpy as np
 import torch
 
-from . import _abi
+from . import _abi, mlp
 from .atmosphere import Context, LutSet, _ptr
 from .mlp import RECORD, PackedMLP
 from .pathtrace import DensityGrid
@@ -187,6 +187,8 @@ class Model:
 
 def load_model(path) -> Model:
     d = np.load(path, allow_pickle=False)
+    if d["params"].size != mlp.PARAMS:
+        raise ValueError(f"{path}: a network of {d['params'].size} parameters, this build's has {mlp.PARAMS}")
     table = d["error_table"] if "error_table" in d.files else np.full(BINS * BINS, float(d["network_error"]),
                                                                         np.float32)
     return Model(d["params"], float(d["label_scale"]), float(d["network_error"]), table, str(d["meta"]))

@@ -10,11 +10,12 @@ import pytest
 
 from oracle import oracle as orc
 
-P = 15491
+IN = 79  # the network's inputs (include/skyr_mlp.h)
+P = 17795
 
 
 def _layer_slices():
-    fan = [(43, 64), (64, 64), (64, 64), (64, 64), (64, 3)]
+    fan = [(IN, 64), (64, 64), (64, 64), (64, 64), (64, 3)]
     out, o = [], 0
     for fi, fo in fan:
         out.append(("W", o, o + fi * fo))
@@ -36,7 +37,7 @@ def test_oracle_gradient_matches_finite_differences():
     unit direction) is small enough that no pre-activation changes sign."""
     rng = np.random.default_rng(3)
     p = _params(1)
-    x = rng.random((16, 43)).astype(np.float32)
+    x = rng.random((16, IN)).astype(np.float32)
     t = rng.random((16, 3)).astype(np.float32)
     eps = 1e8
     _, g = orc.mlp_gradient(p, x, t, loss_eps=eps, mirror=False)
@@ -59,7 +60,7 @@ def test_oracle_gradient_matches_finite_differences():
 def test_oracle_loss_definition():
     rng = np.random.default_rng(4)
     p = _params(2)
-    x = rng.random((5, 43)).astype(np.float32)
+    x = rng.random((5, IN)).astype(np.float32)
     t = rng.random((5, 3)).astype(np.float32)
     y = orc.mlp_predict(p, x, mirror=False)
     loss, _ = orc.mlp_gradient(p, x, t, label_scale=2.0, loss_eps=0.3, mirror=False)
@@ -71,7 +72,7 @@ def test_oracle_loss_definition():
 def test_oracle_bf16_mirror_is_close_to_fp64():
     rng = np.random.default_rng(5)
     p = _params(3, 0.15)
-    x = rng.random((64, 43)).astype(np.float32)
+    x = rng.random((64, IN)).astype(np.float32)
     y64 = orc.mlp_predict(p, x, mirror=False)
     y16 = orc.mlp_predict(p, x, mirror=True)
     rms = np.sqrt(np.mean(y64 ** 2))
@@ -98,7 +99,7 @@ def test_init_params_he_uniform():
         if kind == "b":
             assert np.all(seg == 0)
         else:
-            fan_in = 43 if a == 0 else 64
+            fan_in = IN if a == 0 else 64
             bound = np.sqrt(6.0 / fan_in)
             assert np.max(np.abs(seg)) <= bound
             assert np.std(seg) == pytest.approx(bound / np.sqrt(3.0), rel=0.1)

@@ -24,10 +24,11 @@ from skyrendering_gb300.atmosphere import _ptr
 
 pytestmark = pytest.mark.gpu
 P = mlp.PARAMS
+IN = mlp.INPUTS
 
 
 def _blocks():
-    fan = [(43, 64), (64, 64), (64, 64), (64, 64), (64, 3)]
+    fan = [(IN, 64), (64, 64), (64, 64), (64, 64), (64, 3)]
     out, o = [], 0
     for li, (fi, fo) in enumerate(fan):
         out.append((f"W{li + 1}", o, o + fi * fo))
@@ -39,7 +40,7 @@ def _blocks():
 
 def _data(n, seed):
     rng = np.random.default_rng(seed)
-    x = rng.random((n, 43)).astype(np.float32)
+    x = rng.random((n, IN)).astype(np.float32)
     rec = mlp.to_records(torch.from_numpy(x))
     xb = mlp.records_to_numpy(rec)  # the bf16 values the GPU sees
     t = (0.5 + rng.random((n, 3))).astype(np.float32)
@@ -216,7 +217,7 @@ def test_adam_step_matches_oracle(ctx):
 def test_training_reduces_loss(ctx):
     rng = np.random.default_rng(51)
     n = 16384
-    x = rng.random((n, 43)).astype(np.float32)
+    x = rng.random((n, IN)).astype(np.float32)
     # a smooth positive target of a few inputs
     t = np.stack([0.5 + x[:, 0] * x[:, 1], 1.0 + np.sin(3 * x[:, 2]) * 0.5, 0.2 + x[:, 3:8].mean(1)], 1)
     t = t.astype(np.float32)

@@ -11,7 +11,7 @@
   the committed network (BF16 rounding points mirrored): mean relative error
   of the luminance <= 1e-3, transmittance 1e-5;
 * accuracy: on the 512x640x352 evaluation cloud at 128^2 the network image is
-  within 8 % relative L1 of a 8192-spp path-traced reference while single
+  within 5 % relative L1 of a 8192-spp path-traced reference while single
   scattering alone is >= 80 % off (what the trained network gains).
 """
 import ctypes as C
@@ -73,14 +73,71 @@ def _view_neighbours(grid, x, v, sun, sigma_ref):
     return sig / sigma_ref
 
 
+REC = mlp.RECORD  # 80 bf16: features 0..78 (skyr_surrogate.h), then a zero
+
+
+def _mips(data, levels=6):
+    """The grid's mip chain in FP64: each texel the mean of the existing texels
+    of the 2 x 2 x 2 block below it (ceil sizes), level 0 the grid."""
+    out = [np.asarray(data, dtype=np.float64)]
+    for _ in range(levels):
+        a = out[-1]
+        nz, ny, nx = a.shape
+        p = np.full(((nz + 1) // 2 * 2, (ny + 1) // 2 * 2, (nx + 1) // 2 * 2), np.nan)
+        p[:nz, :ny, :nx] = a
+        b = p.reshape(p.shape[0] // 2, 2, p.shape[1] // 2, 2, p.shape[2] // 2, 2)
+        out.append(np.nanmean(b, axis=(1, 3, 5)))
+    return out
+
+
+def _trilinear_zero(vol, origin, voxel, pts):
+    """Trilinear between texel centres with a zero border (the grid lookups' convention)."""
+    g = (pts - origin) / voxel - 0.5
+    f0 = np.floor(g).astype(int)
+    fr = g - f0
+    nz, ny, nx = vol.shape
+    out = np.zeros(len(pts))
+    for c in range(8):
+        d = np.array([c & 1, (c >> 1) & 1, c >> 2])
+        i = f0 + d
+        w = np.prod(np.where(d, fr, 1 - fr), 1)
+        ok = (i[:, 0] >= 0) & (i[:, 0] < nx) & (i[:, 1] >= 0) & (i[:, 1] < ny) & (i[:, 2] >= 0) & (i[:, 2] < nz)
+        v = np.zeros(len(pts))
+        v[ok] = vol[i[ok, 2], i[ok, 1], i[ok, 0]]
+        out += w * v
+    return out
+
+
+def _stencil(grid, x, sun, sigma_ref):
+    """Features 44..78: the density stencil at mip levels 2..6, centre and +-2 texels
+    of the level along the sun, its horizontal perpendicular (sun x z) and their cross."""
+    g = grid.struct
+    e1 = sun / np.linalg.norm(sun)
+    e2 = np.array([e1[1], -e1[0], 0.0])
+    if np.linalg.norm(e2) < 1e-3:
+        e2 = np.array([0.0, e1[2], -e1[1]])
+    e2 /= np.linalg.norm(e2)
+    e3 = np.cross(e1, e2)
+    axes = [e1, e2, e3]
+    mips = _mips(grid.data.float().cpu().numpy())
+    org = np.array(g.origin[:], dtype=np.float64)
+    cols = []
+    for lv in range(2, 7):
+        h = g.voxel_size * 2 ** (lv + 1)
+        for j in range(7):
+            p = x if j == 0 else x + axes[(j - 1) >> 1] * (h if j & 1 else -h)
+            cols.append(_trilinear_zero(mips[lv], org, g.voxel_size * 2 ** lv, p) * g.density / sigma_ref)
+    return np.stack(cols, 1)
+
+
 def test_lattice_matches_oracle(small):
     sc, grid, fv = small
     g = grid.struct
     raw = fv.buf.cpu().numpy()
     st = fv.struct
     nodes = st.nx * st.ny * st.nz
-    rec = raw[: nodes * 96].view(np.uint16).reshape(nodes, 48)
-    tau = raw[nodes * 96: nodes * 100].view(np.float32)
+    rec = raw[: nodes * REC * 2].view(np.uint16).reshape(nodes, REC)
+    tau = raw[nodes * REC * 2: nodes * (REC * 2 + 4)].view(np.float32)
     data = grid.data.cpu().numpy()
     rng = np.random.default_rng(1)
     idx = rng.choice(nodes, 48, replace=False)
@@ -101,7 +158,11 @@ def test_lattice_matches_oracle(small):
     got = rec[idx, :42].astype(np.uint32) << 16
     got = got.view(np.float32)
     np.testing.assert_allclose(got, _bf16(feat), rtol=1e-2, atol=1e-3)
-    assert np.all(rec[idx, 42:] == 0)
+    # the per-sample slots (cos, far side) and the pad stay zero
+    assert np.all(rec[idx, 42:44] == 0) and np.all(rec[idx, REC - 1] == 0)
+    # the stencil over the mip chain (the GPU's levels are FP16)
+    got_s = (rec[idx, 44:79].astype(np.uint32) << 16).view(np.float32)
+    np.testing.assert_allclose(got_s, _bf16(_stencil(grid, x, sun, st.sigma_ref)), rtol=1e-2, atol=2e-3)
     # optical depth to the sun: midpoint rule at half a voxel to the box exit
     t1 = _box_exit(org, hi, x, sun[None, :])
     for n, node in enumerate(idx):
@@ -118,14 +179,14 @@ def test_records_interpolate_lattice(ctx, small):
     st = fv.struct
     nodes = st.nx * st.ny * st.nz
     raw = fv.buf.cpu().numpy()
-    lat = (raw[: nodes * 96].view(np.uint16).reshape(nodes, 48).astype(np.uint32) << 16).view(np.float32)
+    lat = (raw[: nodes * REC * 2].view(np.uint16).reshape(nodes, REC).astype(np.uint32) << 16).view(np.float32)
     p = pts.cpu().numpy().astype(np.float64)
     g = grid.struct
     q = (p[:, :3] - np.array(g.origin[:])) / (g.voxel_size * st.stride)
     n3 = np.array([st.nx, st.ny, st.nz])
     i0 = np.clip(np.floor(q).astype(int), 0, n3 - 2)
     fr = np.clip(q - i0, 0, 1)
-    f = np.zeros((len(p), 48))
+    f = np.zeros((len(p), REC))
     for c in range(8):
         d = np.array([c & 1, (c >> 1) & 1, c >> 2])
         w = np.prod(np.where(d, fr, 1 - fr), 1)
@@ -134,6 +195,16 @@ def test_records_interpolate_lattice(ctx, small):
     sun = np.array(st.sun[:], dtype=np.float64)
     f[:, 42] = p[:, 3:] @ sun
     f[:, 33:41] = _view_neighbours(grid, p[:, :3], p[:, 3:], sun, st.sigma_ref)
+    # far side: transmittance along the view direction to the box's exit (midpoint, half-voxel steps)
+    org = np.array(g.origin[:], dtype=np.float64)
+    hi = org + np.array(SMALL) * g.voxel_size
+    t1 = _box_exit(org, hi, p[:, :3], p[:, 3:])
+    data = grid.data.cpu().numpy()
+    for n in range(len(p)):
+        steps = max(int(math.ceil(t1[n] / (0.5 * g.voxel_size))), 1)
+        h = t1[n] / steps
+        od = orc.grid_sigma(g, data, p[n, :3] + np.outer((np.arange(steps) + 0.5) * h, p[n, 3:])).sum() * h
+        f[n, 43] = math.exp(-od)
     got = rec.float().cpu().numpy()
     np.testing.assert_allclose(got, _bf16(f), rtol=1e-2, atol=2e-3)
 
@@ -226,9 +297,11 @@ def test_surrogate_accuracy_and_network_gain(ctx):
     ctx.check_status()
     e_net, e_ss = S.relative_l1(with_net, ref), S.relative_l1(ss_only, ref)
     print(f"relative L1 vs 8192 spp: network {e_net:.4f}, single scattering only {e_ss:.4f}")
-    assert e_net <= 0.08
+    # measured 0.041 with the 79-input network; the 8192-spp reference's own
+    # noise (about 2.5% relative L1) is part of it
+    assert e_net <= 0.05
     assert e_ss >= 0.8
-    assert e_ss >= 10 * e_net
+    assert e_ss >= 15 * e_net
     # the view transmittance is the same with or without the network and matches the path tracer's alpha
     torch.testing.assert_close(with_net[..., 3], ss_only[..., 3])
     assert float((with_net[..., 3] - ref[..., 3]).abs().mean()) < 2e-3
