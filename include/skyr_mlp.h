@@ -1,6 +1,6 @@
 /*
  * skyr_mlp.h — C ABI of the learned multiple-scattering surrogate's network:
- * a 79 -> 64 -> 64 -> 64 -> 64 -> 3 ReLU MLP with BF16 weights and FP32
+ * a 103 -> 64 -> 64 -> 64 -> 64 -> 3 ReLU MLP with BF16 weights and FP32
  * accumulation, its tensor-core training step (forward, relative-L2 loss,
  * backward, Adam) and batched inference.  No counterpart in the reference:
  * the network replaces the multiple-scattering heuristic of the cloud
@@ -9,11 +9,11 @@
  *
  * Parameter vector (FP32, the master copy the optimiser updates), layer by
  * layer, weights row-major [out][in]:
- *   W1[64][79] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[64][64] b4[64]
- *   W5[3][64] b5[3]                                   (17795 floats)
+ *   W1[64][103] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[64][64] b4[64]
+ *   W5[3][64] b5[3]                                   (19331 floats)
  *
- * Feature record (the network input, device memory): SKYR_MLP_RECORD = 80
- * bf16 values per sample, features 0..78 followed by one zero (the features
+ * Feature record (the network input, device memory): SKYR_MLP_RECORD = 112
+ * bf16 values per sample, features 0..102 followed by 9 zeros (the features
  * of skyr_surrogate.h).
  *
  * Packed network (device memory, skyr_mlp_packed_bytes()): the BF16 weights
@@ -31,11 +31,11 @@
 extern "C" {
 #endif
 
-#define SKYR_MLP_INPUTS 79
-#define SKYR_MLP_RECORD 80
+#define SKYR_MLP_INPUTS 103
+#define SKYR_MLP_RECORD 112
 #define SKYR_MLP_WIDTH 64
 #define SKYR_MLP_OUTPUTS 3
-#define SKYR_MLP_PARAMS 17795
+#define SKYR_MLP_PARAMS 19331
 
 /* struct id 11 of skyr_struct_size */
 typedef struct skyr_mlp_hparams {

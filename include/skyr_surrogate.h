@@ -27,15 +27,19 @@
  *           perpendicular (sun x z; sun x x with the sun at the zenith) and
  *           their cross product; feature 44 + 7 (l - 2) + j, j = 0 the centre,
  *           j = 1, 2 +- the sun axis, 3, 4 the second axis, 5, 6 the third
- *   79      zero
+ *   79..102 the view-oriented stencil: mean extinction / sigma_ref from mip
+ *           levels l = 3..6 at +-2^(l+1) voxels along v, u and w (the frame of
+ *           33..40); feature 79 + 6 (l - 3) + j, j = 0, 1 +-v, 2, 3 +-u, 4, 5 +-w
+ *   103..111 zero
  * span = the grid's longest edge; extinctions are divided by sigma_ref.
  * Features 0..32, 41 and 44..78 depend on the position only: they are taken at
- * the nodes of a coarse lattice (every `stride` voxels, where the other slots
- * are zero) and interpolated trilinearly; 33..40, 42 and 43 are computed per
- * sample.  Both are done the same way for training points and for the
- * raymarch.  Features 0..42 are the configured inputs; 43..78 (the view ray's
- * far side and the stencil) halve the network's error against path-traced
- * labels.
+ * the nodes of a coarse lattice (every `stride` voxels, 80 bf16 per node
+ * holding features 0..79, the per-sample slots zero) and interpolated
+ * trilinearly; 33..40, 42, 43 and 79..102 are computed per sample.  Both are
+ * done the same way for training points and for the raymarch.  Features 0..42
+ * are the configured inputs; 43..102 (the view ray's far side and the two
+ * stencils) cut the network's error against path-traced labels by more than
+ * half.
  */
 #ifndef SKYR_SURROGATE_H_
 #define SKYR_SURROGATE_H_
@@ -49,8 +53,8 @@ extern "C" {
 
 /* Feature lattice of one (grid, sun direction) pair (struct id 12). */
 typedef struct skyr_feature_volume {
-    void* data;        /* device: records [nodes][80] bf16, sun optical depth [nodes] f32, then the
-                        * grid's mip levels 1..6 (FP16, each 256-byte aligned) */
+    void* data;        /* device: node records [nodes][80] bf16, sun optical depth [nodes] f32, then
+                        * the grid's mip levels 1..6 (FP16, each 256-byte aligned) */
     int stride;        /* voxels between lattice nodes */
     int nx, ny, nz;    /* nodes per axis: (grid n + stride - 1) / stride + 1 */
     float sigma_ref;   /* extinctions are divided by this */

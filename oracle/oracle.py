@@ -343,7 +343,7 @@ def _fp(a: np.ndarray):
 
 
 def mlp_predict(params: np.ndarray, x: np.ndarray, mirror: bool = True, nthreads: int | None = None) -> np.ndarray:
-    """FP64 forward of the surrogate network: x[n][79] -> y[n][3]."""
+    """FP64 forward of the surrogate network: x[n][103] -> y[n][3]."""
     p = np.ascontiguousarray(params, dtype=np.float32)
     xx = np.ascontiguousarray(x, dtype=np.float32)
     y = np.zeros((len(xx), 3))
@@ -353,7 +353,7 @@ def mlp_predict(params: np.ndarray, x: np.ndarray, mirror: bool = True, nthreads
 
 def mlp_gradient(params: np.ndarray, x: np.ndarray, t: np.ndarray, label_scale: float = 1.0,
                  loss_eps: float = 1e-2, mirror: bool = True):
-    """(loss, gradient[17795]) of the mean relative-L2 loss, FP64."""
+    """(loss, gradient[19331]) of the mean relative-L2 loss, FP64."""
     p = np.ascontiguousarray(params, dtype=np.float32)
     xx = np.ascontiguousarray(x, dtype=np.float32)
     tt = np.ascontiguousarray(t, dtype=np.float32)
@@ -380,7 +380,7 @@ def _declare_surrogate(lb):
     lb.oracle_point_radiance.argtypes = [P, P, P, P, P, P, P, D, D, D, D, D, C.c_uint, C.c_int, D, C.c_int, C.c_int,
                                          D, D]
     lb.oracle_surrogate_render.restype = C.c_int
-    lb.oracle_surrogate_render.argtypes = [P, P, P, P, P, P, D, D, D, U16, FP, P, FP, C.c_double, C.c_int, C.c_int,
+    lb.oracle_surrogate_render.argtypes = [P, P, P, P, P, P, D, D, D, C.POINTER(C.c_uint8), P, FP, C.c_double, C.c_int, C.c_int,
                                            C.c_double, C.c_double, I32, C.c_int, C.c_int, D, D]
 
 
@@ -440,15 +440,12 @@ def surrogate_render(atmo, cloud, grid_struct, data_half, pt, view, sizes, luts:
     view = _host_view(view, froxel, keep)
     g = _grid_copy(grid_struct, data_half, keep)
     arrs = _lut_arrays(luts, ("transmittance", "aerial_perspective_luminance", "aerial_perspective_transmittance"))
-    nodes = fv.nx * fv.ny * fv.nz
-    raw = np.ascontiguousarray(lattice, dtype=np.uint8)
-    rec = np.ascontiguousarray(raw[: nodes * 160].view(np.uint16))
-    tau = np.ascontiguousarray(raw[nodes * 160: nodes * 164].view(np.float32))
+    raw = np.ascontiguousarray(lattice, dtype=np.uint8)  # records, optical depths, mip levels
     p = np.ascontiguousarray(params, dtype=np.float32)
     px = np.ascontiguousarray(pixels, dtype=np.int32)
     out, err = np.zeros((len(px), 4)), np.zeros(len(px))
     rc = lib().oracle_surrogate_render(_ref(atmo), _ref(cloud), _ref(g), _ref(pt), _ref(view), _ref(sizes),
-                                       *[_dp(a) for a in arrs], rec.ctypes.data_as(U16), tau.ctypes.data_as(FP),
+                                       *[_dp(a) for a in arrs], raw.ctypes.data_as(C.POINTER(C.c_uint8)),
                                        _ref(fv), p.ctypes.data_as(FP), out_scale, steps, int(use_network), min_t,
                                        rel_err, px.ctypes.data_as(I32), len(px), nthreads or threads(), _dp(out),
                                        _dp(err))

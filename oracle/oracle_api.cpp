@@ -452,7 +452,7 @@ int oracle_pathtrace(const skyr_atmosphere_parameters* atmo, const skyr_cloud_pa
 
 extern "C" {
 
-// y[n][3] = MLP(x[n][79]) in FP64 (BF16 rounding points mirrored when `mirror`)
+// y[n][3] = MLP(x[n][103]) in FP64 (BF16 rounding points mirrored when `mirror`)
 int oracle_mlp_predict(const float* params, const float* x, int n, int mirror, int threads, double* y) {
     orc::MlpOracle net(params, mirror != 0);
     parallel_for(n, threads, [&](int s) {
@@ -463,7 +463,7 @@ int oracle_mlp_predict(const float* params, const float* x, int n, int mirror, i
     return 0;
 }
 
-// gradient of the mean relative-L2 loss (grad[17795] overwritten); returns the loss
+// gradient of the mean relative-L2 loss (grad[19331] overwritten); returns the loss
 double oracle_mlp_gradient(const float* params, const float* x, const float* t, int n, double label_scale,
                            double loss_eps, int mirror, double* grad) {
     orc::MlpOracle net(params, mirror != 0);
@@ -545,17 +545,19 @@ int oracle_point_radiance(const skyr_atmosphere_parameters* atmo, const skyr_clo
 }
 
 // The surrogate raymarch of skyr_surrogate_render for listed pixels, in FP64
-// over the GPU-built feature lattice (records bf16 [nodes][80] then sun
-// optical depth f32 [nodes]); the network is oracle_mlp.hpp with the BF16
+// over the GPU-built feature lattice `lattice_raw` (node records bf16
+// [nodes][80], sun optical depth f32 [nodes], then the grid's FP16 mip levels
+// 1..6, each 256-byte aligned); the network is oracle_mlp.hpp with the BF16
 // rounding points mirrored.  The far-side feature (43) of sample k is the
 // transmittance of what remains of the ray's optical depth at the march's
-// samples past it: exp(-(sum_j>k sigma_j dt + sigma_k dt / 2)).  out[n][4] = (luminance rgb, transmittance),
+// samples past it: exp(-(sum_j>k sigma_j dt + sigma_k dt / 2)); features
+// 79..102 are the view-oriented stencil over mip levels 3..6.  out[n][4] = (luminance rgb, transmittance),
 // err[n] = the error estimate with a single relative error `rel_err`.
 int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_cloud_parameters* cp,
                             const skyr_density_grid* gd, const skyr_pathtrace_parameters* pt,
                             const skyr_cloud_view* v, const skyr_lut_sizes* s, const double* tlut,
-                            const double* apl, const double* apt, const uint16_t* lattice_rec,
-                            const float* lattice_tau, const skyr_feature_volume* fv, const float* params,
+                            const double* apl, const double* apt, const uint8_t* lattice_raw,
+                            const skyr_feature_volume* fv, const float* params,
                             double out_scale, int steps, int use_network, double min_t, double rel_err,
                             const int* pixels, int n, int threads, double* out, double* err) {
     skyr_cloud_material m = minimal_material();
@@ -575,7 +577,48 @@ int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_c
     const double cell = (double)gd->voxel_size * fv->stride;
     const orc::V3<double> og(gd->origin[0], gd->origin[1], gd->origin[2]);
     const orc::V3<double> sun(fv->sun[0], fv->sun[1], fv->sun[2]);
-    constexpr int kRec = 80, kIn = orc::kMlpIn;
+    constexpr int kLat = 80, kIn = orc::kMlpIn;
+    const size_t nodes = (size_t)fv->nx * fv->ny * fv->nz;
+    const uint16_t* lattice_rec = reinterpret_cast<const uint16_t*>(lattice_raw);
+    const float* lattice_tau = reinterpret_cast<const float*>(lattice_raw + nodes * kLat * 2);
+    struct Mip {
+        const uint16_t* d;
+        int nx, ny, nz;
+        double voxel;
+    };
+    Mip mip[7];
+    {
+        size_t off = nodes * (kLat * 2 + 4);
+        int nx = gd->nx, ny = gd->ny, nz = gd->nz;
+        for (int l = 1; l <= 6; ++l) {
+            off = (off + 255) & ~(size_t)255;
+            nx = (nx + 1) / 2, ny = (ny + 1) / 2, nz = (nz + 1) / 2;
+            mip[l] = Mip{reinterpret_cast<const uint16_t*>(lattice_raw + off), nx, ny, nz,
+                         (double)gd->voxel_size * (1 << l)};
+            off += (size_t)nx * ny * nz * 2;
+        }
+    }
+    // trilinear between texel centres, zero border
+    auto mip_value = [&](int l, orc::V3<double> p) {
+        const Mip& M = mip[l];
+        double g[3];
+        for (int a = 0; a < 3; ++a) g[a] = (p[a] - gd->origin[a]) / M.voxel - 0.5;
+        int i0[3];
+        double fr[3];
+        for (int a = 0; a < 3; ++a) {
+            i0[a] = (int)std::floor(g[a]);
+            fr[a] = g[a] - i0[a];
+        }
+        double v = 0.0;
+        for (int c = 0; c < 8; ++c) {
+            int x = i0[0] + (c & 1), y = i0[1] + ((c >> 1) & 1), z = i0[2] + (c >> 2);
+            if (x < 0 || y < 0 || z < 0 || x >= M.nx || y >= M.ny || z >= M.nz) continue;
+            double w = ((c & 1) ? fr[0] : 1 - fr[0]) * (((c >> 1) & 1) ? fr[1] : 1 - fr[1]) *
+                       ((c >> 2) ? fr[2] : 1 - fr[2]);
+            v += w * orc::half_to_float(M.d[((size_t)z * M.ny + y) * M.nx + x]);
+        }
+        return v;
+    };
     auto lattice = [&](orc::V3<double> x, double f[kIn], double& tau) {
         orc::V3<double> g = (x - og) / cell;
         int i0[3];
@@ -593,7 +636,7 @@ int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_c
             for (int a = 0; a < 3; ++a) w *= d[a] ? fr[a] : 1.0 - fr[a];
             size_t node = ((size_t)(i0[2] + d[2]) * fv->ny + (i0[1] + d[1])) * fv->nx + (i0[0] + d[0]);
             tau += w * lattice_tau[node];
-            for (int k = 0; k < kIn; ++k) f[k] += w * orc::bf16_to_float(lattice_rec[node * kRec + k]);
+            for (int k = 0; k < kLat; ++k) f[k] += w * orc::bf16_to_float(lattice_rec[node * kLat + k]);
         }
     };
     // features 33..40: the view-oriented cube corners (skyr_surrogate.h)
@@ -612,6 +655,13 @@ int oracle_surrogate_render(const skyr_atmosphere_parameters* atmo, const skyr_c
         for (int j = 0; j < 8; ++j) {
             orc::V3<double> o = v * ((j & 1) ? nbr : -nbr) + u * ((j & 2) ? nbr : -nbr) + w * ((j & 4) ? nbr : -nbr);
             f[33 + j] = PT.grid_sigma(x + o) * inv_ref;
+        }
+        // 79..102: +-2^(l+1) voxels along v, u, w at mip levels l = 3..6
+        const orc::V3<double> axes[3] = {v, u, w};
+        for (int s = 0; s < 24; ++s) {
+            int l = 3 + s / 6, j = s % 6;
+            double h = (double)gd->voxel_size * (2 << l) * ((j & 1) ? -1.0 : 1.0);
+            f[79 + s] = mip_value(l, x + axes[j >> 1] * h) * gd->density * inv_ref;
         }
     };
     const double gb = pt->back_phase_g, gf = pt->forward_phase_g, ratio = pt->forward_scattering_ratio;

@@ -21,8 +21,8 @@
 
 namespace orc {
 
-constexpr int kMlpIn = 79, kMlpWidth = 64, kMlpOut = 3, kMlpLayers = 5;
-constexpr int kMlpParams = 17795;
+constexpr int kMlpIn = 103, kMlpWidth = 64, kMlpOut = 3, kMlpLayers = 5;
+constexpr int kMlpParams = 19331;
 
 inline int mlp_fan_in(int l) { return l == 0 ? kMlpIn : kMlpWidth; }
 inline int mlp_fan_out(int l) { return l == kMlpLayers - 1 ? kMlpOut : kMlpWidth; }

@@ -436,7 +436,7 @@ _SIGNATURES.update({
 # ---------------------------------------------------------------------------
 # skyr_mlp.h
 # ---------------------------------------------------------------------------
-SKYR_MLP_INPUTS, SKYR_MLP_RECORD, SKYR_MLP_WIDTH, SKYR_MLP_OUTPUTS, SKYR_MLP_PARAMS = 79, 80, 64, 3, 17795
+SKYR_MLP_INPUTS, SKYR_MLP_RECORD, SKYR_MLP_WIDTH, SKYR_MLP_OUTPUTS, SKYR_MLP_PARAMS = 103, 112, 64, 3, 19331
 
 
 class MlpHparams(C.Structure):

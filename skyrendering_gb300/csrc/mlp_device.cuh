@@ -17,16 +17,16 @@
 namespace skyr {
 namespace mlp {
 
-constexpr int kIn = SKYR_MLP_INPUTS;    // 79
-constexpr int kRec = SKYR_MLP_RECORD;   // 80
-constexpr int kKT = kRec / 16;          // k-tiles of the first layer (5)
+constexpr int kIn = SKYR_MLP_INPUTS;    // 103
+constexpr int kRec = SKYR_MLP_RECORD;   // 112
+constexpr int kKT = kRec / 16;          // k-tiles of the first layer (7)
 constexpr int kW = SKYR_MLP_WIDTH;      // 64
 constexpr int kOut = SKYR_MLP_OUTPUTS;  // 3
 constexpr int kLayers = 5;
 static_assert(kRec % 16 == 0 && kIn < kRec && kRec <= 128, "record: whole k-tiles, at most two 64-column tiles");
 
 // Row strides (bf16) of the packed weight matrices: rows of an odd number of
-// 16-byte units (176 B, 144 B) put the 8 rows an ldmatrix phase reads in 8
+// 16-byte units (240 B, 144 B) put the 8 rows an ldmatrix phase reads in 8
 // different 16-byte bank groups.
 constexpr int kS1 = kRec + 8;  // W1 [64][kS1], columns kIn.. zero
 constexpr int kSH = 72;        // W2..W4 [64][kSH], W5 [8][kSH] (rows 3..7 zero)
@@ -40,7 +40,7 @@ constexpr int kOffB = kOffW5 + 8 * kSH * 2;          // b1..b4 [4][64] f32, b5 [
 constexpr int kOffScale = kOffB + (4 * kW + 8) * 4;
 constexpr int kPackedBytes = kOffScale + 16;
 
-// Row stride (bf16) of a feature-record tile in shared memory (176 B rows)
+// Row stride (bf16) of a feature-record tile in shared memory (240 B rows)
 constexpr int kXS = kRec + 8;
 
 __host__ __device__ constexpr int fan_in(int l) { return l == 0 ? kIn : kW; }

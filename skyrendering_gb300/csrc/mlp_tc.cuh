@@ -8,7 +8,7 @@
 // t (tensor-memory lane t), so a layer's epilogue (bias, ReLU, BF16) runs on
 // the thread's own accumulator row and writes the next layer's A operand row.
 // One elected thread issues each layer's MMAs (M = 128, N = 64, K = the record
-// width (80) or 64) and commits them to an mbarrier the CTA waits on (bounded).
+// width (112) or 64) and commits them to an mbarrier the CTA waits on (bounded).
 #pragma once
 
 #include <cuda_bf16.h>

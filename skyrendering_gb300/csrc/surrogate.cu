@@ -19,24 +19,29 @@ namespace skyr {
 namespace {
 
 // Feature record layout (skyr_surrogate.h): kRec bf16, kRec / 8 chunks of 16 bytes.
-constexpr int kRecQ = SKYR_MLP_RECORD / 8;  // chunks per record (10)
+constexpr int kRecQ = SKYR_MLP_RECORD / 8;  // chunks per record (14)
+constexpr int kLatQ = 10;                   // chunks per lattice node: features 0..79 of the record
 constexpr int kSun = 32;                    // samples toward the sun (features 1..32)
 constexpr int kViewNbr = 33;                // features 33..40: view-oriented cube corners (per sample)
 constexpr int kHeight = 41;                 // height in the grid box (lattice)
 constexpr int kCos = 42;                    // cos(view, sun) (per sample)
 constexpr int kFar = 43;                    // transmittance along the view ray to the box's exit (per sample)
-constexpr int kStencil = 44;                // features 44..78: the density stencil (lattice)
+constexpr int kStencil = 44;                // features 44..78: the sun-oriented density stencil (lattice)
 constexpr int kStencilLevels = 5;           // mip levels 2..6
 constexpr int kStencilFirst = 2;
 constexpr int kStencilPoints = 7;           // centre and +-1 along the stencil's three axes
+constexpr int kViewSt = kStencil + kStencilLevels * kStencilPoints;  // 79..102: the view-oriented stencil (per sample)
+constexpr int kViewStLevels = 4;            // mip levels 3..6
+constexpr int kViewStFirst = 3;
+constexpr int kViewStPoints = 6;            // +-1 along the view frame's three axes (the centres are in 44..78)
 constexpr int kMipLevels = 6;               // levels 1..6 of the grid, kept in the lattice's buffer
-static_assert(kStencil + kStencilLevels * kStencilPoints + 1 == SKYR_MLP_RECORD, "record layout");
-static_assert(kStencil + kStencilLevels * kStencilPoints == SKYR_MLP_INPUTS, "network inputs");
+static_assert(kViewSt + kViewStLevels * kViewStPoints == SKYR_MLP_INPUTS, "network inputs");
+static_assert(kLatQ * 8 == kViewSt + 1 && kRecQ >= kLatQ, "lattice nodes hold features 0..kViewSt");
 constexpr int kMaxSampleTries = 64;
 constexpr int kMaxTrackSteps = 1 << 16;
 
 struct Lattice {
-    const uint4* rec;  // [nodes][kRecQ] (kRec bf16, the per-sample slots zero)
+    const uint4* rec;  // [nodes][kLatQ] (features 0..79 of the record, the per-sample slots zero)
     const float* tau;  // [nodes]
     int nx, ny, nz;
     float3 origin;
@@ -53,6 +58,7 @@ struct MipLevel {
 };
 struct Mips {
     MipLevel level[kMipLevels + 1];  // [0] is the grid itself
+    float voxel;                     // the grid's voxel edge
 };
 
 __device__ __forceinline__ float u01(uint32_t& s) {
@@ -158,9 +164,10 @@ __device__ __forceinline__ float lattice_tau(const Lattice& L, const LatticeCell
 // sun's component perpendicular to v (any perpendicular when the two are
 // parallel), w = v x u.  Corner j takes +dist/sqrt(3) along v, u, w where bit
 // 0, 1, 2 of j is set, -dist/sqrt(3) where it is not.
-__device__ __forceinline__ void view_neighbours(const PtConsts& P, float3 x, float3 v, float3 sun, float dist,
-                                                float inv_ref, float (&nb)[8]) {
-    float3 u = sun - v * dot3(v, sun);
+// The view frame (v, u, w): u the sun's component perpendicular to v (any
+// perpendicular when the two are parallel), w = v x u.
+__device__ __forceinline__ void view_frame(float3 v, float3 sun, float3& u, float3& w) {
+    u = sun - v * dot3(v, sun);
     float l2 = dot3(u, u);
     if (l2 < 1e-8f) {
         float3 b1;
@@ -168,7 +175,11 @@ __device__ __forceinline__ void view_neighbours(const PtConsts& P, float3 x, flo
     } else {
         u = u * rsqrtf(l2);
     }
-    float3 w = f3(v.y * u.z - v.z * u.y, v.z * u.x - v.x * u.z, v.x * u.y - v.y * u.x);
+    w = f3(v.y * u.z - v.z * u.y, v.z * u.x - v.x * u.z, v.x * u.y - v.y * u.x);
+}
+
+__device__ __forceinline__ void view_neighbours(const PtConsts& P, float3 x, float3 v, float3 u, float3 w, float dist,
+                                                float inv_ref, float (&nb)[8]) {
     const float r = dist * 0.57735026918962576f;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
@@ -179,33 +190,39 @@ __device__ __forceinline__ void view_neighbours(const PtConsts& P, float3 x, flo
 
 // The feature record of a sample at x seen along v: the lattice's features
 // interpolated trilinearly chunk by chunk, with the per-sample slots filled in
-// (the view neighbours, cos(v, sun), the far-side transmittance `far_t`),
-// written as kRecQ 16-byte chunks to `row`.  Returns the sun optical depth;
-// f0 / near_sun receive feature 0 and the mean of features 1..8 (the error
-// table's bin).
-__device__ __forceinline__ float write_record(const Lattice& L, const PtConsts& P, float3 x, float3 v, float nbr,
-                                              float inv_ref, float far_t, uint4* row, float& f0, float& near_sun) {
+// (the view neighbours, cos(v, sun), the far-side transmittance `far_t`, the
+// view-oriented stencil over the mip levels M), written as kRecQ 16-byte
+// chunks to `row`.  Returns the sun optical depth; f0 / near_sun receive
+// feature 0 and the mean of features 1..8 (the error table's bin).
+__device__ __forceinline__ float write_record(const Lattice& L, const PtConsts& P, const Mips& M, float3 x, float3 v,
+                                              float nbr, float inv_ref, float far_t, uint4* row, float& f0,
+                                              float& near_sun) {
     LatticeCell c;
     lattice_cell(L, x, c);
     const float tau = lattice_tau(L, c);
+    float3 fu, fw;
+    view_frame(v, L.sun, fu, fw);
     float nb[8];
-    view_neighbours(P, x, v, L.sun, nbr, inv_ref, nb);
+    view_neighbours(P, x, v, fu, fw, nbr, inv_ref, nb);
     const float mu = dot3(v, L.sun);
+    const float k_ref = inv_ref * P.density;
     float near = 0.f;
 #pragma unroll
     for (int q = 0; q < kRecQ; ++q) {
         float a[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) a[e] = 0.f;
+        if (q < kLatQ) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            uint4 u = __ldg(L.rec + c.node[k] * kRecQ + q);
-            uint32_t w4[4] = {u.x, u.y, u.z, u.w};
+            for (int k = 0; k < 8; ++k) {
+                uint4 u = __ldg(L.rec + c.node[k] * kLatQ + q);
+                uint32_t w4[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
-            for (int h = 0; h < 4; ++h) {
-                __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&w4[h]);
-                a[2 * h] = fmaf(c.w[k], __low2float(b), a[2 * h]);
-                a[2 * h + 1] = fmaf(c.w[k], __high2float(b), a[2 * h + 1]);
+                for (int h = 0; h < 4; ++h) {
+                    __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&w4[h]);
+                    a[2 * h] = fmaf(c.w[k], __low2float(b), a[2 * h]);
+                    a[2 * h + 1] = fmaf(c.w[k], __high2float(b), a[2 * h + 1]);
+                }
             }
         }
 #pragma unroll
@@ -219,6 +236,17 @@ __device__ __forceinline__ float write_record(const Lattice& L, const PtConsts& 
         }
         row[q] = make_uint4(mlp::pack_bf16(a[0], a[1]), mlp::pack_bf16(a[2], a[3]), mlp::pack_bf16(a[4], a[5]),
                             mlp::pack_bf16(a[6], a[7]));
+    }
+    // the view-oriented stencil over the chunks' zeros, one value at a time in a
+    // rolled loop (unrolled, its 24 lookups crowd the instruction cache):
+    // +-2^(l+1) voxels along v, u, w at mip level l = kViewStFirst + s / 6
+    __nv_bfloat16* rb = reinterpret_cast<__nv_bfloat16*>(row);
+#pragma unroll 1
+    for (int s = 0; s < kViewStLevels * kViewStPoints; ++s) {
+        const int lv = kViewStFirst + s / kViewStPoints, j = s % kViewStPoints;
+        const float3 ax = j < 2 ? v : j < 4 ? fu : fw;
+        const float h = M.voxel * (float)(2 << lv) * ((j & 1) ? -1.f : 1.f);
+        rb[kViewSt + s] = __float2bfloat16_rn(mip_value(M.level[lv], P.origin, x + ax * h) * k_ref);
     }
     near_sun = near * 0.125f;
     return tau;
@@ -245,7 +273,7 @@ __global__ void __launch_bounds__(128) feature_lattice_kernel(PtConsts P, GridBo
     // chunk by chunk: the features of positions q * 8 .. q * 8 + 7
     const float k_ref = Q.inv_sigma_ref * P.density;
 #pragma unroll 1
-    for (int q = 0; q < kRecQ; ++q) {
+    for (int q = 0; q < kLatQ; ++q) {
         float a[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
@@ -268,7 +296,7 @@ __global__ void __launch_bounds__(128) feature_lattice_kernel(PtConsts P, GridBo
             }
             a[e] = v;
         }
-        rec[node * kRecQ + q] = make_uint4(mlp::pack_bf16(a[0], a[1]), mlp::pack_bf16(a[2], a[3]),
+        rec[node * kLatQ + q] = make_uint4(mlp::pack_bf16(a[0], a[1]), mlp::pack_bf16(a[2], a[3]),
                                            mlp::pack_bf16(a[4], a[5]), mlp::pack_bf16(a[6], a[7]));
     }
     // optical depth to the sun: midpoint rule to the exit of the grid box
@@ -343,7 +371,8 @@ __global__ void __launch_bounds__(128) sample_points_kernel(PtConsts P, GridBox 
     o6[3] = d.x; o6[4] = d.y; o6[5] = d.z;
 }
 
-__global__ void __launch_bounds__(128) records_kernel(Lattice L, PtConsts P, GridBox B, float nbr, float inv_ref,
+__global__ void __launch_bounds__(128) records_kernel(Lattice L, PtConsts P, GridBox B, Mips M, float nbr,
+                                                      float inv_ref,
                                                       float far_step, const float* __restrict__ pts, int n,
                                                       uint4* __restrict__ rec) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -351,7 +380,7 @@ __global__ void __launch_bounds__(128) records_kernel(Lattice L, PtConsts P, Gri
     const float* q = pts + 6 * (size_t)i;
     float3 x = f3(q[0], q[1], q[2]), d = f3(q[3], q[4], q[5]);
     float f0, near_sun;
-    write_record(L, P, x, d, nbr, inv_ref, far_transmittance(P, B, x, d, far_step), rec + (size_t)i * kRecQ, f0,
+    write_record(L, P, M, x, d, nbr, inv_ref, far_transmittance(P, B, x, d, far_step), rec + (size_t)i * kRecQ, f0,
                  near_sun);
 }
 
@@ -395,7 +424,7 @@ constexpr int kSmOut = 32 * 4 * 4;            // network outputs of one warp
 constexpr int kSmRender = mlp::kPackedBytes + kRenderWarps * (kSmTile + kSmOut);
 
 template <class S>
-__global__ void __launch_bounds__(32 * kRenderWarps, 2) surrogate_render_kernel(CloudConsts C, AtmoConsts A, PtConsts P, Lattice L,
+__global__ void __launch_bounds__(32 * kRenderWarps, 2) surrogate_render_kernel(CloudConsts C, AtmoConsts A, PtConsts P, Lattice L, Mips M,
                                                                   RenderConsts R, const float4* __restrict__ tlut,
                                                                   int tw, int th, const S* __restrict__ apl,
                                                                   const S* __restrict__ apt,
@@ -449,7 +478,7 @@ __global__ void __launch_bounds__(32 * kRenderWarps, 2) surrogate_render_kernel(
             if (need) {
                 const float far_t = __expf(-fmaxf(tau_total - run + 0.5f * sigma * dt, 0.f));
                 float f0, near_sun;
-                tau = write_record(L, P, x, dir, R.nbr, R.inv_ref, far_t, row, f0, near_sun);
+                tau = write_record(L, P, M, x, dir, R.nbr, R.inv_ref, far_t, row, f0, near_sun);
                 if (R.error_table) rel_err = __ldg(R.error_table + error_bin(f0, near_sun));
             } else {
 #pragma unroll
@@ -527,11 +556,12 @@ int grid_setup(const skyr_density_grid* grid, PtConsts& P, GridBox& B) {
 // With M: the levels' sizes, texel sizes and byte offsets from the buffer's
 // start (in data), level 0 being the grid itself.
 size_t lattice_bytes(const skyr_density_grid* grid, size_t nodes, Mips* M) {
-    size_t off = nodes * (kRecQ * 16 + 4);
+    size_t off = nodes * (kLatQ * 16 + 4);
     int nx = grid->nx, ny = grid->ny, nz = grid->nz;
     if (M) {
         M->level[0] = MipLevel{reinterpret_cast<const unsigned short*>(grid->data), nx, ny, nz,
                                1.f / grid->voxel_size};
+        M->voxel = grid->voxel_size;
     }
     for (int l = 1; l <= kMipLevels; ++l) {
         off = (off + 255) & ~(size_t)255;
@@ -544,6 +574,16 @@ size_t lattice_bytes(const skyr_density_grid* grid, size_t nodes, Mips* M) {
     return off;
 }
 
+// The mip chain in a lattice's buffer, with absolute device pointers.
+Mips lattice_mips(const skyr_density_grid* grid, const skyr_feature_volume* fv) {
+    Mips M;
+    lattice_bytes(grid, (size_t)fv->nx * fv->ny * fv->nz, &M);
+    const unsigned char* base = reinterpret_cast<const unsigned char*>(fv->data);
+    for (int l = 1; l <= kMipLevels; ++l)
+        M.level[l].data = reinterpret_cast<const unsigned short*>(base + reinterpret_cast<size_t>(M.level[l].data));
+    return M;
+}
+
 int lattice_setup(const skyr_density_grid* grid, const skyr_feature_volume* fv, Lattice& L) {
     if (!fv || !fv->data) return set_error(SKYR_EINVAL, "null feature lattice");
     if (fv->stride < 1 || fv->nx < 2 || fv->ny < 2 || fv->nz < 2)
@@ -554,7 +594,7 @@ int lattice_setup(const skyr_density_grid* grid, const skyr_feature_volume* fv, 
     if (reinterpret_cast<uintptr_t>(fv->data) & 15) return set_error(SKYR_EINVAL, "feature lattice must be 16-byte aligned");
     size_t nodes = (size_t)fv->nx * fv->ny * fv->nz;
     L.rec = reinterpret_cast<const uint4*>(fv->data);
-    L.tau = reinterpret_cast<const float*>(reinterpret_cast<const unsigned char*>(fv->data) + nodes * kRecQ * 16);
+    L.tau = reinterpret_cast<const float*>(reinterpret_cast<const unsigned char*>(fv->data) + nodes * kLatQ * 16);
     L.nx = fv->nx;
     L.ny = fv->ny;
     L.nz = fv->nz;
@@ -652,12 +692,9 @@ int skyr_feature_volume_build(skyr_ctx* ctx, const skyr_atmosphere_parameters* a
         Q.spacing[l] = grid->voxel_size * (float)(2 << (kStencilFirst + l));
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     // the mip chain of the grid, in the lattice's buffer after the optical depths
-    Mips M;
+    const Mips M = lattice_mips(grid, fv);
     size_t nodes = (size_t)L.nx * L.ny * L.nz;
-    lattice_bytes(grid, nodes, &M);
-    unsigned char* base = reinterpret_cast<unsigned char*>(fv->data);
     for (int l = 1; l <= kMipLevels; ++l) {
-        M.level[l].data = reinterpret_cast<const unsigned short*>(base + reinterpret_cast<size_t>(M.level[l].data));
         size_t n = (size_t)M.level[l].nx * M.level[l].ny * M.level[l].nz;
         mip_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
             M.level[l - 1], M.level[l], const_cast<unsigned short*>(M.level[l].data));
@@ -696,7 +733,8 @@ int skyr_surrogate_records(skyr_ctx* ctx, const skyr_density_grid* grid, const s
     if (int e = lattice_setup(grid, fv, L)) return e;
     if (n == 0) return SKYR_OK;
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
-    records_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(L, P, B, 0.1f * B.span, 1.f / fv->sigma_ref,
+    records_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(L, P, B, lattice_mips(grid, fv), 0.1f * B.span,
+                                                           1.f / fv->sigma_ref,
                                                            0.5f * grid->voxel_size, points, n,
                                                            reinterpret_cast<uint4*>(records));
     return check_cuda(cudaGetLastError(), "records kernel");
@@ -765,6 +803,7 @@ int skyr_surrogate_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmos
     R.nbr = 0.1f * B.span;
     R.inv_ref = 1.f / fv->sigma_ref;
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    const Mips mips = lattice_mips(grid, fv);
     auto launch = [&](auto tag) -> int {
         using S = decltype(tag);
         auto kernel = surrogate_render_kernel<S>;
@@ -774,7 +813,7 @@ int skyr_surrogate_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmos
             return e;
         int tiles = ((view->width + 7) / 8) * ((view->height + 3) / 4);
         kernel<<<(tiles + kRenderWarps - 1) / kRenderWarps, 32 * kRenderWarps, use_smem, ctx->stream>>>(
-            C, A, P, L, R, reinterpret_cast<const float4*>(transmittance), sizes->transmittance_width,
+            C, A, P, L, mips, R, reinterpret_cast<const float4*>(transmittance), sizes->transmittance_width,
             sizes->transmittance_height, reinterpret_cast<const S*>(aerial_perspective_luminance),
             reinterpret_cast<const S*>(aerial_perspective_transmittance),
             reinterpret_cast<const unsigned char*>(packed), reinterpret_cast<float4*>(out_rgba), out_error);

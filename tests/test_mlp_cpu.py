@@ -10,8 +10,8 @@ import pytest
 
 from oracle import oracle as orc
 
-IN = 79  # the network's inputs (include/skyr_mlp.h)
-P = 17795
+IN = 103  # the network's inputs (include/skyr_mlp.h)
+P = 19331
 
 
 def _layer_slices():

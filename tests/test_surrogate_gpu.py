@@ -11,7 +11,7 @@
   the committed network (BF16 rounding points mirrored): mean relative error
   of the luminance <= 1e-3, transmittance 1e-5;
 * accuracy: on the 512x640x352 evaluation cloud at 128^2 the network image is
-  within 5 % relative L1 of a 8192-spp path-traced reference while single
+  within 2.5 % relative L1 of a 32768-spp path-traced reference while single
   scattering alone is >= 80 % off (what the trained network gains).
 """
 import ctypes as C
@@ -73,7 +73,8 @@ def _view_neighbours(grid, x, v, sun, sigma_ref):
     return sig / sigma_ref
 
 
-REC = mlp.RECORD  # 80 bf16: features 0..78 (skyr_surrogate.h), then a zero
+REC = mlp.RECORD  # 112 bf16: features 0..102 (skyr_surrogate.h), then zeros
+LAT = 80  # bf16 per lattice node: features 0..79 of the record, the per-sample slots zero
 
 
 def _mips(data, levels=6):
@@ -136,8 +137,8 @@ def test_lattice_matches_oracle(small):
     raw = fv.buf.cpu().numpy()
     st = fv.struct
     nodes = st.nx * st.ny * st.nz
-    rec = raw[: nodes * REC * 2].view(np.uint16).reshape(nodes, REC)
-    tau = raw[nodes * REC * 2: nodes * (REC * 2 + 4)].view(np.float32)
+    rec = raw[: nodes * LAT * 2].view(np.uint16).reshape(nodes, LAT)
+    tau = raw[nodes * LAT * 2: nodes * (LAT * 2 + 4)].view(np.float32)
     data = grid.data.cpu().numpy()
     rng = np.random.default_rng(1)
     idx = rng.choice(nodes, 48, replace=False)
@@ -159,7 +160,7 @@ def test_lattice_matches_oracle(small):
     got = got.view(np.float32)
     np.testing.assert_allclose(got, _bf16(feat), rtol=1e-2, atol=1e-3)
     # the per-sample slots (cos, far side) and the pad stay zero
-    assert np.all(rec[idx, 42:44] == 0) and np.all(rec[idx, REC - 1] == 0)
+    assert np.all(rec[idx, 42:44] == 0) and np.all(rec[idx, LAT - 1] == 0)
     # the stencil over the mip chain (the GPU's levels are FP16)
     got_s = (rec[idx, 44:79].astype(np.uint32) << 16).view(np.float32)
     np.testing.assert_allclose(got_s, _bf16(_stencil(grid, x, sun, st.sigma_ref)), rtol=1e-2, atol=2e-3)
@@ -179,7 +180,7 @@ def test_records_interpolate_lattice(ctx, small):
     st = fv.struct
     nodes = st.nx * st.ny * st.nz
     raw = fv.buf.cpu().numpy()
-    lat = (raw[: nodes * REC * 2].view(np.uint16).reshape(nodes, REC).astype(np.uint32) << 16).view(np.float32)
+    lat = (raw[: nodes * LAT * 2].view(np.uint16).reshape(nodes, LAT).astype(np.uint32) << 16).view(np.float32)
     p = pts.cpu().numpy().astype(np.float64)
     g = grid.struct
     q = (p[:, :3] - np.array(g.origin[:])) / (g.voxel_size * st.stride)
@@ -187,11 +188,12 @@ def test_records_interpolate_lattice(ctx, small):
     i0 = np.clip(np.floor(q).astype(int), 0, n3 - 2)
     fr = np.clip(q - i0, 0, 1)
     f = np.zeros((len(p), REC))
+    fl = f[:, :LAT]
     for c in range(8):
         d = np.array([c & 1, (c >> 1) & 1, c >> 2])
         w = np.prod(np.where(d, fr, 1 - fr), 1)
         node = ((i0[:, 2] + d[2]) * st.ny + (i0[:, 1] + d[1])) * st.nx + (i0[:, 0] + d[0])
-        f += w[:, None] * lat[node]
+        fl += w[:, None] * lat[node]
     sun = np.array(st.sun[:], dtype=np.float64)
     f[:, 42] = p[:, 3:] @ sun
     f[:, 33:41] = _view_neighbours(grid, p[:, :3], p[:, 3:], sun, st.sigma_ref)
@@ -205,6 +207,17 @@ def test_records_interpolate_lattice(ctx, small):
         h = t1[n] / steps
         od = orc.grid_sigma(g, data, p[n, :3] + np.outer((np.arange(steps) + 0.5) * h, p[n, 3:])).sum() * h
         f[n, 43] = math.exp(-od)
+    # 79..102: the view-oriented stencil, +-2^(l+1) voxels along v, u, w at mip levels 3..6
+    v = p[:, 3:]
+    u = sun[None, :] - v * (v @ sun)[:, None]
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    w = np.cross(v, u)
+    mips = _mips(grid.data.float().cpu().numpy())
+    for s_ in range(24):
+        lv, j = 3 + s_ // 6, s_ % 6
+        ax = (v, u, w)[j >> 1]
+        h = g.voxel_size * 2 ** (lv + 1) * (-1.0 if j & 1 else 1.0)
+        f[:, 79 + s_] = _trilinear_zero(mips[lv], org, g.voxel_size * 2 ** lv, p[:, :3] + ax * h) * g.density / st.sigma_ref
     got = rec.float().cpu().numpy()
     np.testing.assert_allclose(got, _bf16(f), rtol=1e-2, atol=2e-3)
 
@@ -291,15 +304,14 @@ def test_surrogate_accuracy_and_network_gain(ctx):
     ss_only, _ = S.render(ctx, sc.atmo, sc.cloud, grid, sc.pt, sc.view, sc.sizes, sc.luts, fv, None,
                           S.parameters(use_network=0))
     tr = PathTracer(ctx, sc.pt, sc.cloud, sc.view, sc.env, sc.sizes, grid=grid)
-    for _ in range(2):
+    for _ in range(8):
         tr.render(sc.atmo, sc.luts, 4096)
     ref = tr.acc / tr.frames
     ctx.check_status()
     e_net, e_ss = S.relative_l1(with_net, ref), S.relative_l1(ss_only, ref)
-    print(f"relative L1 vs 8192 spp: network {e_net:.4f}, single scattering only {e_ss:.4f}")
-    # measured 0.032 with the 79-input network; the 8192-spp reference's own
-    # noise (about 2.5% relative L1) is part of it
-    assert e_net <= 0.05
+    print(f"relative L1 vs 32768 spp: network {e_net:.4f}, single scattering only {e_ss:.4f}")
+    # the 32768-spp reference's own noise (about 1.2% relative L1) is part of it
+    assert e_net <= 0.025
     assert e_ss >= 0.8
     assert e_ss >= 15 * e_net
     # the view transmittance is the same with or without the network and matches the path tracer's alpha
@@ -313,10 +325,10 @@ def test_training_pipeline_reduces_error(ctx):
     vrec, vlab = T.dataset(sc, range(900, 901), 2048, 128)
     untrained = mlp.PackedMLP.from_params(ctx, mlp.init_params(7), float(lab.mean()))
     e0 = T.validation_error(untrained, vrec, vlab)
-    params, scale, curve = T.train(ctx, rec, lab, vrec, vlab, epochs=12, batch=4096, log=lambda *a: None)
+    params, scale, curve = T.train(ctx, rec, lab, vrec, vlab, epochs=24, batch=4096, log=lambda *a: None)
     e1 = T.validation_error(mlp.PackedMLP.from_params(ctx, params, scale), vrec, vlab)
     print(f"validation relative L1: untrained {e0:.3f} -> trained {e1:.3f}")
-    assert e1 < 0.6 * e0
+    assert e1 < 0.65 * e0  # measured 0.58 with the 103-input network
 
 
 def test_fallback_replaces_flagged_pixels(ctx, small):
