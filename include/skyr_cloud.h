@@ -68,17 +68,18 @@ size_t skyr_noise_expanded_bytes(const skyr_noise_texture_desc* desc, int channe
 int skyr_noise_expand(skyr_ctx* ctx, const skyr_noise_texture_desc* desc, const void* tex, int channels,
                       void* out);
 
-/* A hardware sampler of level 0 of one channel of a generated texture: the
- * bytes are copied (ordered on the context's stream) into a CUDA array that the
- * texture units filter as the GL texture of the reference does -- LINEAR,
- * REPEAT, UNORM8 -- with its 8-bit fixed-point filter weights (1/256), the
- * precision GL drivers filter the reference's textures with.  The cloud
- * raymarch takes its magnified Material1 fetches from it when
- * skyr_cloud_textures names one; minified fetches (NEAREST_MIPMAP_NEAREST at
- * the levels above 0) still read `tex`.  The library allocates the array; the
- * sampler keeps no pointer to `tex`.  skyr_noise_sampler_handle gives the
- * cudaTextureObject_t as a 64-bit value.  (Counterpart: the texture objects the
- * reference binds, VolumetricCloudDefaultMaterial.cpp:40-72.) */
+/* Hardware samplers of one channel of a generated texture: the bytes are
+ * copied (ordered on the context's stream) into CUDA arrays that the texture
+ * units sample as the GL texture of the reference is sampled -- REPEAT,
+ * UNORM8.  skyr_noise_sampler_handle: level 0 with LINEAR filtering and its
+ * 8-bit fixed-point weights (1/256), the precision GL drivers filter the
+ * reference's textures with (magnification).  skyr_noise_sampler_nearest_handle:
+ * every mip level, NEAREST at an explicit level (the NEAREST_MIPMAP_NEAREST
+ * minification, the level chosen by the caller's own LOD).  The cloud raymarch
+ * takes its Material1 fetches from them when skyr_cloud_textures names them.
+ * The library allocates the arrays; the sampler keeps no pointer to `tex`.
+ * Handles are cudaTextureObject_t as 64-bit values.  (Counterpart: the texture
+ * objects the reference binds, VolumetricCloudDefaultMaterial.cpp:40-72.) */
 typedef struct skyr_noise_sampler skyr_noise_sampler;
 int skyr_noise_sampler_create(skyr_ctx* ctx, const skyr_noise_texture_desc* desc, const void* tex, int channel,
                               skyr_noise_sampler** out);
@@ -86,6 +87,7 @@ int skyr_noise_sampler_create(skyr_ctx* ctx, const skyr_noise_texture_desc* desc
 int skyr_noise_sampler_update(skyr_ctx* ctx, skyr_noise_sampler* sampler, const void* tex);
 int skyr_noise_sampler_destroy(skyr_noise_sampler* sampler);
 uint64_t skyr_noise_sampler_handle(const skyr_noise_sampler* sampler);
+uint64_t skyr_noise_sampler_nearest_handle(const skyr_noise_sampler* sampler);
 
 /* ---- material plug-ins (IVolumetricCloudMaterial) --------------------- */
 #define SKYR_MATERIAL_DEFAULT0 0 /* VolumetricCloudDefaultMaterial0 (VolumetricCloudDefaultMaterial0.glsl) */
@@ -146,9 +148,11 @@ typedef struct skyr_cloud_textures {
     const void* voxel_expanded;
     int cloud_map_expanded_channels, detail_expanded_channels;
     int displacement_expanded_channels, voxel_expanded_channels;
-    /* optional hardware samplers (skyr_noise_sampler_handle, 0 = none) of
-     * channel 0 of the cloud map and of the detail texture */
+    /* optional hardware samplers of channel 0 of the cloud map and of the
+     * detail texture (0 = none): skyr_noise_sampler_handle (magnified, LINEAR)
+     * and skyr_noise_sampler_nearest_handle (minified, NEAREST per level) */
     uint64_t cloud_map_sampler, detail_sampler;
+    uint64_t cloud_map_sampler_nearest, detail_sampler_nearest;
 } skyr_cloud_textures;
 
 /* ---- volumetric cloud (VolumetricCloud) ------------------------------ */

@@ -227,7 +227,8 @@ class CloudTextures(C.Structure):
                 ("displacement_expanded", C.c_void_p), ("voxel_expanded", C.c_void_p),
                 ("cloud_map_expanded_channels", C.c_int), ("detail_expanded_channels", C.c_int),
                 ("displacement_expanded_channels", C.c_int), ("voxel_expanded_channels", C.c_int),
-                ("cloud_map_sampler", C.c_uint64), ("detail_sampler", C.c_uint64)]
+                ("cloud_map_sampler", C.c_uint64), ("detail_sampler", C.c_uint64),
+                ("cloud_map_sampler_nearest", C.c_uint64), ("detail_sampler_nearest", C.c_uint64)]
 
 
 class CloudParameters(C.Structure):
@@ -264,6 +265,7 @@ _SIGNATURES.update({
     "skyr_noise_sampler_update": (C.c_int, [P, P, P]),
     "skyr_noise_sampler_destroy": (C.c_int, [P]),
     "skyr_noise_sampler_handle": (C.c_uint64, [P]),
+    "skyr_noise_sampler_nearest_handle": (C.c_uint64, [P]),
     "skyr_cloud_parameters_default": (C.c_int, [C.POINTER(CloudParameters)]),
     "skyr_cloud_render": (C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters),
                                     C.POINTER(CloudMaterial), C.POINTER(CloudTextures), C.POINTER(CloudView),

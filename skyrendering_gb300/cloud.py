@@ -67,8 +67,13 @@ class NoiseTexture:
 
     @property
     def sampler(self) -> int:
-        """The sampler's texture-object handle, 0 without one."""
+        """The LINEAR level-0 sampler's texture-object handle, 0 without one."""
         return int(_abi.lib().skyr_noise_sampler_handle(self._sampler)) if self._sampler else 0
+
+    @property
+    def sampler_nearest(self) -> int:
+        """The NEAREST every-level sampler's texture-object handle, 0 without one."""
+        return int(_abi.lib().skyr_noise_sampler_nearest_handle(self._sampler)) if self._sampler else 0
 
     def close_sampler(self) -> None:
         if self._sampler:
@@ -119,6 +124,7 @@ def textures_struct(cloud_map: NoiseTexture | None = None, detail: NoiseTexture 
                 setattr(t, name + "_expanded_channels", tex.expanded_channels)
             if name in ("cloud_map", "detail") and tex.sampler:
                 setattr(t, name + "_sampler", tex.sampler)
+                setattr(t, name + "_sampler_nearest", tex.sampler_nearest)
     return t
 
 

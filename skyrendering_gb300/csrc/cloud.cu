@@ -139,10 +139,11 @@ static void derive_fast_consts(const skyr_cloud_material& m, const skyr_cloud_te
         cd.width != cd.height || cd.depth != 1 || dd.width != dd.height || dd.width != dd.depth || dd.depth < 2)
         return;
     auto fill = [&](FastTex& t, const DTex& d, const skyr_noise_texture_desc& desc, double repeat,
-                    uint64_t sampler) {
+                    uint64_t sampler, uint64_t sampler_nearest) {
         t.base = d.base;
         t.ex = d.ex;
         t.tex = sampler;
+        t.tex_near = sampler_nearest;
         t.w = desc.width;
         t.h = desc.height;
         t.d = desc.depth;
@@ -160,8 +161,8 @@ static void derive_fast_consts(const skyr_cloud_material& m, const skyr_cloud_te
             t.off[l] = l < d.levels ? (unsigned)noise_level_offset(&desc, l) : 0u;
     };
     FastConsts& f = mc.fast;
-    fill(f.cm, mc.cloud_map_tex, cd, m.cloud_map_repeat_size, tex.cloud_map_sampler);
-    fill(f.dt, mc.detail_tex, dd, m.detail_repeat_size, tex.detail_sampler);
+    fill(f.cm, mc.cloud_map_tex, cd, m.cloud_map_repeat_size, tex.cloud_map_sampler, tex.cloud_map_sampler_nearest);
+    fill(f.dt, mc.detail_tex, dd, m.detail_repeat_size, tex.detail_sampler, tex.detail_sampler_nearest);
     // Material1's terms in 0..255 texel units (VolumetricCloudDefaultMaterial1.glsl:18-28)
     const double e = m.base_edge_hardness, hh = m.base_height_hardness;
     f.cov_a = (float)(e / 255.0);

@@ -15,11 +15,12 @@
 //     multiply-add with saturation;
 //   * a level's byte offset is one constant load (kernel parameters are
 //     __grid_constant__), not a loop over the levels above it;
-//   * where the caller gives a hardware sampler of level 0
-//     (skyr_noise_sampler), the magnified LINEAR fetch is one texture
-//     instruction: the texture unit filters UNORM8 texels with 8-bit
-//     fixed-point weights, as GL does for the reference's textures, and the
-//     filter arithmetic leaves the SM's pipes.
+//   * where the caller gives hardware samplers (skyr_noise_sampler), the
+//     magnified LINEAR fetch is one texture instruction -- the texture unit
+//     filters UNORM8 texels with 8-bit fixed-point weights, as GL does for the
+//     reference's textures, and the filter arithmetic leaves the SM's pipes --
+//     and the minified NEAREST fetch is one texture instruction at the level
+//     computed here (the texel addressing and the REPEAT wrap leave the SM).
 // The host picks this path (MaterialConsts::fast_ok) only when every
 // condition holds, square / cubic textures included; anything else runs the
 // general sample_sigma_t.
@@ -73,6 +74,12 @@ template <bool D3>
 __device__ __forceinline__ float fast_nearest(const FastTex& T, float u, float v, float s, float d2) {
     float lambda = fminf(fmaf(0.5f, __log2f(d2), T.lod_k), 1000.f);
     int l = min((int)ceilf(lambda + 0.5f) - 1, T.last);
+    if (T.tex_near) {  // the texture unit's NEAREST at level l (REPEAT), the byte itself
+        const cudaTextureObject_t o = (cudaTextureObject_t)T.tex_near;
+        const unsigned b = D3 ? (unsigned)tex3DLod<unsigned char>(o, u, v, s, (float)l)
+                              : (unsigned)tex2DLod<unsigned char>(o, u, v, (float)l);
+        return __uint_as_float(0x4B000000u | b) - 8388608.f;
+    }
     unsigned wl = (unsigned)T.w >> l, mask = wl - 1;
     float scale = T.fw * __int_as_float((127 - l) << 23);  // (size >> l) as a float: size * 2^-l
     unsigned x = (unsigned)(int)floorf(u * scale) & mask, y = (unsigned)(int)floorf(v * scale) & mask;

@@ -143,7 +143,8 @@ struct SampleInfoD {
 struct FastTex {
     const uint8_t* base;  // channel 0 of level l at base + off[l]
     const void* ex;       // expanded level 0 of channel 0 (uint32 per 2D texel, uint64 per 3D texel)
-    unsigned long long tex;  // hardware sampler of level 0, channel 0 (cudaTextureObject_t), or 0
+    unsigned long long tex;       // hardware sampler of level 0, channel 0, LINEAR (cudaTextureObject_t), or 0
+    unsigned long long tex_near;  // hardware sampler of every level, channel 0, NEAREST per level, or 0
     int w, h, d;          // level-0 size (powers of two; d = 1 for a 2D texture)
     int last;             // index of the last mip level
     float fw, fh, fd;     // level-0 size as floats

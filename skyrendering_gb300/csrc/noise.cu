@@ -240,25 +240,43 @@ int skyr_noise_expand(skyr_ctx* ctx, const skyr_noise_texture_desc* desc, const 
 
 struct skyr_noise_sampler {
     int device = 0;
-    cudaArray_t array = nullptr;
+    cudaArray_t array = nullptr;            // level 0: LINEAR filtering (magnification)
     cudaTextureObject_t tex = 0;
+    cudaMipmappedArray_t mips = nullptr;    // every level: NEAREST at an explicit level (minification)
+    cudaTextureObject_t tex_nearest = 0;
     skyr_noise_texture_desc desc{};
     int channel = 0;
 };
 
 namespace {
 // Channel `channel` of level 0 of `tex` (channel-planar layout) into the sampler's array.
-int sampler_copy(skyr_ctx* ctx, skyr_noise_sampler* smp, const void* tex) {
+// Channel `channel` of level `level` of `tex` (per level channel-planar) into `dst`.
+int level_copy(skyr_ctx* ctx, const skyr_noise_sampler* smp, const void* tex, int level, cudaArray_t dst) {
     const skyr_noise_texture_desc& d = smp->desc;
-    const bool d3 = d.depth > 1;
-    const size_t plane = (size_t)d.width * d.height * d.depth;
+    const int w = std::max(d.width >> level, 1), h = std::max(d.height >> level, 1),
+              dp = std::max(d.depth >> level, 1);
+    const size_t plane = (size_t)w * h * dp;
     cudaMemcpy3DParms cp{};
-    cp.srcPtr = make_cudaPitchedPtr(const_cast<uint8_t*>(reinterpret_cast<const uint8_t*>(tex)) + smp->channel * plane,
-                                    (size_t)d.width, (size_t)d.width, (size_t)d.height);
-    cp.dstArray = smp->array;
-    cp.extent = make_cudaExtent((size_t)d.width, (size_t)d.height, d3 ? (size_t)d.depth : 1);
+    cp.srcPtr = make_cudaPitchedPtr(const_cast<uint8_t*>(reinterpret_cast<const uint8_t*>(tex)) +
+                                        noise_level_offset(&d, level) + smp->channel * plane,
+                                    (size_t)w, (size_t)w, (size_t)h);
+    cp.dstArray = dst;
+    cp.extent = make_cudaExtent((size_t)w, (size_t)h, d.depth > 1 ? (size_t)dp : 1);
     cp.kind = cudaMemcpyDeviceToDevice;
     return check_cuda(cudaMemcpy3DAsync(&cp, ctx->stream), "copy into the noise sampler");
+}
+
+// Level 0 into the LINEAR array, every level into the mipmapped array.
+int sampler_copy(skyr_ctx* ctx, skyr_noise_sampler* smp, const void* tex) {
+    if (int e = level_copy(ctx, smp, tex, 0, smp->array)) return e;
+    const int levels = noise_levels(&smp->desc);
+    for (int l = 0; l < levels; ++l) {
+        cudaArray_t a = nullptr;
+        if (int e = check_cuda(cudaGetMipmappedArrayLevel(&a, smp->mips, (unsigned)l), "mipmapped array level"))
+            return e;
+        if (int e = level_copy(ctx, smp, tex, l, a)) return e;
+    }
+    return SKYR_OK;
 }
 }  // namespace
 
@@ -269,8 +287,16 @@ int skyr_noise_sampler_destroy(skyr_noise_sampler* sampler) {
     cudaSetDevice(sampler->device);
     int st = SKYR_OK;
     if (sampler->tex) st = check_cuda(cudaDestroyTextureObject(sampler->tex), "cudaDestroyTextureObject");
+    if (sampler->tex_nearest) {
+        int e = check_cuda(cudaDestroyTextureObject(sampler->tex_nearest), "cudaDestroyTextureObject");
+        if (!st) st = e;
+    }
     if (sampler->array) {
         int e = check_cuda(cudaFreeArray(sampler->array), "cudaFreeArray");
+        if (!st) st = e;
+    }
+    if (sampler->mips) {
+        int e = check_cuda(cudaFreeMipmappedArray(sampler->mips), "cudaFreeMipmappedArray");
         if (!st) st = e;
     }
     delete sampler;
@@ -293,7 +319,11 @@ int skyr_noise_sampler_create(skyr_ctx* ctx, const skyr_noise_texture_desc* desc
     const bool d3 = desc->depth > 1;
     cudaChannelFormatDesc fmt = cudaCreateChannelDesc<unsigned char>();
     cudaExtent ext = make_cudaExtent((size_t)desc->width, (size_t)desc->height, d3 ? (size_t)desc->depth : 0);
+    const int levels = noise_levels(desc);
     int e = check_cuda(cudaMalloc3DArray(&smp->array, &fmt, ext, 0), "cudaMalloc3DArray(noise sampler)");
+    if (!e)
+        e = check_cuda(cudaMallocMipmappedArray(&smp->mips, &fmt, ext, (unsigned)levels, 0),
+                       "cudaMallocMipmappedArray(noise sampler)");
     if (!e) e = sampler_copy(ctx, smp, tex);
     if (!e) {
         cudaResourceDesc rd{};
@@ -305,6 +335,21 @@ int skyr_noise_sampler_create(skyr_ctx* ctx, const skyr_noise_texture_desc* desc
         td.readMode = cudaReadModeNormalizedFloat;                                         // UNORM8
         td.normalizedCoords = 1;
         e = check_cuda(cudaCreateTextureObject(&smp->tex, &rd, &td, nullptr), "cudaCreateTextureObject");
+    }
+    if (!e) {
+        // GL NEAREST_MIPMAP_NEAREST at a level the caller chooses (tex*Lod with an integer level)
+        cudaResourceDesc rd{};
+        rd.resType = cudaResourceTypeMipmappedArray;
+        rd.res.mipmap.mipmap = smp->mips;
+        cudaTextureDesc td{};
+        td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeWrap;  // GL REPEAT
+        td.filterMode = cudaFilterModePoint;
+        td.mipmapFilterMode = cudaFilterModePoint;
+        td.readMode = cudaReadModeElementType;                                             // the byte itself
+        td.normalizedCoords = 1;
+        td.minMipmapLevelClamp = 0.f;
+        td.maxMipmapLevelClamp = (float)(levels - 1);
+        e = check_cuda(cudaCreateTextureObject(&smp->tex_nearest, &rd, &td, nullptr), "cudaCreateTextureObject");
     }
     if (e) {
         skyr_noise_sampler_destroy(smp);
@@ -323,6 +368,10 @@ int skyr_noise_sampler_update(skyr_ctx* ctx, skyr_noise_sampler* sampler, const 
 
 uint64_t skyr_noise_sampler_handle(const skyr_noise_sampler* sampler) {
     return sampler ? (uint64_t)sampler->tex : 0;
+}
+
+uint64_t skyr_noise_sampler_nearest_handle(const skyr_noise_sampler* sampler) {
+    return sampler ? (uint64_t)sampler->tex_nearest : 0;
 }
 
 int skyr_blue_noise_generate(uint32_t seed, float* out) {

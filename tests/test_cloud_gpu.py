@@ -215,6 +215,28 @@ def test_expanded_layout_renders_like_plain_layout(ctx):
     assert mean_rel(ga, gb) <= 1e-5
 
 
+def test_nearest_samplers_fetch_the_mip_bytes(ctx):
+    """The minified fetches (NEAREST_MIPMAP_NEAREST at the level the raymarch
+    computes) from the texture units' mip arrays against the same fetches from
+    the mip bytes in memory: the texel the texture unit addresses (normalized
+    coordinates, REPEAT) is the one floor(u 2^-l size) & (size 2^-l - 1) picks,
+    up to coordinates within the unit's fixed-point resolution of a texel edge."""
+    cam = W.frame_camera()
+    a = Frame(ctx, cam, 45.0)
+    assert a.vc.textures.cloud_map_sampler_nearest and a.vc.textures.detail_sampler_nearest
+    t = textures_struct(**a.tex)
+    t.cloud_map_sampler_nearest = 0
+    t.detail_sampler_nearest = 0
+    b = VolumetricCloud(ctx, a.cloud, a.material, t)
+    rgba_b, dist_b = b.render(a.atmo, a.view, a.sizes, a.luts, a.bn)
+    ctx.synchronize()
+    ga, gb = a.rgba.float().cpu().numpy().reshape(-1, 4), rgba_b.float().cpu().numpy().reshape(-1, 4)
+    err = mean_rel(ga[:, :3], gb[:, :3])
+    changed = int((ga[:, :3] != gb[:, :3]).any(axis=1).sum())
+    print(f"nearest samplers against the mip bytes: mean rel {err:.2e}, {changed} pixels differ")
+    assert err <= 1e-4
+
+
 def test_hardware_samplers_filter_like_gl(ctx):
     """The Material1 frame with hardware samplers (the texture units' LINEAR filter,
     8-bit fixed-point weights, as GL filters the reference's textures) against the

@@ -11,7 +11,7 @@
   the committed network (BF16 rounding points mirrored): mean relative error
   of the luminance <= 1e-3, transmittance 1e-5;
 * accuracy: on the 512x640x352 evaluation cloud at 128^2 the network image is
-  within 2.5 % relative L1 of a 32768-spp path-traced reference while single
+  within 2 % relative L1 of a 32768-spp path-traced reference while single
   scattering alone is >= 80 % off (what the trained network gains).
 """
 import ctypes as C
@@ -310,8 +310,9 @@ def test_surrogate_accuracy_and_network_gain(ctx):
     ctx.check_status()
     e_net, e_ss = S.relative_l1(with_net, ref), S.relative_l1(ss_only, ref)
     print(f"relative L1 vs 32768 spp: network {e_net:.4f}, single scattering only {e_ss:.4f}")
-    # the 32768-spp reference's own noise (about 1.2% relative L1) is part of it
-    assert e_net <= 0.025
+    # the target: within 2% (measured 0.0186); the 32768-spp reference's own
+    # noise (about 1.2% relative L1) is part of it
+    assert e_net <= 0.02
     assert e_ss >= 0.8
     assert e_ss >= 15 * e_net
     # the view transmittance is the same with or without the network and matches the path tracer's alpha
