@@ -553,9 +553,10 @@ int grid_setup(const skyr_density_grid* grid, PtConsts& P, GridBox& B) {
 
 // Bytes of a lattice of `nodes` nodes over `grid`: the records, the sun optical
 // depths, then the grid's mip levels 1..kMipLevels (each 256-byte aligned).
-// With M: the levels' sizes, texel sizes and byte offsets from the buffer's
-// start (in data), level 0 being the grid itself.
-size_t lattice_bytes(const skyr_density_grid* grid, size_t nodes, Mips* M) {
+// With M: the levels' sizes and texel sizes, and their addresses in the buffer
+// that starts at `base`; level 0 is the grid itself.
+size_t lattice_bytes(const skyr_density_grid* grid, size_t nodes, Mips* M = nullptr,
+                     const unsigned char* base = nullptr) {
     size_t off = nodes * (kLatQ * 16 + 4);
     int nx = grid->nx, ny = grid->ny, nz = grid->nz;
     if (M) {
@@ -567,20 +568,17 @@ size_t lattice_bytes(const skyr_density_grid* grid, size_t nodes, Mips* M) {
         off = (off + 255) & ~(size_t)255;
         nx = (nx + 1) / 2, ny = (ny + 1) / 2, nz = (nz + 1) / 2;
         if (M)
-            M->level[l] = MipLevel{reinterpret_cast<const unsigned short*>(off), nx, ny, nz,
+            M->level[l] = MipLevel{reinterpret_cast<const unsigned short*>(base + off), nx, ny, nz,
                                    1.f / (grid->voxel_size * (float)(1 << l))};
         off += (size_t)nx * ny * nz * 2;
     }
     return off;
 }
 
-// The mip chain in a lattice's buffer, with absolute device pointers.
+// The mip chain in a lattice's buffer.
 Mips lattice_mips(const skyr_density_grid* grid, const skyr_feature_volume* fv) {
     Mips M;
-    lattice_bytes(grid, (size_t)fv->nx * fv->ny * fv->nz, &M);
-    const unsigned char* base = reinterpret_cast<const unsigned char*>(fv->data);
-    for (int l = 1; l <= kMipLevels; ++l)
-        M.level[l].data = reinterpret_cast<const unsigned short*>(base + reinterpret_cast<size_t>(M.level[l].data));
+    lattice_bytes(grid, (size_t)fv->nx * fv->ny * fv->nz, &M, reinterpret_cast<const unsigned char*>(fv->data));
     return M;
 }
 
@@ -642,7 +640,7 @@ size_t skyr_feature_volume_bytes(const skyr_density_grid* grid, int stride, skyr
         fv->ny = ny;
         fv->nz = nz;
     }
-    return lattice_bytes(grid, (size_t)nx * ny * nz, nullptr);
+    return lattice_bytes(grid, (size_t)nx * ny * nz);
 }
 
 int skyr_feature_volume_build(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
