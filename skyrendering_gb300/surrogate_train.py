@@ -1,7 +1,7 @@
 """Train the multiple-scattering surrogate on path-traced targets.
 
-    python -m skyrendering_gb300.surrogate_train [--clouds 400] [--points 20000] [--paths 128]
-                                                 [--epochs 144] [--out model.npz]
+    python -m skyrendering_gb300.surrogate_train [--clouds 600] [--points 20000] [--paths 128]
+                                                 [--epochs 192] [--out model.npz]
 
 For each of `clouds` seeded synthetic clouds (the voxel scene's generator with
 seeds 1000, 1001, ...; the evaluation cloud 0x5EED is not among them) the grid
@@ -115,11 +115,11 @@ def train(ctx: Context, rec: torch.Tensor, lab: torch.Tensor, val_rec: torch.Ten
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--clouds", type=int, default=400)
+    ap.add_argument("--clouds", type=int, default=600)
     ap.add_argument("--val-clouds", type=int, default=8)
     ap.add_argument("--points", type=int, default=20000)
     ap.add_argument("--paths", type=int, default=128)
-    ap.add_argument("--epochs", type=int, default=144)
+    ap.add_argument("--epochs", type=int, default=192)
     ap.add_argument("--out", default="surrogate_model.npz")
     a = ap.parse_args(argv)
     torch.cuda.set_device(0)
