@@ -83,7 +83,9 @@ size_t skyr_feature_volume_bytes(const skyr_density_grid* grid, int stride, skyr
 /* Build the lattice of `grid` for the sun of `view` (angles, and the frame of
  * `atmosphere` / `cloud`): the grid's mip chain, the position features per node
  * and the optical depth to the sun (a midpoint march at half the voxel edge to
- * the grid box's exit).
+ * the grid box's exit).  Where the grid carries brick majorants
+ * (skyr_grid_majorants, which must then be current) the march skips the
+ * lookups in bricks whose majorant is 0: they add exactly 0.
  * fv->data (skyr_feature_volume_bytes), fv->stride and fv->sigma_ref are the
  * caller's; the node counts and fv->sun are filled in. */
 int skyr_feature_volume_build(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,

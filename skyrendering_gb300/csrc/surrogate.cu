@@ -259,7 +259,17 @@ struct LatticeBuild {
     float step;        // sun optical-depth march step
     float3 axis[3];    // the stencil's axes: the sun, then two perpendiculars
     float spacing[kStencilLevels];  // stencil step at each level: 2 texels of the level
+    float inv_brick;   // 1 / the brick edge (P.maj non-null)
 };
+
+// Whether the grid is empty around p: the brick majorant there is 0, so every
+// trilinear sample in the brick is 0 (its one-voxel apron included).
+__device__ __forceinline__ bool empty_brick(const PtConsts& P, float inv_brick, float3 p) {
+    int i = min(max((int)floorf((p.x - P.origin.x) * inv_brick), 0), P.bx - 1);
+    int j = min(max((int)floorf((p.y - P.origin.y) * inv_brick), 0), P.by - 1);
+    int k = min(max((int)floorf((p.z - P.origin.z) * inv_brick), 0), P.bz - 1);
+    return __ldg(P.maj + ((size_t)k * P.by + j) * P.bx + i) == 0.f;
+}
 
 __global__ void __launch_bounds__(128) feature_lattice_kernel(PtConsts P, GridBox B, Lattice L, LatticeBuild Q,
                                                               Mips M, int stride, uint4* __restrict__ rec,
@@ -299,14 +309,19 @@ __global__ void __launch_bounds__(128) feature_lattice_kernel(PtConsts P, GridBo
         rec[node * kLatQ + q] = make_uint4(mlp::pack_bf16(a[0], a[1]), mlp::pack_bf16(a[2], a[3]),
                                            mlp::pack_bf16(a[4], a[5]), mlp::pack_bf16(a[6], a[7]));
     }
-    // optical depth to the sun: midpoint rule to the exit of the grid box
+    // optical depth to the sun: midpoint rule to the exit of the grid box; a
+    // sample in an empty brick adds exactly 0, so its lookup is skipped
     float t0, t1;
     box_hit(B.lo, B.hi, x, L.sun, t0, t1);
     float od = 0.f;
     if (t1 > 0.f) {
         int steps = min((int)ceilf(t1 / Q.step), kMaxTrackSteps);
         float h = t1 / (float)max(steps, 1);
-        for (int s = 0; s < steps; ++s) od += grid_sigma(P, x + L.sun * ((s + 0.5f) * h));
+        for (int s = 0; s < steps; ++s) {
+            const float3 p = x + L.sun * ((s + 0.5f) * h);
+            if (P.maj && empty_brick(P, Q.inv_brick, p)) continue;
+            od += grid_sigma(P, p);
+        }
         od *= h;
     }
     tau[node] = od;
@@ -544,6 +559,13 @@ int grid_setup(const skyr_density_grid* grid, PtConsts& P, GridBox& B) {
     P.origin = make_float3(grid->origin[0], grid->origin[1], grid->origin[2]);
     P.inv_voxel = 1.f / grid->voxel_size;
     P.density = grid->density;
+    if (grid->majorant && grid->brick >= 1) {  // the brick majorants, when the grid carries them
+        P.maj = grid->majorant;
+        P.bx = skyr_grid_brick_count(grid->nx, grid->brick);
+        P.by = skyr_grid_brick_count(grid->ny, grid->brick);
+        P.bz = skyr_grid_brick_count(grid->nz, grid->brick);
+        P.brick_size = grid->voxel_size * (float)grid->brick;
+    }
     B.lo = P.origin;
     B.hi = make_float3(grid->origin[0] + grid->nx * grid->voxel_size, grid->origin[1] + grid->ny * grid->voxel_size,
                        grid->origin[2] + grid->nz * grid->voxel_size);
@@ -688,6 +710,7 @@ int skyr_feature_volume_build(skyr_ctx* ctx, const skyr_atmosphere_parameters* a
     }
     for (int l = 0; l < kStencilLevels; ++l)
         Q.spacing[l] = grid->voxel_size * (float)(2 << (kStencilFirst + l));
+    Q.inv_brick = P.maj ? 1.f / P.brick_size : 0.f;
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     // the mip chain of the grid, in the lattice's buffer after the optical depths
     const Mips M = lattice_mips(grid, fv);
