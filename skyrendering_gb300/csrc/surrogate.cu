@@ -413,7 +413,15 @@ struct RenderConsts {
     const float* error_table;
     float nbr, inv_ref;  // view-neighbour distance and 1 / sigma_ref
     long long copy_wait_cycles;  // bound of the wait for the network's bulk copy
+    float inv_brick;     // 1 / the brick edge (P.maj non-null)
 };
+
+// The grid's extinction at a march sample: 0 without a lookup where the brick
+// majorant says the brick is empty (the lookup would return exactly 0).
+__device__ __forceinline__ float march_sigma(const PtConsts& P, float inv_brick, float3 x) {
+    if (P.maj && empty_brick(P, inv_brick, x)) return 0.f;
+    return grid_sigma(P, x);
+}
 
 constexpr int kBins = SKYR_SURROGATE_ERROR_BINS;
 
@@ -474,7 +482,7 @@ __global__ void __launch_bounds__(32 * kRenderWarps, 2) surrogate_render_kernel(
     // the far-side feature of sample s is what remains of it past the sample
     float tau_total = 0.f;
     if (R.use_network && hit) {
-        for (int s = 0; s < R.steps; ++s) tau_total += grid_sigma(P, march_point(C.cam, dir, t0, dt, jitter, s));
+        for (int s = 0; s < R.steps; ++s) tau_total += march_sigma(P, R.inv_brick, march_point(C.cam, dir, t0, dt, jitter, s));
         tau_total *= dt;
     }
     float run = 0.f;  // optical depth up to and including the current sample
@@ -483,7 +491,7 @@ __global__ void __launch_bounds__(32 * kRenderWarps, 2) surrogate_render_kernel(
         if (!__any_sync(full, live)) break;
         float t = fmaf((float)s + jitter, dt, t0);
         float3 x = march_point(C.cam, dir, t0, dt, jitter, s);
-        float sigma = live ? grid_sigma(P, x) : 0.f;
+        float sigma = live ? march_sigma(P, R.inv_brick, x) : 0.f;
         run = fmaf(sigma, dt, run);
         bool need = live && sigma > 0.f;
         if (!__any_sync(full, need)) continue;
@@ -823,6 +831,7 @@ int skyr_surrogate_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmos
     R.error_table = sp->error_table;
     R.nbr = 0.1f * B.span;
     R.inv_ref = 1.f / fv->sigma_ref;
+    R.inv_brick = P.maj ? 1.f / P.brick_size : 0.f;
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
     const Mips mips = lattice_mips(grid, fv);
     auto launch = [&](auto tag) -> int {
