@@ -115,7 +115,9 @@ int skyr_surrogate_error_bins(skyr_ctx* ctx, const uint16_t* records, int n, int
  * pixel, may be NULL) receives an absolute error estimate: the network's
  * contribution to the luminance, each step weighted by the relative error of
  * its error-table bin (or by network_error).  `packed` is the network
- * (skyr_mlp_pack) or NULL when use_network is 0. */
+ * (skyr_mlp_pack) or NULL when use_network is 0.  Where the grid carries brick
+ * majorants (which must then be current) march samples in bricks whose
+ * majorant is 0 take no grid lookup: their extinction is exactly 0. */
 int skyr_surrogate_render(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
                           const skyr_cloud_parameters* cloud, const skyr_density_grid* grid,
                           const skyr_pathtrace_parameters* pt, const skyr_cloud_view* view,
