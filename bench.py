@@ -1,12 +1,14 @@
 """Benchmark of the atmosphere-LUT / volumetric-cloud hot path on one GB300.
 
-The timed step (value, e2e) is one plain 1920x1080 frame, replayed from two
-CUDA graphs captured once through the public API (skyr_graph_*):
+The timed step (value, e2e) is one plain 1920x1080 frame, replayed from one
+CUDA graph captured once through the public API (skyr_graph_*):
   * the whole LUT set (transmittance 256x64 / 40 samples, multi-scattering
     32x32 / 64 directions x 20 samples, sky-view 192x108 / 30 samples, aerial
     perspective 32^3 / 40 samples over 32 km), then
   * the per-pixel cloud raymarch (layer 1.5-4.0 km, Material1, 50/km,
     64 primary steps, 6 light-march steps, seeded blue-noise jitter).
+The split into the two parts (lut_set_us, cloud_frame_ms) is timed from the
+same parts captured as two graphs.
 Noise textures (512^2 RG8 weather map, 128^3 RGBA8 base noise) are generated
 once before timing, as the reference regenerates them only when their
 parameters change.  Inputs are seeded synthetic (skyrendering_gb300/workloads.py).
@@ -376,7 +378,7 @@ def batched_frames(ctx, reps: int = 5, n_sets: int = 256, n_views: int = 64):
                       "cloud_block_warps_x": cloud_best.cloud_block_warps_x,
                       "cloud_blocks_per_sm": cloud_best.cloud_blocks_per_sm,
                       "cloud_ray_lanes": cloud_best.cloud_ray_lanes},
-           "autotune_lut_ms": {"transmittance_lanes_4_8_16": lut_times[:3], "view_lanes_4_8_16": lut_times[3:]},
+           "autotune_lut_ms": {"transmittance_lanes_2_4_8_16": lut_times[:4], "view_lanes_2_4_8_16": lut_times[4:]},
            "autotune_cloud_ms": {f"{cloud_tile(w, g)}/{bx}/{occ}/{g}": t
                                  for (w, bx, occ, g), t in zip(B.CLOUD_CANDIDATES, cloud_times)}}
     cap.graph.close()
@@ -691,32 +693,44 @@ def run_skyr(args):
         fs.luts_step()
         fs.cloud_step()
     barrier()
-    # the production form of the step: the LUT set and the raymarch each captured
-    # once into a CUDA graph (skyr_graph_*), replayed every frame; two graphs keep
-    # the per-component split measurable
+    # the production form of the step: the LUT set and the raymarch captured once
+    # into one CUDA graph (skyr_graph_*), replayed every frame.  The same two
+    # parts captured as two graphs give the per-component split.
+    with B.capture(ctx) as frame_cap:
+        fs.luts_step()
+        fs.cloud_step()
     with B.capture(ctx) as lut_cap:
         fs.luts_step()
     with B.capture(ctx) as cloud_cap:
         fs.cloud_step()
-    lut_graph, cloud_graph = lut_cap.graph, cloud_cap.graph
+    frame_graph, lut_graph, cloud_graph = frame_cap.graph, lut_cap.graph, cloud_cap.graph
     for _ in range(3):
+        frame_graph.launch()
         lut_graph.launch()
         cloud_graph.launch()
     barrier()
 
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
+    split_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     with ClockSampler(local) as clk:
         barrier()
         wall0 = time.perf_counter()
         for i in range(args.steps):
             flush.fill_(float(i))  # evict L2 between steps (outside the timed interval)
             ev[i][0].record(stream)
-            lut_graph.launch()
+            frame_graph.launch()
             ev[i][1].record(stream)
-            cloud_graph.launch()
-            ev[i][2].record(stream)
         barrier()
         wall = time.perf_counter() - wall0
+        # the split: the same step as two graph launches with an event between them
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            split_ev[i][0].record(stream)
+            lut_graph.launch()
+            split_ev[i][1].record(stream)
+            cloud_graph.launch()
+            split_ev[i][2].record(stream)
+        barrier()
         # e2e through the public API with host buffers: the blue-noise tile
         # H2D from pinned memory (parameter blocks travel by value in the
         # launches); the frame's two outputs reach pinned host memory through
@@ -728,28 +742,29 @@ def run_skyr(args):
             fs.vc.render_to_host(fs.atmo, fs.view, fs.sizes, fs.luts, fs.bn, out_rgba=host_rgba,
                                  out_distance=host_dist)
 
-        try:
-            with B.capture(ctx) as host_cap:
-                render_to_host()
-            host_graph = host_cap.graph
-            host_launch = host_graph.launch
-        except Exception as exc:  # capture refused: the same call, launched directly
-            print(f"bench: raymarch-to-host graph capture failed ({exc}); launching directly", file=sys.stderr)
-            host_graph, host_launch = None, render_to_host
-
         # the tile's H2D runs on a second stream while the LUT set (which does not
-        # read it) runs, and the raymarch waits for both
+        # read it) runs, and the raymarch waits for both; the whole step is one
+        # CUDA graph (the copy a memcpy node on its own branch)
         copy_stream = torch.cuda.Stream()
         bn_ready = torch.cuda.Event()
 
-        def e2e_step():
+        def e2e_body():
             copy_stream.wait_stream(stream)  # the previous step's raymarch has read the tile
             with torch.cuda.stream(copy_stream):
                 fs.bn.copy_(fs.bn_host, non_blocking=True)
                 bn_ready.record(copy_stream)
-            lut_graph.launch()
+            fs.luts_step()
             stream.wait_event(bn_ready)
-            host_launch()
+            render_to_host()
+
+        try:
+            with B.capture(ctx) as e2e_cap:
+                e2e_body()
+            e2e_graph = e2e_cap.graph
+            e2e_step, e2e_form = e2e_graph.launch, "one CUDA graph"
+        except Exception as exc:  # capture refused: the same calls, launched directly
+            print(f"bench: e2e graph capture failed ({exc}); launching directly", file=sys.stderr)
+            e2e_graph, e2e_step, e2e_form = None, e2e_body, "direct launches"
 
         for _ in range(3):
             e2e_step()
@@ -761,9 +776,9 @@ def run_skyr(args):
         e1.record(stream)
         barrier()
     e2e_ms = e0.elapsed_time(e1) / args.steps
-    lut_ms = [a.elapsed_time(b) for a, b, _ in ev]
-    cloud_ms = [b.elapsed_time(c) for _, b, c in ev]
-    frame_ms = [a.elapsed_time(c) for a, _, c in ev]
+    lut_ms = [a.elapsed_time(b) for a, b, _ in split_ev]
+    cloud_ms = [b.elapsed_time(c) for _, b, c in split_ev]
+    frame_ms = [a.elapsed_time(b) for a, b in ev]
     ms = statistics.mean(frame_ms)
     if world > 1:
         ms = max_over_ranks(ms, "cuda")
@@ -784,8 +799,8 @@ def run_skyr(args):
     torch.cuda.synchronize()
     e2e_matches = bool(torch.equal(host_rgba.view(torch.int16), fs.rgba.cpu().view(torch.int16)) and
                        torch.equal(host_dist.view(torch.int32), fs.dist.cpu().view(torch.int32)))
-    if host_graph is not None:
-        host_graph.close()
+    if e2e_graph is not None:
+        e2e_graph.close()
 
     clocks = clk.summary()
     hbm_peak, peak_kind = peaks()
@@ -822,7 +837,9 @@ def run_skyr(args):
                                "Material1 50/km, 64 steps, 6 light steps)",
                    "l2": "flushed between timed steps (512 MB write outside the timed interval)",
                    "parallelism": f"replicas x{world}",
-                   "launch": "two CUDA graphs per step (LUT set, raymarch), captured once",
+                   "launch": "one CUDA graph per step (LUT set + raymarch), captured once; lut_set_us and "
+                             "cloud_frame_ms from the same two parts captured as two graphs, timed in a second "
+                             "loop of as many steps with an event between the launches",
                    "tuning": {"transmittance_lanes": lut_tuned.transmittance_lanes,
                               "view_lanes": lut_tuned.view_lanes,
                               "cloud_tile": cloud_tile(cloud_tuned.cloud_tile_width, cloud_tuned.cloud_ray_lanes),
@@ -832,14 +849,15 @@ def run_skyr(args):
         "lut_set_us": statistics.mean(lut_ms) * 1000.0,
         "cloud_frame_ms": cloud_mean,
         "components": {"lut_set_us": statistics.mean(lut_ms) * 1000.0, "cloud_frame_ms": cloud_mean,
+                       "two_graph_frame_ms": statistics.mean(a.elapsed_time(c) for a, _, c in split_ev),
                        "raymarch_samples": samples, "density_evaluations": evals,
                        "density_evaluations_past_coverage": detail_evals,
                        "density_evaluations_per_s": evals / (cloud_mean * 1e-3)},
         "e2e": {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": fs.bn_host.numel() * 4,
                 "d2h_bytes_per_step": host_rgba.numel() * 2 + host_dist.numel() * 4,
-                "path": "blue-noise tile H2D (pinned, on a second stream beside the LUT-set graph) + LUT-set graph "
-                        "+ skyr_cloud_render_to_host graph: the raymarch stores the frame into mapped pinned host "
-                        "buffers while it runs",
+                "path": f"{e2e_form} per step: blue-noise tile H2D (pinned, on a second stream beside the "
+                        "LUT set) + LUT set + skyr_cloud_render_to_host: the raymarch stores the frame into "
+                        "mapped pinned host buffers while it runs",
                 "matches_device_frame": e2e_matches},
         "gpu_launches": kernels_per_step * args.steps,
         "roofline": {"kernel": "cloud_render_kernel", "bound": "fp32", "achieved": fp32_achieved,

@@ -18,8 +18,8 @@ extern "C" {
  * context starts with the defaults and every later launch on it uses its
  * current values. */
 typedef struct skyr_tuning {
-    int transmittance_lanes; /* lanes sharing one transmittance texel: 4, 8, 16 */
-    int view_lanes;          /* lanes sharing one sky-view / aerial-perspective ray: 4, 8, 16 */
+    int transmittance_lanes; /* lanes sharing one transmittance texel: 2, 4, 8, 16 */
+    int view_lanes;          /* lanes sharing one sky-view / aerial-perspective ray: 2, 4, 8, 16 */
     int cloud_tile_width;    /* pixels across one warp's tile (height 32 / width): 4, 8, 16, 32 */
     int cloud_block_warps_x; /* warps side by side in a 4-warp block: 1, 2, 4 */
     int cloud_blocks_per_sm; /* resident blocks per SM the raymarch's registers are cut for: 5 .. 10 */
@@ -35,7 +35,7 @@ int skyr_ctx_get_tuning(const skyr_ctx* ctx, skyr_tuning* t);
  * and `reps` launches each, CUDA events on the context's stream; the call
  * synchronises), keep the fastest in the context and return it in *best.
  * times_ms (may be NULL) receives the mean time per candidate:
- *   LUTs:  [0..2] transmittance lanes 4, 8, 16; [3..5] view lanes 4, 8, 16
+ *   LUTs:  [0..3] transmittance lanes 2, 4, 8, 16; [4..7] view lanes 2, 4, 8, 16
  *          (the LUT set of skyr_update_lut_set; the outputs are overwritten);
  *   cloud: SKYR_CLOUD_TUNE_CANDIDATES = ray lanes {1, 2, 4, 8} x blocks per SM
  *          {5, 6, 7, 8, 9, 10} x the 12 (tile width, block warps x) pairs (4,1) (4,2) (4,4)

@@ -50,9 +50,9 @@ def _luts_args(luts: LutSet):
 
 
 def autotune_luts(ctx: Context, params, renders, n: int, sizes, luts: LutSet, reps: int = 5):
-    """(chosen tuning, times ms: transmittance lanes 4/8/16, view lanes 4/8/16)."""
+    """(chosen tuning, times ms: transmittance lanes 2/4/8/16, view lanes 2/4/8/16)."""
     best = _abi.Tuning()
-    times = (C.c_float * 6)()
+    times = (C.c_float * 8)()
     _abi.call("skyr_autotune_luts", ctx.handle, params, renders, n, C.byref(sizes), *_luts_args(luts), reps,
               C.byref(best), times)
     return best, list(times)

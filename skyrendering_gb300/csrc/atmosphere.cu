@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(128) view_luts_kernel(JobSrc<TABLE> jobs, int 
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
-// Lanes per texel / ray are a tuning choice (skyr_tuning): 4, 8 or 16.
+// Lanes per texel / ray are a tuning choice (skyr_tuning): 2, 4, 8 or 16.
 template <int LANES, bool TABLE>
 static void t_launch(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, float4* out, cudaStream_t st) {
     long long threads = (long long)n_sets * s.transmittance_width * s.transmittance_height * LANES;
@@ -303,6 +303,7 @@ template <bool TABLE>
 cudaError_t launch_transmittance(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, float4* out,
                                  cudaStream_t st, int lanes) {
     switch (lanes) {
+        case 2: t_launch<2, TABLE>(jobs, n_sets, s, out, st); break;
         case 4: t_launch<4, TABLE>(jobs, n_sets, s, out, st); break;
         case 16: t_launch<16, TABLE>(jobs, n_sets, s, out, st); break;
         default: t_launch<8, TABLE>(jobs, n_sets, s, out, st); break;
@@ -359,6 +360,7 @@ template <class S, bool TABLE>
 cudaError_t launch_view_luts(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, const float4* tlut,
                              const S* ms, S* svl, S* svt, S* apl, S* apt, cudaStream_t st, int lanes) {
     switch (lanes) {
+        case 2: v_launch<2, S, TABLE>(jobs, n_sets, s, tlut, ms, svl, svt, apl, apt, st); break;
         case 4: v_launch<4, S, TABLE>(jobs, n_sets, s, tlut, ms, svl, svt, apl, apt, st); break;
         case 16: v_launch<16, S, TABLE>(jobs, n_sets, s, tlut, ms, svl, svt, apl, apt, st); break;
         default: v_launch<8, S, TABLE>(jobs, n_sets, s, tlut, ms, svl, svt, apl, apt, st); break;

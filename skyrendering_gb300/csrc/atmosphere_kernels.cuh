@@ -21,7 +21,7 @@ struct JobSrc<true> {
     __device__ __forceinline__ const LutSetJob& get(int s) const { return t[s]; }
 };
 
-// `lanes`: lanes per texel / ray (4, 8, 16; anything else is 8)
+// `lanes`: lanes per texel / ray (2, 4, 8, 16; anything else is 8)
 template <bool TABLE>
 cudaError_t launch_transmittance(JobSrc<TABLE> jobs, int n_sets, const skyr_lut_sizes& s, float4* out,
                                  cudaStream_t st, int lanes);

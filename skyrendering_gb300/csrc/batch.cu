@@ -47,13 +47,14 @@ namespace {
 
 constexpr int kTileCandidates[SKYR_CLOUD_TILE_CANDIDATES][2] = {
     {4, 1}, {4, 2}, {4, 4}, {8, 1}, {8, 2}, {8, 4}, {16, 1}, {16, 2}, {16, 4}, {32, 1}, {32, 2}, {32, 4}};
-constexpr int kLaneCandidates[3] = {4, 8, 16};
+constexpr int kLaneCandidates[4] = {2, 4, 8, 16};
+constexpr int kLanes = 4;
 
 constexpr int kOccupancyCandidates[6] = {5, 6, 7, 8, 9, 10};
 constexpr int kOccupancies = 6;
 constexpr int kRayLaneCandidates[4] = {1, 2, 4, 8};
 
-bool valid_lanes(int l) { return l == 4 || l == 8 || l == 16; }
+bool valid_lanes(int l) { return l == 2 || l == 4 || l == 8 || l == 16; }
 bool valid_tile(int w, int bx) { return (w == 4 || w == 8 || w == 16 || w == 32) && (bx == 1 || bx == 2 || bx == 4); }
 
 // Mean GPU time of fn() over `reps` launches after one warm-up (events on the
@@ -120,7 +121,7 @@ int skyr_tuning_default(skyr_tuning* t) {
 int skyr_ctx_set_tuning(skyr_ctx* ctx, const skyr_tuning* t) {
     if (!ctx || !t) return set_error(SKYR_EINVAL, "null argument");
     if (!valid_lanes(t->transmittance_lanes) || !valid_lanes(t->view_lanes))
-        return set_error(SKYR_EINVAL, "lanes must be 4, 8 or 16");
+        return set_error(SKYR_EINVAL, "lanes must be 2, 4, 8 or 16");
     if (!valid_tile(t->cloud_tile_width, t->cloud_block_warps_x))
         return set_error(SKYR_EINVAL, "cloud tile width must be 4, 8, 16 or 32 and block warps 1, 2 or 4");
     if (t->cloud_blocks_per_sm < 5 || t->cloud_blocks_per_sm > 10)
@@ -254,13 +255,13 @@ int skyr_autotune_luts(skyr_ctx* ctx, const skyr_atmosphere_parameters* params,
                                      aerial_perspective_luminance, aerial_perspective_transmittance);
     };
     int st = SKYR_OK;
-    float tt[6] = {};
+    float tt[2 * kLanes] = {};
     for (int pass = 0; pass < 2 && !st; ++pass) {
         int best_i = 0;
-        for (int i = 0; i < 3 && !st; ++i) {
+        for (int i = 0; i < kLanes && !st; ++i) {
             (pass == 0 ? ctx->tuning.transmittance_lanes : ctx->tuning.view_lanes) = kLaneCandidates[i];
-            st = time_launches(ctx, reps, run, &tt[pass * 3 + i]);
-            if (!st && tt[pass * 3 + i] < tt[pass * 3 + best_i]) best_i = i;
+            st = time_launches(ctx, reps, run, &tt[pass * kLanes + i]);
+            if (!st && tt[pass * kLanes + i] < tt[pass * kLanes + best_i]) best_i = i;
         }
         if (!st) (pass == 0 ? t.transmittance_lanes : t.view_lanes) = kLaneCandidates[best_i];
         ctx->tuning = t;

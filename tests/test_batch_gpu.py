@@ -80,7 +80,7 @@ def test_lut_batch_matches_update_lut_set(sctx, fmt):
     b.close()
 
 
-@pytest.mark.parametrize("lanes", [4, 16])
+@pytest.mark.parametrize("lanes", [2, 4, 16])
 def test_lut_lanes_variants(sctx, lanes):
     params, renders = W.batched_lut_sets(6)
     sizes = W.plain_lut_sizes(0)
@@ -157,9 +157,10 @@ def test_autotuners(sctx):
     sizes = W.plain_lut_sizes(1)
     luts = LutSet.allocate(sizes, 16)
     best, times = B.autotune_luts(sctx, params, renders, 16, sizes, luts, reps=2)
-    assert best.transmittance_lanes in (4, 8, 16) and best.view_lanes in (4, 8, 16)
-    assert all(t > 0 for t in times)
-    assert min(times[:3]) == pytest.approx(times[[4, 8, 16].index(best.transmittance_lanes)])
+    assert best.transmittance_lanes in (2, 4, 8, 16) and best.view_lanes in (2, 4, 8, 16)
+    assert len(times) == 8 and all(t > 0 for t in times)
+    assert min(times[:4]) == pytest.approx(times[[2, 4, 8, 16].index(best.transmittance_lanes)])
+    assert min(times[4:]) == pytest.approx(times[4 + [2, 4, 8, 16].index(best.view_lanes)])
     got = B.tuning(sctx)
     assert (got.transmittance_lanes, got.view_lanes) == (best.transmittance_lanes, best.view_lanes)
     cl = Clouds(sctx)
@@ -210,6 +211,8 @@ def test_batched_subset_matches_oracle(sctx):
 def test_invalid_arguments(sctx):
     with pytest.raises(_abi.SkyrError):
         B.set_tuning(sctx, transmittance_lanes=5)
+    with pytest.raises(_abi.SkyrError):
+        B.set_tuning(sctx, view_lanes=1)
     with pytest.raises(_abi.SkyrError):
         B.set_tuning(sctx, cloud_tile_width=64)
     with pytest.raises(_abi.SkyrError):
