@@ -93,23 +93,7 @@ struct GridBox {
 __device__ __forceinline__ float mip_value(const MipLevel& M, float3 origin, float3 p) {
     float gx = (p.x - origin.x) * M.inv_voxel - 0.5f, gy = (p.y - origin.y) * M.inv_voxel - 0.5f,
           gz = (p.z - origin.z) * M.inv_voxel - 0.5f;
-    float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
-    float a = gx - fx, b = gy - fy, c = gz - fz;
-    int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
-    auto at = [&](int x, int y, int z) -> float {
-        if ((unsigned)x >= (unsigned)M.nx || (unsigned)y >= (unsigned)M.ny || (unsigned)z >= (unsigned)M.nz)
-            return 0.f;
-        return __half2float(__ushort_as_half(__ldg(M.data + ((size_t)z * M.ny + y) * M.nx + x)));
-    };
-    float r[2];
-#pragma unroll
-    for (int dz = 0; dz < 2; ++dz) {
-        float t00 = at(x0, y0, z0 + dz), t10 = at(x0 + 1, y0, z0 + dz);
-        float t01 = at(x0, y0 + 1, z0 + dz), t11 = at(x0 + 1, y0 + 1, z0 + dz);
-        float top = fmaf(a, t10 - t00, t00), bot = fmaf(a, t11 - t01, t01);
-        r[dz] = fmaf(b, bot - top, top);
-    }
-    return fmaf(c, r[1] - r[0], r[0]);
+    return trilinear_zero_border(M.data, M.nx, M.ny, M.nz, gx, gy, gz);
 }
 
 // Level l + 1 texel (x, y, z) from level l: the mean of the texels that exist.

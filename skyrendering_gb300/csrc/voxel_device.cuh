@@ -63,10 +63,34 @@ __device__ __forceinline__ float rand01(const PtConsts& P, uint32_t& seed) {
     return r;
 }
 
-__device__ __forceinline__ float grid_voxel(const PtConsts& P, int x, int y, int z) {
-    if ((unsigned)x >= (unsigned)P.nx || (unsigned)y >= (unsigned)P.ny || (unsigned)z >= (unsigned)P.nz) return 0.f;
-    unsigned short h = __ldg(P.grid + ((size_t)z * P.ny + y) * P.nx + x);
-    return __half2float(__ushort_as_half(h));
+// Trilinear between texel centres of an FP16 volume of nx x ny x nz texels
+// with a zero border, at continuous texel coordinates (gx, gy, gz) (texel
+// centres at integers): a texel outside the volume reads 0.  The eight texels
+// are addressed from one base offset, and each axis is tested once per end;
+// a texel that fails its test is not loaded.
+__device__ __forceinline__ float trilinear_zero_border(const unsigned short* __restrict__ data, int nx, int ny,
+                                                       int nz, float gx, float gy, float gz) {
+    float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
+    float a = gx - fx, b = gy - fy, c = gz - fz;
+    int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
+    const bool vx0 = (unsigned)x0 < (unsigned)nx, vx1 = (unsigned)(x0 + 1) < (unsigned)nx;
+    const bool vy0 = (unsigned)y0 < (unsigned)ny, vy1 = (unsigned)(y0 + 1) < (unsigned)ny;
+    const long long sy = nx, sz = (long long)nx * ny;
+    const long long base = (long long)z0 * sz + (long long)y0 * sy + x0;
+    auto texel = [&](long long i, bool v) -> float {
+        return v ? __half2float(__ushort_as_half(__ldg(data + i))) : 0.f;
+    };
+    float r[2];
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz) {
+        const bool vz = (unsigned)(z0 + dz) < (unsigned)nz;
+        const long long i = base + dz * sz;
+        float t00 = texel(i, vz && vy0 && vx0), t10 = texel(i + 1, vz && vy0 && vx1);
+        float t01 = texel(i + sy, vz && vy1 && vx0), t11 = texel(i + sy + 1, vz && vy1 && vx1);
+        float top = fmaf(a, t10 - t00, t00), bot = fmaf(a, t11 - t01, t01);
+        r[dz] = fmaf(b, bot - top, top);
+    }
+    return fmaf(c, r[1] - r[0], r[0]);
 }
 
 // trilinear between voxel centres, zero border
@@ -74,18 +98,7 @@ __device__ __forceinline__ float grid_sigma(const PtConsts& P, float3 p) {
     float gx = (p.x - P.origin.x) * P.inv_voxel - 0.5f;
     float gy = (p.y - P.origin.y) * P.inv_voxel - 0.5f;
     float gz = (p.z - P.origin.z) * P.inv_voxel - 0.5f;
-    float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
-    float a = gx - fx, b = gy - fy, c = gz - fz;
-    int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
-    float r[2];
-#pragma unroll
-    for (int dz = 0; dz < 2; ++dz) {
-        float t00 = grid_voxel(P, x0, y0, z0 + dz), t10 = grid_voxel(P, x0 + 1, y0, z0 + dz);
-        float t01 = grid_voxel(P, x0, y0 + 1, z0 + dz), t11 = grid_voxel(P, x0 + 1, y0 + 1, z0 + dz);
-        float top = fmaf(a, t10 - t00, t00), bot = fmaf(a, t11 - t01, t01);
-        r[dz] = fmaf(b, bot - top, top);
-    }
-    return fmaf(c, r[1] - r[0], r[0]) * P.density;
+    return trilinear_zero_border(P.grid, P.nx, P.ny, P.nz, gx, gy, gz) * P.density;
 }
 
 // CloudRegionIntersect (PathTracing.comp:57-75)
