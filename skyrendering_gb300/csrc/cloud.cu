@@ -238,6 +238,8 @@ int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud
         c.cam_rho2 = (float)(h * (2.0 * R + h));
     }
     c.jitter_offset = (float)v.frame_id * 0.61803398875f;
+    c.row_pivot = 0;  // march order: the identity until the launch sets it (march_order)
+    c.row_dir = 1;
     c.sun_illuminance_scale = cp.sun_illuminance_scale;
     c.max_raymarch_distance = cp.max_raymarch_distance;
     c.max_raymarch_steps = cp.max_raymarch_steps;
@@ -334,6 +336,61 @@ int derive_cloud_consts(const skyr_atmosphere_parameters& atmo, const skyr_cloud
     return SKYR_OK;
 }
 
+// Length of the view ray with cos(view, up) = mu from the camera's altitude h
+// inside the cloud layer [bottom, top] above a sphere of radius R, up to the
+// distance `end` or the ground, in double precision.
+static double layer_path(double R, double h, double bottom, double top, double mu, double end) {
+    const double r = R + h, rm = r * mu;
+    auto inside = [&](double s, double& t0, double& t1) {  // the ray's stretch inside the sphere of radius s
+        const double disc = rm * rm - (r - s) * (r + s);
+        if (disc < 0.0) return false;
+        const double q = std::sqrt(disc);
+        t0 = -rm - q;
+        t1 = -rm + q;
+        return true;
+    };
+    double g0, g1, o0, o1, i0, i1;
+    if (r > R && inside(R, g0, g1) && g0 > 0.0) end = std::min(end, g0);
+    if (!inside(R + top, o0, o1)) return 0.0;
+    const double a = std::max(0.0, o0), b = std::min(end, o1);
+    if (!(b > a)) return 0.0;
+    double len = b - a;
+    if (inside(R + bottom, i0, i1)) {
+        const double lo = std::max(a, i0), hi = std::min(b, i1);
+        if (hi > lo) len -= hi - lo;
+    }
+    return len;
+}
+
+// The raymarch's block-row order (march_row): outward from the block row whose
+// centre ray runs the longest way through the cloud layer within the visible
+// distance, towards the longer-running neighbour first.  The rays that graze
+// the layer are the costliest, so they start first and the launch ends on
+// cheap rows; with no row in the layer the order stays the identity.  Every
+// pixel's result is the same in any order.
+static void march_order(CloudConsts& C, int rows_per_block, int block_rows) {
+    auto path = [&](int by) -> double {
+        if (by < 0 || by >= block_rows) return -1.0;
+        const int py = std::min(by * rows_per_block + rows_per_block / 2, C.height - 1);
+        const double y = 2.0 * ((py + 0.5) / C.height) - 1.0;  // centre column, no depth
+        const double dx = (double)C.a1.x * y + C.af.x, dy = (double)C.a1.y * y + C.af.y,
+                     dz = (double)C.a1.z * y + C.af.z, wv = (double)C.w1 * y + C.wf;
+        const double len = std::sqrt(dx * dx + dy * dy + dz * dz);
+        if (!(len > 0.0) || wv == 0.0) return 0.0;
+        const double mu = dz / len * (wv < 0.0 ? -1.0 : 1.0);
+        const double vis = std::min(len / std::fabs(wv), (double)C.max_visible_distance);
+        return layer_path(C.R, C.cam.z, C.bottom, C.top, mu, vis);
+    };
+    int p = 0;
+    double best = 0.0;
+    for (int by = 0; by < block_rows; ++by) {
+        const double l = path(by);
+        if (l > best) best = l, p = by;
+    }
+    C.row_pivot = p;
+    C.row_dir = path(p + 1) >= path(p - 1) ? 1 : -1;
+}
+
 int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_parameters* atmosphere,
                     const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
                     const skyr_cloud_textures* textures, const skyr_cloud_view* view, const skyr_lut_sizes* sizes,
@@ -377,6 +434,7 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
     const int G = ctx->tuning.cloud_ray_lanes, tw = std::min(tile_w, 32 / G);
     const int bw = tw * warps_x, bh = (32 / G / tw) * (4 / warps_x);
     dim3 grid((C.width + bw - 1) / bw, (C.height + bh - 1) / bh);
+    march_order(C, bh, (int)grid.y);
     const float4* T = reinterpret_cast<const float4*>(transmittance);
     const bool half = sizes->format == SKYR_FORMAT_RGBA16F;
     const int occ = ctx->tuning.cloud_blocks_per_sm;
@@ -386,6 +444,7 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
         const int tw1 = std::min(tile_w, 32);
         dim3 grid1((C.width + tw1 * warps_x - 1) / (tw1 * warps_x),
                    (C.height + (32 / tw1) * (4 / warps_x) - 1) / ((32 / tw1) * (4 / warps_x)));
+        march_order(C, (32 / tw1) * (4 / warps_x), (int)grid1.y);
         launch_cloud_render_counted(half, grid1, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
                                     aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,
                                     tile_w, warps_x);

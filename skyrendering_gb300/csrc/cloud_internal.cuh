@@ -217,7 +217,23 @@ struct CloudConsts {
     const float2* cb_index;
     const float* cb_depth;
     int cb_w, cb_h;
+    // the order in which the raymarch's block rows start (march_row): outward
+    // from block row row_pivot, the side of row_dir (+1 or -1) first
+    int row_pivot, row_dir;
 };
+
+// The block row that the k-th of n block rows marches: p, then alternately
+// p + d, p - d, p + 2d, p - 2d, ... while both sides last, then the rest of
+// the longer side outward.  A bijection of [0, n) for p in [0, n) and d = +-1.
+__device__ __forceinline__ int march_row(int k, int n, int p, int d) {
+    p = min(max(p, 0), n - 1);
+    d = d < 0 ? -1 : 1;
+    const int first = d > 0 ? n - 1 - p : p, second = d > 0 ? p : n - 1 - p, m = min(first, second);
+    int off;
+    if (k <= 2 * m) off = (k & 1) ? (k + 1) >> 1 : -(k >> 1);
+    else off = first > second ? k - m : -(k - m);
+    return p + d * off;
+}
 
 // The checkerboard input of a quarter-resolution raymarch.
 struct CloudCheckerboard {

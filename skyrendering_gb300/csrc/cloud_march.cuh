@@ -268,7 +268,8 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(const __grid_co
     int ray = lane / G, sub = lane % G;
     int rw = min(tile_w, 32 / G), tile_h = 32 / G / rw, warps_y = 4 / warps_x;
     int px = blockIdx.x * (rw * warps_x) + (warp % warps_x) * rw + (ray % rw);
-    int py = blockIdx.y * (tile_h * warps_y) + (warp / warps_x) * tile_h + (ray / rw);
+    int py = march_row((int)blockIdx.y, (int)gridDim.y, C.row_pivot, C.row_dir) * (tile_h * warps_y) +
+             (warp / warps_x) * tile_h + (ray / rw);
     if (px >= C.width || py >= C.height) return;  // the whole ray group leaves together
     const unsigned gmask = G == 1 ? 1u << lane : ((1u << G) - 1u) << (lane & ~(G - 1));
     size_t pix = (size_t)py * C.width + px;
