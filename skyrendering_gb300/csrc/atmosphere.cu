@@ -95,14 +95,22 @@ __global__ void __launch_bounds__(128) transmittance_kernel(JobSrc<TABLE> jobs, 
 }
 
 // ---------------------------------------------------------------------------
-// MULTISCATTERING (Atmosphere.glsl:342-438): one 256-thread block per texel.
-// Thread t integrates chunk (t % MS_CHUNKS) of sphere direction t / MS_CHUNKS
-// (GetDirectionFromLocalIndex, :344-355); the chunks of a direction are
-// composed through shuffles, the 64 directions summed through shuffles and a
-// shared-memory pass over the block's warps.
+// MULTISCATTERING (Atmosphere.glsl:342-438): one 128-thread block per texel.
+// The 64 sphere directions of GetDirectionFromLocalIndex (:344-355) are
+// (cos phi sin theta, cos theta, sin phi sin theta) on an 8 x 8 (theta, phi)
+// grid, with the start point on the y axis and the sun in the y-z plane.  The
+// integrand depends on the direction only through its y and z components
+// (the height along the ray, cos(sun, zenith) at each sample, cos(view, sun)),
+// so phi and pi - phi give the same luminance: the phi columns 0, 1, 4, 5 are
+// integrated and stand for their mirrors 3, 2, 7, 6, and the sums over the 32
+// directions are doubled.  Thread t integrates chunk (t % kMsChunks) of
+// direction t / kMsChunks; the chunks of a direction are composed through
+// shuffles, the directions summed through shuffles and a shared-memory pass
+// over the block's warps.
 // ---------------------------------------------------------------------------
 constexpr int kMsChunks = 4;
-constexpr int kMsThreads = 64 * kMsChunks;
+constexpr int kMsDirs = 32;  // mirror pairs of the 64 directions
+constexpr int kMsThreads = kMsDirs * kMsChunks;
 
 template <class S, bool TABLE>
 __global__ void __launch_bounds__(kMsThreads) multiscattering_kernel(JobSrc<TABLE> jobs, int n_sets, LutView L,
@@ -128,10 +136,11 @@ __global__ void __launch_bounds__(kMsThreads) multiscattering_kernel(JobSrc<TABL
     int n = sample_count(0.5f, steps);
     const float iso = 1.f / (4.f * SKYR_PI);
 
-    int index = threadIdx.x / kMsChunks;
+    int pair = threadIdx.x / kMsChunks;
     int chunk = threadIdx.x % kMsChunks;
-    float unit_theta = (0.5f + (float)(index / 8)) / 8.f;
-    float unit_phi = (0.5f + (float)(index % 8)) / 8.f;
+    int phi_col = (pair & 1) | ((pair & 2) << 1);  // 0, 1, 4, 5 (mirrors 3, 2, 7, 6)
+    float unit_theta = (0.5f + (float)(pair >> 2)) / 8.f;
+    float unit_phi = (0.5f + (float)phi_col) / 8.f;
     float cos_theta = 1.f - 2.f * unit_theta;
     float sin_theta = sqrtf(clamp01(1.f - cos_theta * cos_theta));
     float sphi, cphi;
@@ -176,7 +185,8 @@ __global__ void __launch_bounds__(kMsThreads) multiscattering_kernel(JobSrc<TABL
             L2 += f3(red[i][0], red[i][1], red[i][2]);
             F += f3(red[i][3], red[i][4], red[i][5]);
         }
-        float3 l2 = L2 * (1.f / 64.f), fms = F * (1.f / 64.f);
+        // each pair counts twice: (2 x the sum over 32 pairs) / 64 directions
+        float3 l2 = L2 * (1.f / 32.f), fms = F * (1.f / 32.f);
         float3 c = l2 / (f3(1.f) - fms);
         store_rgba(out, (size_t)set * per_set + t, c, 1.f);
     }
