@@ -1,14 +1,16 @@
 """Benchmark of the atmosphere-LUT / volumetric-cloud hot path on one GB300.
 
-The timed step (value, e2e) is one plain 1920x1080 frame, replayed from one
-CUDA graph captured once through the public API (skyr_graph_*):
+The timed step (value, e2e) is one plain 1920x1080 frame, one
+skyr_render_frame call replayed from a CUDA graph captured once through the
+public API (skyr_graph_*):
   * the whole LUT set (transmittance 256x64 / 40 samples, multi-scattering
     32x32 / 64 directions x 20 samples, sky-view 192x108 / 30 samples, aerial
     perspective 32^3 / 40 samples over 32 km), then
   * the per-pixel cloud raymarch (layer 1.5-4.0 km, Material1, 50/km,
-    64 primary steps, 6 light-march steps, seeded blue-noise jitter).
+    64 primary steps, 6 light-march steps, seeded blue-noise jitter), launched
+    as a programmatic dependent of the LUT set's last pass.
 The split into the two parts (lut_set_us, cloud_frame_ms) is timed from the
-same parts captured as two graphs.
+two calls (skyr_update_lut_set, skyr_cloud_render) captured as two graphs.
 Noise textures (512^2 RG8 weather map, 128^3 RGBA8 base noise) are generated
 once before timing, as the reference regenerates them only when their
 parameters change.  Inputs are seeded synthetic (skyrendering_gb300/workloads.py).
@@ -217,6 +219,12 @@ class FrameState:
     def cloud_step(self):
         self.vc.render(self.atmo, self.view, self.sizes, self.luts, self.bn, out_rgba=self.rgba,
                        out_distance=self.dist)
+
+    def frame_step(self, out_rgba=None, out_distance=None, on_host=False):
+        """The LUT set and the raymarch in one call (skyr_render_frame)."""
+        self.vc.render_frame(self.atmo, self.render, self.view, self.sizes, self.luts, self.bn,
+                             out_rgba=self.rgba if out_rgba is None else out_rgba,
+                             out_distance=self.dist if out_distance is None else out_distance, on_host=on_host)
 
 
 def surrogate_vs_pathtracer(ctx, small: int = 256, ref_spp: int = 16384, big: int = 1024):
@@ -693,12 +701,13 @@ def run_skyr(args):
         fs.luts_step()
         fs.cloud_step()
     barrier()
-    # the production form of the step: the LUT set and the raymarch captured once
-    # into one CUDA graph (skyr_graph_*), replayed every frame.  The same two
-    # parts captured as two graphs give the per-component split.
+    # the production form of the step: one skyr_render_frame call (the LUT set,
+    # then the raymarch as a programmatic dependent of its last pass) captured
+    # once into a CUDA graph (skyr_graph_*), replayed every frame.  The two parts
+    # captured as two graphs (skyr_update_lut_set, skyr_cloud_render) give the
+    # per-component split.
     with B.capture(ctx) as frame_cap:
-        fs.luts_step()
-        fs.cloud_step()
+        fs.frame_step()
     with B.capture(ctx) as lut_cap:
         fs.luts_step()
     with B.capture(ctx) as cloud_cap:
@@ -733,29 +742,16 @@ def run_skyr(args):
         barrier()
         # e2e through the public API with host buffers: the blue-noise tile
         # H2D from pinned memory (parameter blocks travel by value in the
-        # launches); the frame's two outputs reach pinned host memory through
-        # skyr_cloud_render_to_host, whose raymarch stores every pixel into the
-        # mapped host buffers (the D2H bytes move while the kernel runs)
+        # launches), then skyr_render_frame with the frame's two outputs in
+        # pinned host memory: its raymarch stores every pixel into the mapped
+        # host buffers, so the D2H bytes move while the kernel runs.  The whole
+        # step is one CUDA graph (the copy a memcpy node).
         host_rgba = torch.empty(fs.rgba.shape, dtype=fs.rgba.dtype, pin_memory=True)
         host_dist = torch.empty(fs.dist.shape, dtype=fs.dist.dtype, pin_memory=True)
-        def render_to_host():
-            fs.vc.render_to_host(fs.atmo, fs.view, fs.sizes, fs.luts, fs.bn, out_rgba=host_rgba,
-                                 out_distance=host_dist)
-
-        # the tile's H2D runs on a second stream while the LUT set (which does not
-        # read it) runs, and the raymarch waits for both; the whole step is one
-        # CUDA graph (the copy a memcpy node on its own branch)
-        copy_stream = torch.cuda.Stream()
-        bn_ready = torch.cuda.Event()
 
         def e2e_body():
-            copy_stream.wait_stream(stream)  # the previous step's raymarch has read the tile
-            with torch.cuda.stream(copy_stream):
-                fs.bn.copy_(fs.bn_host, non_blocking=True)
-                bn_ready.record(copy_stream)
-            fs.luts_step()
-            stream.wait_event(bn_ready)
-            render_to_host()
+            fs.bn.copy_(fs.bn_host, non_blocking=True)
+            fs.frame_step(out_rgba=host_rgba, out_distance=host_dist, on_host=True)
 
         try:
             with B.capture(ctx) as e2e_cap:
@@ -837,9 +833,11 @@ def run_skyr(args):
                                "Material1 50/km, 64 steps, 6 light steps)",
                    "l2": "flushed between timed steps (512 MB write outside the timed interval)",
                    "parallelism": f"replicas x{world}",
-                   "launch": "one CUDA graph per step (LUT set + raymarch), captured once; lut_set_us and "
-                             "cloud_frame_ms from the same two parts captured as two graphs, timed in a second "
-                             "loop of as many steps with an event between the launches",
+                   "launch": "one CUDA graph per step (skyr_render_frame: LUT set + raymarch, the raymarch a "
+                             "programmatic dependent of the LUT set's last pass), captured once; lut_set_us and "
+                             "cloud_frame_ms from the two parts captured as two graphs (skyr_update_lut_set, "
+                             "skyr_cloud_render), timed in a second loop of as many steps with an event between "
+                             "the launches",
                    "tuning": {"transmittance_lanes": lut_tuned.transmittance_lanes,
                               "view_lanes": lut_tuned.view_lanes,
                               "cloud_tile": cloud_tile(cloud_tuned.cloud_tile_width, cloud_tuned.cloud_ray_lanes),
@@ -855,9 +853,9 @@ def run_skyr(args):
                        "density_evaluations_per_s": evals / (cloud_mean * 1e-3)},
         "e2e": {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": fs.bn_host.numel() * 4,
                 "d2h_bytes_per_step": host_rgba.numel() * 2 + host_dist.numel() * 4,
-                "path": f"{e2e_form} per step: blue-noise tile H2D (pinned, on a second stream beside the "
-                        "LUT set) + LUT set + skyr_cloud_render_to_host: the raymarch stores the frame into "
-                        "mapped pinned host buffers while it runs",
+                "path": f"{e2e_form} per step: blue-noise tile H2D (pinned) + skyr_render_frame with host "
+                        "outputs (LUT set, then the raymarch as a programmatic dependent of its last pass, storing "
+                        "the frame into mapped pinned host buffers while it runs)",
                 "matches_device_frame": e2e_matches},
         "gpu_launches": kernels_per_step * args.steps,
         "roofline": {"kernel": "cloud_render_kernel", "bound": "fp32", "achieved": fp32_achieved,

@@ -244,6 +244,30 @@ int skyr_cloud_render_to_host(skyr_ctx* ctx, const skyr_atmosphere_parameters* a
                               const void* aerial_perspective_transmittance, const float* blue_noise,
                               const float* depth, void* host_rgba, float* host_distance);
 
+/* One frame's LUT set and cloud raymarch, in the reference's per-frame order
+ * (AppWindow::Render: AtmosphereRenderer::Render's LUT passes through
+ * RenderViewport, src/SkyRendering/AppWindow.cpp:216, then
+ * VolumetricCloud::Render, :174): skyr_update_lut_set for one parameter set
+ * (atmosphere, render) into the six LUT buffers, then skyr_cloud_render (or,
+ * with outputs_on_host nonzero, skyr_cloud_render_to_host) reading that set's
+ * transmittance and aerial-perspective LUTs.  The results are those of the two
+ * calls, bit for bit.  The raymarch is launched as a programmatic dependent of
+ * the LUT set's last pass: its rays march while the LUT passes finish and wait
+ * for them only before their first LUT read, so part of the raymarch overlaps
+ * the LUT set.  Everything else the raymarch reads (textures, blue noise,
+ * depth, the view's shadow froxel) must be complete when the call is
+ * enqueued, as for the two calls.  All arguments are checked before anything
+ * is enqueued; the sky-view pair may be NULL, the aerial-perspective pair not.
+ * (No reference counterpart as one call.) */
+int skyr_render_frame(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                      const skyr_atmosphere_render_parameters* render, const skyr_lut_sizes* sizes,
+                      void* transmittance, void* multiscattering, void* sky_view_luminance,
+                      void* sky_view_transmittance, void* aerial_perspective_luminance,
+                      void* aerial_perspective_transmittance, const skyr_cloud_parameters* cloud,
+                      const skyr_cloud_material* material, const skyr_cloud_textures* textures,
+                      const skyr_cloud_view* view, const float* blue_noise, const float* depth, void* out_rgba,
+                      float* out_distance, int outputs_on_host);
+
 /* skyr_cloud_render that also accumulates work counters into device memory
  * `counters` (3 x uint64, not cleared): [0] raymarch samples taken,
  * [1] SampleSigmaT evaluations (raymarch + light march), [2] those of them

@@ -277,6 +277,10 @@ _SIGNATURES.update({
 _SIGNATURES["skyr_cloud_render_to_host"] = (
     C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters), C.POINTER(CloudMaterial),
               C.POINTER(CloudTextures), C.POINTER(CloudView), C.POINTER(LutSizes), P, P, P, P, P, P, P])
+_SIGNATURES["skyr_render_frame"] = (
+    C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(AtmosphereRenderParameters), C.POINTER(LutSizes),
+              P, P, P, P, P, P, C.POINTER(CloudParameters), C.POINTER(CloudMaterial), C.POINTER(CloudTextures),
+              C.POINTER(CloudView), P, P, P, P, C.c_int])
 _SIGNATURES["skyr_cloud_render_counted"] = (
     C.c_int, [P, C.POINTER(AtmosphereParameters), C.POINTER(CloudParameters), C.POINTER(CloudMaterial),
               C.POINTER(CloudTextures), C.POINTER(CloudView), C.POINTER(LutSizes), P, P, P, P, P, P, P, P])

@@ -188,6 +188,27 @@ class VolumetricCloud:
                   _ptr(out_distance))
         return out_rgba, out_distance
 
+    def render_frame(self, atmosphere: _abi.AtmosphereParameters, render: _abi.AtmosphereRenderParameters,
+                     view: _abi.CloudView, sizes: _abi.LutSizes, luts: LutSet, blue_noise: torch.Tensor,
+                     depth: torch.Tensor | None = None, out_rgba: torch.Tensor | None = None,
+                     out_distance: torch.Tensor | None = None, on_host: bool = False):
+        """One frame (skyr_render_frame): the LUT set of (atmosphere, render)
+        into `luts` (set 0), then render() -- or render_to_host() with
+        `on_host` -- reading it, the raymarch overlapping the LUT set's end."""
+        if out_rgba is None:
+            out_rgba = (torch.empty((view.height, view.width, 4), dtype=torch.float16, pin_memory=True) if on_host
+                        else torch.empty((view.height, view.width, 4), dtype=torch.float16, device="cuda"))
+        if out_distance is None:
+            out_distance = (torch.empty((view.height, view.width), dtype=torch.float32, pin_memory=True) if on_host
+                            else torch.empty((view.height, view.width), dtype=torch.float32, device="cuda"))
+        _abi.call("skyr_render_frame", self.ctx.handle, C.byref(atmosphere), C.byref(render), C.byref(sizes),
+                  _ptr(luts.transmittance), _ptr(luts.multiscattering), _ptr(luts.sky_view_luminance),
+                  _ptr(luts.sky_view_transmittance), _ptr(luts.aerial_perspective_luminance),
+                  _ptr(luts.aerial_perspective_transmittance), C.byref(self.params), C.byref(self.material),
+                  C.byref(self.textures), C.byref(view), _ptr(blue_noise), _ptr(depth), _ptr(out_rgba),
+                  _ptr(out_distance), 1 if on_host else 0)
+        return out_rgba, out_distance
+
 
 def shadow_sizes(viewport_width: int, viewport_height: int) -> _abi.CloudShadowSizes:
     """512 x 512 map, (w / 12) x (h / 12) x 128 froxel (VolumetricCloud.cpp:52,134-135)."""

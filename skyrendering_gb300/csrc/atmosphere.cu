@@ -13,7 +13,8 @@
 //  * the multi-scattering texel is one 256-thread block (64 sphere directions
 //    x 4 chunks), reduced with shuffles and one shared-memory pass;
 //  * the passes after the first are programmatic dependent launches, so each
-//    one's blocks are scheduled while the previous one drains.
+//    one's blocks are scheduled while the previous one drains; the view pass
+//    lets its own dependents (the raymarch of skyr_render_frame) start at once.
 #include <utility>
 
 #include "skyr_internal.cuh"
@@ -204,6 +205,10 @@ __global__ void __launch_bounds__(128) view_luts_kernel(JobSrc<TABLE> jobs, int 
                                                         int sv_w, int sv_h, int ap_w, int ap_h, int ap_d,
                                                         S* __restrict__ sv_lum, S* __restrict__ sv_trans,
                                                         S* __restrict__ ap_lum, S* __restrict__ ap_trans) {
+    // A programmatic dependent of this pass (the raymarch of skyr_render_frame)
+    // may be scheduled as soon as all its blocks run: it reads the LUTs only
+    // after its own griddepcontrol.wait, that is after this pass has ended.
+    pdl_launch_dependents();
     int gid = blockIdx.x * blockDim.x + threadIdx.x;
     int lane = gid % LANES;
     int ray = gid / LANES;

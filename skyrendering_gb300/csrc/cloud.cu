@@ -397,7 +397,7 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
                     const void* transmittance, const void* aerial_perspective_luminance,
                     const void* aerial_perspective_transmittance, const float* blue_noise, const float* depth,
                     void* out_rgba, float* out_distance, unsigned long long* counters,
-                    const CloudCheckerboard* checkerboard) {
+                    const CloudCheckerboard* checkerboard, int mode) {
     if (!ctx) return set_error(SKYR_EINVAL, "null context");
     if (!atmosphere || !cloud || !material || !textures || !view || !sizes)
         return set_error(SKYR_EINVAL, "null parameter block");
@@ -427,9 +427,11 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
         C.cb_h = checkerboard->half_h;
         depth = nullptr;
     }
+    if (mode & kCloudCheckOnly) return SKYR_OK;
     AtmoConsts A;
     derive_atmo_consts(*atmosphere, A);
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    const bool pdl = (mode & kCloudAfterLuts) && !checkerboard;
     const int tile_w = ctx->tuning.cloud_tile_width, warps_x = ctx->tuning.cloud_block_warps_x;
     const int G = ctx->tuning.cloud_ray_lanes, tw = std::min(tile_w, 32 / G);
     const int bw = tw * warps_x, bh = (32 / G / tw) * (4 / warps_x);
@@ -453,21 +455,47 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
     if (G == 8)
         launch_cloud_render<8>(half, occ, grid, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
                                aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,
-                               tile_w, warps_x);
+                               tile_w, warps_x, pdl);
     else if (G == 4)
         launch_cloud_render<4>(half, occ, grid, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
                                aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,
-                               tile_w, warps_x);
+                               tile_w, warps_x, pdl);
     else if (G == 2)
         launch_cloud_render<2>(half, occ, grid, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
                                aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,
-                               tile_w, warps_x);
+                               tile_w, warps_x, pdl);
     else
         launch_cloud_render<1>(half, occ, grid, stream, C, M, A, T, tlw, tlh, aerial_perspective_luminance,
                                aerial_perspective_transmittance, blue_noise, depth, out, out_distance, counters,
-                               tile_w, warps_x);
+                               tile_w, warps_x, pdl);
     return check_cuda(cudaGetLastError(), "cloud raymarch kernel");
 }
+// The device aliases of the raymarch's host outputs: both must be page-locked
+// host memory mapped into this device's address space, and the kernel then
+// stores through the mapped alias.  Anything else (pageable or device memory)
+// is refused, before any launch.
+int map_host_outputs(void* host_rgba, float* host_distance, void* alias[2]) {
+    void* host[2] = {host_rgba, host_distance};
+    const size_t align[2] = {8, 4};
+    const char* name[2] = {"host_rgba", "host_distance"};
+    for (int k = 0; k < 2; ++k) {
+        alias[k] = nullptr;
+        if (!host[k]) continue;
+        cudaPointerAttributes a{};
+        cudaError_t e = cudaPointerGetAttributes(&a, host[k]);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(SKYR_EINVAL, "%s: not page-locked host memory (%s)", name[k], cudaGetErrorString(e));
+        }
+        if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr)
+            return set_error(SKYR_EINVAL, "%s: not page-locked host memory mapped for the device", name[k]);
+        if (reinterpret_cast<uintptr_t>(a.devicePointer) % align[k] != 0)
+            return set_error(SKYR_EINVAL, "%s: not %zu-byte aligned", name[k], align[k]);
+        alias[k] = a.devicePointer;
+    }
+    return SKYR_OK;
+}
+
 }  // namespace skyr
 
 using namespace skyr;
@@ -494,30 +522,40 @@ int skyr_cloud_render_to_host(skyr_ctx* ctx, const skyr_atmosphere_parameters* a
                               const float* depth, void* host_rgba, float* host_distance) {
     if (!ctx) return set_error(SKYR_EINVAL, "null context");
     if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
-    // Both outputs must be page-locked host memory mapped into this device's
-    // address space; the kernel then stores through the mapped alias.  Anything
-    // else (pageable or device memory) is refused here, before any launch.
     void* alias[2] = {nullptr, nullptr};
-    void* host[2] = {host_rgba, host_distance};
-    const size_t align[2] = {8, 4};
-    const char* name[2] = {"host_rgba", "host_distance"};
-    for (int k = 0; k < 2; ++k) {
-        if (!host[k]) continue;
-        cudaPointerAttributes a{};
-        cudaError_t e = cudaPointerGetAttributes(&a, host[k]);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return set_error(SKYR_EINVAL, "%s: not page-locked host memory (%s)", name[k], cudaGetErrorString(e));
-        }
-        if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr)
-            return set_error(SKYR_EINVAL, "%s: not page-locked host memory mapped for the device", name[k]);
-        if (reinterpret_cast<uintptr_t>(a.devicePointer) % align[k] != 0)
-            return set_error(SKYR_EINVAL, "%s: not %zu-byte aligned", name[k], align[k]);
-        alias[k] = a.devicePointer;
-    }
+    if (int st = map_host_outputs(host_rgba, host_distance, alias)) return st;
     return cloud_render_on(ctx, ctx->stream, atmosphere, cloud, material, textures, view, sizes, transmittance,
                            aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise, depth,
                            alias[0], static_cast<float*>(alias[1]), nullptr);
+}
+
+int skyr_render_frame(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,
+                      const skyr_atmosphere_render_parameters* render, const skyr_lut_sizes* sizes,
+                      void* transmittance, void* multiscattering, void* sky_view_luminance,
+                      void* sky_view_transmittance, void* aerial_perspective_luminance,
+                      void* aerial_perspective_transmittance, const skyr_cloud_parameters* cloud,
+                      const skyr_cloud_material* material, const skyr_cloud_textures* textures,
+                      const skyr_cloud_view* view, const float* blue_noise, const float* depth, void* out_rgba,
+                      float* out_distance, int outputs_on_host) {
+    if (!ctx) return set_error(SKYR_EINVAL, "null context");
+    if (int e = check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice")) return e;
+    void* out[2] = {out_rgba, out_distance};
+    if (outputs_on_host)
+        if (int st = map_host_outputs(out_rgba, out_distance, out)) return st;
+    // the raymarch's arguments are checked before the LUT set is enqueued, so a
+    // rejected call enqueues nothing
+    if (int st = cloud_render_on(ctx, ctx->stream, atmosphere, cloud, material, textures, view, sizes, transmittance,
+                                 aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise, depth,
+                                 out[0], static_cast<float*>(out[1]), nullptr, nullptr, kCloudCheckOnly))
+        return st;
+    if (!render) return set_error(SKYR_EINVAL, "null render parameters");
+    if (int st = skyr_update_lut_set(ctx, atmosphere, render, 1, sizes, transmittance, multiscattering,
+                                     sky_view_luminance, sky_view_transmittance, aerial_perspective_luminance,
+                                     aerial_perspective_transmittance))
+        return st;
+    return cloud_render_on(ctx, ctx->stream, atmosphere, cloud, material, textures, view, sizes, transmittance,
+                           aerial_perspective_luminance, aerial_perspective_transmittance, blue_noise, depth, out[0],
+                           static_cast<float*>(out[1]), nullptr, nullptr, kCloudAfterLuts);
 }
 
 int skyr_cloud_render_counted(skyr_ctx* ctx, const skyr_atmosphere_parameters* atmosphere,

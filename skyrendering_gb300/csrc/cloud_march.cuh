@@ -319,6 +319,11 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(const __grid_co
                                          ph_back, ph_fwd, mk, sub, gmask);
     }
 
+    // The LUTs are first read here.  A raymarch launched as a programmatic
+    // dependent of the view-LUT pass (skyr_render_frame) marches while the LUT
+    // passes finish and waits here for them to complete; for any other launch
+    // this is a no-op.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     float avg_t = mk.wsum == 0.f ? frag_dist : mk.wsum / mk.trans_sum;
     float3 ap = C.cam + view * avg_t;
     // GetSunVisibility(transmittance_texture, pos) at the mean depth
@@ -377,7 +382,7 @@ __global__ void __launch_bounds__(128, MINB) cloud_render_kernel(const __grid_co
 }
 
 // Launches the raymarch kernel for G lanes per ray and the register cut MINB
-// (resident blocks per SM: 5, 6, 7 or 8) with the LUT storage type (half:
+// (resident blocks per SM: 5 to 10) with the LUT storage type (half:
 // RGBA16F, else RGBA32F) and the density evaluation M.fast_ok selects.  Every (G, MINB) pair is instantiated in one of the
 // cloud_raymarch_l<G>_c<cuts>.cu translation units, two cuts per unit, so the
 // kernel variants compile in parallel.
@@ -386,12 +391,24 @@ void launch_cloud_render_cut(bool half, dim3 grid, cudaStream_t stream, const Cl
                              const MaterialConsts& M, const AtmoConsts& A, const float4* tlut, int tw, int th,
                              const void* ap_lum, const void* ap_trans, const float* blue_noise, const float* depth,
                              __half2* out_rgba, float* out_dist, unsigned long long* counters, int tile_w,
-                             int warps_x) {
+                             int warps_x, bool pdl) {
+    // pdl: a programmatic dependent launch (programmatic stream serialisation),
+    // whose blocks may start before the previous kernel on the stream ends
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
     auto go = [&](auto tag, auto fast) {
         using S = decltype(tag);
-        cloud_render_kernel<S, MINB, G, false, decltype(fast)::value><<<grid, 128, 0, stream>>>(
-            C, M, A, tlut, tw, th, reinterpret_cast<const S*>(ap_lum), reinterpret_cast<const S*>(ap_trans),
-            blue_noise, depth, out_rgba, out_dist, counters, tile_w, warps_x);
+        cudaLaunchKernelEx(&cfg, cloud_render_kernel<S, MINB, G, false, decltype(fast)::value>, C, M, A, tlut, tw, th,
+                           reinterpret_cast<const S*>(ap_lum), reinterpret_cast<const S*>(ap_trans), blue_noise,
+                           depth, out_rgba, out_dist, counters, tile_w, warps_x);
     };
     using Fast = std::true_type;
     using General = std::false_type;
@@ -408,7 +425,7 @@ void launch_cloud_render_cut(bool half, dim3 grid, cudaStream_t stream, const Cl
     void launch_cloud_render_cut<G, B>(bool, dim3, cudaStream_t, const CloudConsts&, const MaterialConsts&,    \
                                        const AtmoConsts&, const float4*, int, int, const void*, const void*,   \
                                        const float*, const float*, __half2*, float*, unsigned long long*, int, \
-                                       int)
+                                       int, bool)
 #define SKYR_CLOUD_CUTS(X, G) X(G, 5); X(G, 6); X(G, 7); X(G, 8); X(G, 9); X(G, 10)
 #define SKYR_CLOUD_CUT_EXTERN(G, B) extern template SKYR_CLOUD_CUT_SIGNATURE(G, B)
 SKYR_CLOUD_CUTS(SKYR_CLOUD_CUT_EXTERN, 1);
@@ -430,11 +447,11 @@ void launch_cloud_render(bool half, int blocks_per_sm, dim3 grid, cudaStream_t s
                          const MaterialConsts& M, const AtmoConsts& A, const float4* tlut, int tw, int th,
                          const void* ap_lum, const void* ap_trans, const float* blue_noise, const float* depth,
                          __half2* out_rgba, float* out_dist, unsigned long long* counters, int tile_w,
-                         int warps_x) {
+                         int warps_x, bool pdl) {
     auto cut = [&](auto minb) {
         launch_cloud_render_cut<G, decltype(minb)::value>(half, grid, stream, C, M, A, tlut, tw, th, ap_lum,
                                                           ap_trans, blue_noise, depth, out_rgba, out_dist,
-                                                          counters, tile_w, warps_x);
+                                                          counters, tile_w, warps_x, pdl);
     };
     switch (blocks_per_sm) {
         case 10: cut(std::integral_constant<int, 10>{}); break;

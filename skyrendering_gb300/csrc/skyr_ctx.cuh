@@ -54,14 +54,19 @@ int derive_jobs(const skyr_atmosphere_parameters* params, const skyr_atmosphere_
 int launch_lut_passes(skyr_ctx* ctx, const LutSetJob* table, int n, const skyr_lut_sizes& s, bool do_view, void* T,
                       void* MS, void* svl, void* svt, void* apl, void* apt);
 // Cloud raymarch of one view on `stream` (cloud.cu); the launch shape from the
-// context's tuning.
+// context's tuning.  `mode`: kCloudCheckOnly validates the arguments and
+// derives the launch constants without launching; kCloudAfterLuts launches the
+// full-resolution raymarch as a programmatic dependent of the view-LUT pass
+// that the stream ran just before it (skyr_render_frame).
+constexpr int kCloudCheckOnly = 1;
+constexpr int kCloudAfterLuts = 2;
 int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_parameters* atmosphere,
                     const skyr_cloud_parameters* cloud, const skyr_cloud_material* material,
                     const skyr_cloud_textures* textures, const skyr_cloud_view* view, const skyr_lut_sizes* sizes,
                     const void* transmittance, const void* aerial_perspective_luminance,
                     const void* aerial_perspective_transmittance, const float* blue_noise, const float* depth,
                     void* out_rgba, float* out_distance, unsigned long long* counters,
-                    const struct CloudCheckerboard* checkerboard = nullptr);
+                    const struct CloudCheckerboard* checkerboard = nullptr, int mode = 0);
 // Create the internal streams / events of a context if needed.
 int ensure_aux_streams(skyr_ctx* ctx);
 }  // namespace skyr

@@ -386,3 +386,125 @@ def _replay_to_host(ctx, B):
             assert torch.equal(dist.view(torch.int32), f.dist.cpu().view(torch.int32))
     finally:
         cap.graph.close()
+
+
+def _luts_bits(luts):
+    return {k: getattr(luts, k).clone() for k in ("transmittance", "multiscattering", "sky_view_luminance",
+                                                   "sky_view_transmittance", "aerial_perspective_luminance",
+                                                   "aerial_perspective_transmittance")}
+
+
+@pytest.mark.parametrize("fmt,size", [(0, None), (1, (481, 271))])
+def test_render_frame_is_the_two_calls(ctx, fmt, size):
+    """skyr_render_frame (the raymarch a programmatic dependent of the LUT
+    set's last pass) writes the LUT set and the frame of skyr_update_lut_set +
+    skyr_cloud_render bit for bit: RGBA32F at 1080p, RGBA16F at a ragged size,
+    device and pinned host outputs, two calls in a row."""
+    from skyrendering_gb300.atmosphere import LutSet
+
+    cam = W.frame_camera() if size is None else W.Camera(pitch=10.0, width=size[0], height=size[1])
+    f = Frame(ctx, cam, 45.0, fmt=fmt)
+    want = _luts_bits(f.luts)
+    luts = LutSet.allocate(f.sizes, 1)
+    for k in want:
+        getattr(luts, k).fill_(float("nan"))
+    rgba = torch.full(tuple(f.rgba.shape), float("nan"), dtype=torch.float16, device="cuda")
+    dist = torch.full(tuple(f.dist.shape), float("nan"), dtype=torch.float32, device="cuda")
+    hrgba = torch.full(tuple(f.rgba.shape), float("nan"), dtype=torch.float16, pin_memory=True)
+    hdist = torch.full(tuple(f.dist.shape), float("nan"), dtype=torch.float32, pin_memory=True)
+    for _ in range(2):
+        f.vc.render_frame(f.atmo, f.render, f.view, f.sizes, luts, f.bn, out_rgba=rgba, out_distance=dist)
+        f.vc.render_frame(f.atmo, f.render, f.view, f.sizes, luts, f.bn, out_rgba=hrgba, out_distance=hdist,
+                          on_host=True)
+        ctx.synchronize()
+        for k, t in want.items():
+            assert torch.equal(getattr(luts, k).view(torch.int16), t.view(torch.int16)), k
+        assert torch.equal(rgba.view(torch.int16), f.rgba.view(torch.int16))
+        assert torch.equal(dist.view(torch.int32), f.dist.view(torch.int32))
+        assert torch.equal(hrgba.view(torch.int16), f.rgba.cpu().view(torch.int16))
+        assert torch.equal(hdist.view(torch.int32), f.dist.cpu().view(torch.int32))
+        rgba.fill_(float("nan"))
+        hrgba.fill_(float("nan"))
+
+
+def test_render_frame_replays_from_a_graph(cuda):
+    """skyr_render_frame captured into a CUDA graph (its programmatic edge
+    between the view-LUT pass and the raymarch captured with it) and replayed
+    twice gives the two calls' frame each time."""
+    from skyrendering_gb300 import batch as B
+    from skyrendering_gb300.atmosphere import Context, LutSet
+
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ctx = Context(s)
+        try:
+            cam = W.Camera(pitch=10.0, width=640, height=360)
+            f = Frame(ctx, cam, 30.0)
+            luts = LutSet.allocate(f.sizes, 1)
+            rgba = torch.empty_like(f.rgba)
+            dist = torch.empty_like(f.dist)
+            with B.capture(ctx) as cap:
+                f.vc.render_frame(f.atmo, f.render, f.view, f.sizes, luts, f.bn, out_rgba=rgba, out_distance=dist)
+            try:
+                for _ in range(2):
+                    rgba.fill_(float("nan"))
+                    luts.aerial_perspective_luminance.fill_(float("nan"))
+                    cap.graph.launch()
+                    ctx.synchronize()
+                    assert torch.equal(rgba.view(torch.int16), f.rgba.view(torch.int16))
+                    assert torch.equal(dist.view(torch.int32), f.dist.view(torch.int32))
+                    assert torch.equal(luts.aerial_perspective_luminance, f.luts.aerial_perspective_luminance)
+            finally:
+                cap.graph.close()
+        finally:
+            ctx.close()
+
+
+def test_render_frame_checks_everything_before_it_enqueues(ctx):
+    """Arguments the raymarch or the LUT set would refuse are refused before
+    anything is enqueued: the LUT buffers keep their contents."""
+    from skyrendering_gb300.atmosphere import LutSet
+
+    import ctypes as C
+
+    from skyrendering_gb300.atmosphere import _ptr
+
+    cam = W.Camera(pitch=10.0, width=64, height=36)
+    f = Frame(ctx, cam, 45.0)
+    luts = LutSet.allocate(f.sizes, 1)
+    for k in _luts_bits(luts):
+        getattr(luts, k).fill_(7.0)
+    lib = _abi.lib()
+
+    def call(view=None, ap=True, bn=True, atmo=None):
+        L = luts
+        return lib.skyr_render_frame(
+            ctx.handle, C.byref(atmo or f.atmo), C.byref(f.render), C.byref(f.sizes), _ptr(L.transmittance),
+            _ptr(L.multiscattering), _ptr(L.sky_view_luminance), _ptr(L.sky_view_transmittance),
+            _ptr(L.aerial_perspective_luminance) if ap else None,
+            _ptr(L.aerial_perspective_transmittance) if ap else None, C.byref(f.vc.params),
+            C.byref(f.vc.material), C.byref(f.vc.textures), C.byref(view or f.view), _ptr(f.bn) if bn else None,
+            None, _ptr(f.rgba), _ptr(f.dist), 0)
+
+    assert call(ap=False) == _abi.SKYR_EINVAL
+    assert call(bn=False) == _abi.SKYR_EINVAL
+    bad_view = W.frame_view(cam, 45.0, width=64, height=36)
+    bad_view.width = 0
+    assert call(view=bad_view) == _abi.SKYR_EINVAL
+    bad_atmo = W.earth_like_atmosphere()
+    bad_atmo.bottom_radius = float("nan")
+    assert call(atmo=bad_atmo) == _abi.SKYR_EINVAL
+    # device outputs refused as host outputs
+    assert lib.skyr_render_frame(
+        ctx.handle, C.byref(f.atmo), C.byref(f.render), C.byref(f.sizes), _ptr(luts.transmittance),
+        _ptr(luts.multiscattering), _ptr(luts.sky_view_luminance), _ptr(luts.sky_view_transmittance),
+        _ptr(luts.aerial_perspective_luminance), _ptr(luts.aerial_perspective_transmittance),
+        C.byref(f.vc.params), C.byref(f.vc.material), C.byref(f.vc.textures), C.byref(f.view), _ptr(f.bn), None,
+        _ptr(f.rgba), _ptr(f.dist), 1) == _abi.SKYR_EINVAL
+    ctx.synchronize()
+    for k in _luts_bits(luts):
+        assert bool((getattr(luts, k).float() == 7.0).all()), k
+    # and a valid call then renders
+    assert call() == _abi.SKYR_OK
+    ctx.synchronize()
+    assert torch.equal(luts.transmittance, f.luts.transmittance)
