@@ -470,11 +470,12 @@ int cloud_render_on(skyr_ctx* ctx, cudaStream_t stream, const skyr_atmosphere_pa
                                tile_w, warps_x, pdl);
     return check_cuda(cudaGetLastError(), "cloud raymarch kernel");
 }
+
 // The device aliases of the raymarch's host outputs: both must be page-locked
 // host memory mapped into this device's address space, and the kernel then
 // stores through the mapped alias.  Anything else (pageable or device memory)
 // is refused, before any launch.
-int map_host_outputs(void* host_rgba, float* host_distance, void* alias[2]) {
+static int map_host_outputs(void* host_rgba, float* host_distance, void* alias[2]) {
     void* host[2] = {host_rgba, host_distance};
     const size_t align[2] = {8, 4};
     const char* name[2] = {"host_rgba", "host_distance"};
