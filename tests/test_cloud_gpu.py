@@ -508,3 +508,34 @@ def test_render_frame_checks_everything_before_it_enqueues(ctx):
     assert call() == _abi.SKYR_OK
     ctx.synchronize()
     assert torch.equal(luts.transmittance, f.luts.transmittance)
+
+
+def test_render_frame_with_depth_and_froxel(ctx):
+    """skyr_render_frame with a depth buffer written just before the call and
+    the view's shadow froxel: the raymarch reads the depth before its wait for
+    the LUT set and the froxel after it; the frame is the two calls' frame."""
+    from skyrendering_gb300.atmosphere import LutSet
+    from skyrendering_gb300.cloud import CloudShadow, shadow_sizes
+
+    cam = W.Camera(pitch=10.0, width=480, height=270)
+    f = Frame(ctx, cam, 30.0)
+    ss = shadow_sizes(f.view.viewport_width, f.view.viewport_height)
+    sh = CloudShadow(ctx, ss)
+    sh.render(f.vc, f.atmo, f.view, f.bn)
+    sh.attach(f.view)
+    depth = torch.ones((270, 480), dtype=torch.float32, device="cuda")
+    want_rgba, want_dist = f.vc.render(f.atmo, f.view, f.sizes, f.luts, f.bn, depth=depth)
+    ctx.synchronize()
+    luts = LutSet.allocate(f.sizes, 1)
+    rgba = torch.full_like(want_rgba, float("nan"))
+    dist = torch.full_like(want_dist, float("nan"))
+    for k in range(2):
+        depth.fill_(1.0)
+        depth[:90] = 0.9995  # geometry in the lower third, written on the stream right before the call
+        if k == 0:
+            want_rgba, want_dist = f.vc.render(f.atmo, f.view, f.sizes, f.luts, f.bn, depth=depth)
+        f.vc.render_frame(f.atmo, f.render, f.view, f.sizes, luts, f.bn, depth=depth, out_rgba=rgba,
+                          out_distance=dist)
+        ctx.synchronize()
+        assert torch.equal(rgba.view(torch.int16), want_rgba.view(torch.int16)), k
+        assert torch.equal(dist.view(torch.int32), want_dist.view(torch.int32)), k
